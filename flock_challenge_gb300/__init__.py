@@ -1,0 +1,137 @@
+"""GB300-native (sm_103a) prover hot path for batched BLAKE3 compressions.
+
+Host-side mirror of the reference's prover entry points
+(crates/flock-prover/src/r1cs_hashes/blake3.rs `Blake3Setup`, and
+crates/flock-core/src/pcs/commit.rs `commit`) over the C ABI of
+include/flock_gpu.h, implemented by libflock_gpu.so (CUDA, built in-tree).
+
+There is no CPU fallback: importing the native library fails loudly when it
+is missing or cannot be loaded.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_LIB = None
+
+COMPRESSION_DTYPE = np.dtype([("cv", "<u4", 8), ("m", "<u4", 16), ("counter", "<u8"),
+                              ("block_len", "<u4"), ("flags", "<u4")])
+assert COMPRESSION_DTYPE.itemsize == 112
+
+FLOCK_OK = 0
+_ERRORS = {-1: "shape", -2: "cuda", -3: "out of memory", -4: "argument", -5: "capacity",
+           -6: "timeout", -7: "verify"}
+
+
+class FlockError(RuntimeError):
+    pass
+
+
+def check(rc, what="flock call"):
+    if rc != FLOCK_OK:
+        raise FlockError(f"{what} failed: {_ERRORS.get(rc, rc)} ({rc})")
+
+
+def lib_path():
+    return _build.LIB
+
+
+def lib(build_if_missing=True):
+    """Loads libflock_gpu.so (building it first when sources are newer)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if build_if_missing:
+        _build.build()
+    if not os.path.exists(_build.LIB):
+        raise FlockError(f"native library missing: {_build.LIB}")
+    L = ctypes.CDLL(_build.LIB)
+    P, sz, i32 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int
+    L.flock_version.restype = ctypes.c_char_p
+    L.flock_create.argtypes = [i32, sz, ctypes.POINTER(P)]
+    L.flock_destroy.argtypes = [P]
+    L.flock_witness.argtypes = [P, sz, i32, P, P, P, P, P]
+    L.flock_ntt.argtypes = [P, P, i32, i32, i32, P]
+    L.flock_merkle_tree.argtypes = [P, sz, sz, P, P]
+    L.flock_commit.argtypes = [P, P, i32, i32, i32, P, P, P, P]
+    _LIB = L
+    return L
+
+
+class Context:
+    """Device context (flock_create / flock_destroy)."""
+
+    def __init__(self, device=0, hbm_budget=0):
+        self._h = ctypes.c_void_p()
+        check(lib().flock_create(device, hbm_budget, ctypes.byref(self._h)), "flock_create")
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            lib().flock_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _dptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream_ptr(stream):
+    return ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
+
+
+def generate_witness(d_blocks, n, n_blocks_log, want_ab=True, want_stripe=True, stream=None):
+    """Witness (z, a, b, stripe) on the device for n compressions in 2^n_blocks_log slots.
+
+    d_blocks: uint8 CUDA tensor of n * 112 bytes (flock_compression records).
+    Returns torch uint8 CUDA tensors (a/b/stripe None when not requested).
+    """
+    import torch
+    m = 14 + n_blocks_log
+    nbytes = (1 << m) // 8
+    dev = d_blocks.device
+    z = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    a = torch.empty(nbytes, dtype=torch.uint8, device=dev) if want_ab else None
+    b = torch.empty(nbytes, dtype=torch.uint8, device=dev) if want_ab else None
+    s = torch.empty(nbytes, dtype=torch.uint8, device=dev) if want_stripe else None
+    check(lib().flock_witness(_dptr(d_blocks), n, n_blocks_log, _dptr(z), _dptr(a), _dptr(b), _dptr(s),
+                              _stream_ptr(stream)), "flock_witness")
+    return z, a, b, s
+
+
+def commit(ctx, d_z, m, log_inv_rate=1, log_batch_size=6, stream=None):
+    """PCS commit on the device: returns (root bytes, codeword tensor, tree tensor)."""
+    import torch
+    log_d = m - 7 - log_batch_size + log_inv_rate
+    cw = torch.empty((1 << (log_d + log_batch_size)) * 16, dtype=torch.uint8, device=d_z.device)
+    tree = torch.empty((2 * (1 << log_d) - 1) * 32, dtype=torch.uint8, device=d_z.device)
+    root = (ctypes.c_uint8 * 32)()
+    check(lib().flock_commit(ctx.handle, _dptr(d_z), m, log_inv_rate, log_batch_size, _dptr(cw), _dptr(tree),
+                             root, _stream_ptr(stream)), "flock_commit")
+    return bytes(root), cw, tree
+
+
+def ntt(ctx, d_data, log_d, log_num_ntts, start_layer=0, stream=None):
+    check(lib().flock_ntt(ctx.handle, _dptr(d_data), log_d, log_num_ntts, start_layer, _stream_ptr(stream)),
+          "flock_ntt")
+
+
+def merkle_tree(d_data, n_leaves, leaf_bytes, stream=None):
+    import torch
+    tree = torch.empty((2 * n_leaves - 1) * 32, dtype=torch.uint8, device=d_data.device)
+    check(lib().flock_merkle_tree(_dptr(d_data), n_leaves, leaf_bytes, _dptr(tree), _stream_ptr(stream)),
+          "flock_merkle_tree")
+    return tree

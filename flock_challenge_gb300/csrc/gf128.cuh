@@ -1,0 +1,118 @@
+// GF(2^128) arithmetic on the device.
+//
+// Field: polynomial basis modulo x^128 + x^7 + x^2 + x + 1 (the reference's
+// GHASH form, crates/flock-core/src/field/gf2_128.rs:1-135). An element is
+// four little-endian 32-bit limbs, limb 0 holding x^0..x^31.
+//
+// The GPU has no carry-less multiply instruction. A 32x32 carry-less product
+// is formed from sixteen 32x32->64 integer multiplies of operands masked to
+// every fourth bit: with four-bit spacing each output position sums at most
+// eight partial bits, so the count never carries into the next position of
+// the same residue class, and masking the residue keeps exactly the parity.
+// 128x128 uses two levels of Karatsuba (nine 32-bit products) and the
+// reference's fold of the upper half (gf2_128.rs:192-216).
+#pragma once
+#include <cstdint>
+
+struct __align__(16) gf128 {
+  uint32_t w[4];
+};
+
+__host__ __device__ __forceinline__ gf128 gf_zero() { gf128 r; r.w[0] = r.w[1] = r.w[2] = r.w[3] = 0; return r; }
+__host__ __device__ __forceinline__ gf128 gf_one() { gf128 r = gf_zero(); r.w[0] = 1; return r; }
+__host__ __device__ __forceinline__ gf128 gf_add(gf128 a, gf128 b) {
+  gf128 r;
+  r.w[0] = a.w[0] ^ b.w[0]; r.w[1] = a.w[1] ^ b.w[1]; r.w[2] = a.w[2] ^ b.w[2]; r.w[3] = a.w[3] ^ b.w[3];
+  return r;
+}
+__host__ __device__ __forceinline__ bool gf_eq(gf128 a, gf128 b) {
+  return ((a.w[0] ^ b.w[0]) | (a.w[1] ^ b.w[1]) | (a.w[2] ^ b.w[2]) | (a.w[3] ^ b.w[3])) == 0;
+}
+
+__device__ __forceinline__ gf128 gf_load(const void* p) {
+  uint4 v = *reinterpret_cast<const uint4*>(p);
+  gf128 r; r.w[0] = v.x; r.w[1] = v.y; r.w[2] = v.z; r.w[3] = v.w;
+  return r;
+}
+__device__ __forceinline__ void gf_store(void* p, gf128 a) {
+  *reinterpret_cast<uint4*>(p) = make_uint4(a.w[0], a.w[1], a.w[2], a.w[3]);
+}
+
+// 32x32 -> 64 unsigned integer product (one IMAD.WIDE.U32).
+__device__ __forceinline__ uint64_t mulw(uint32_t a, uint32_t b) {
+  uint64_t r;
+  asm("mul.wide.u32 %0, %1, %2;" : "=l"(r) : "r"(a), "r"(b));
+  return r;
+}
+
+// 32x32 -> 64 carry-less product via masked integer multiplies.
+__device__ __forceinline__ uint64_t clmul32(uint32_t a, uint32_t b) {
+  const uint32_t m0 = 0x11111111u, m1 = 0x22222222u, m2 = 0x44444444u, m3 = 0x88888888u;
+  uint32_t a0 = a & m0, a1 = a & m1, a2 = a & m2, a3 = a & m3;
+  uint32_t b0 = b & m0, b1 = b & m1, b2 = b & m2, b3 = b & m3;
+  uint64_t r0 = mulw(a0, b0) ^ mulw(a1, b3) ^ mulw(a2, b2) ^ mulw(a3, b1);
+  uint64_t r1 = mulw(a0, b1) ^ mulw(a1, b0) ^ mulw(a2, b3) ^ mulw(a3, b2);
+  uint64_t r2 = mulw(a0, b2) ^ mulw(a1, b1) ^ mulw(a2, b0) ^ mulw(a3, b3);
+  uint64_t r3 = mulw(a0, b3) ^ mulw(a1, b2) ^ mulw(a2, b1) ^ mulw(a3, b0);
+  return (r0 & 0x1111111111111111ull) | (r1 & 0x2222222222222222ull) | (r2 & 0x4444444444444444ull) |
+         (r3 & 0x8888888888888888ull);
+}
+
+// 64x64 -> 128 carry-less product (Karatsuba over 32-bit halves).
+__device__ __forceinline__ void clmul64(uint64_t a, uint64_t b, uint64_t& lo, uint64_t& hi) {
+  uint32_t al = (uint32_t)a, ah = (uint32_t)(a >> 32), bl = (uint32_t)b, bh = (uint32_t)(b >> 32);
+  uint64_t ll = clmul32(al, bl), hh = clmul32(ah, bh), mm = clmul32(al ^ ah, bl ^ bh);
+  mm ^= ll ^ hh;
+  lo = ll ^ (mm << 32);
+  hi = hh ^ (mm >> 32);
+}
+
+// Fold bits 128..255 back: x^128 = x^7 + x^2 + x + 1.
+__device__ __forceinline__ gf128 gf_reduce(uint64_t r0, uint64_t r1, uint64_t r2, uint64_t r3) {
+  uint64_t t_lo = r2 ^ (r2 << 1) ^ (r2 << 2) ^ (r2 << 7);
+  uint64_t t_hi = r3 ^ ((r3 << 1) | (r2 >> 63)) ^ ((r3 << 2) | (r2 >> 62)) ^ ((r3 << 7) | (r2 >> 57));
+  uint64_t ov = (r3 >> 63) ^ (r3 >> 62) ^ (r3 >> 57);
+  uint64_t corr = ov ^ (ov << 1) ^ (ov << 2) ^ (ov << 7);
+  uint64_t lo = r0 ^ t_lo ^ corr, hi = r1 ^ t_hi;
+  gf128 r;
+  r.w[0] = (uint32_t)lo; r.w[1] = (uint32_t)(lo >> 32); r.w[2] = (uint32_t)hi; r.w[3] = (uint32_t)(hi >> 32);
+  return r;
+}
+
+// Unreduced 256-bit product (Karatsuba over 64-bit halves).
+struct gf256 {
+  uint64_t r[4];
+};
+__device__ __forceinline__ gf256 gf_mul_wide(gf128 a, gf128 b) {
+  uint64_t alo = a.w[0] | ((uint64_t)a.w[1] << 32), ahi = a.w[2] | ((uint64_t)a.w[3] << 32);
+  uint64_t blo = b.w[0] | ((uint64_t)b.w[1] << 32), bhi = b.w[2] | ((uint64_t)b.w[3] << 32);
+  uint64_t l0, l1, h0, h1, m0, m1;
+  clmul64(alo, blo, l0, l1);
+  clmul64(ahi, bhi, h0, h1);
+  clmul64(alo ^ ahi, blo ^ bhi, m0, m1);
+  m0 ^= l0 ^ h0;
+  m1 ^= l1 ^ h1;
+  gf256 o;
+  o.r[0] = l0;
+  o.r[1] = l1 ^ m0;
+  o.r[2] = h0 ^ m1;
+  o.r[3] = h1;
+  return o;
+}
+__device__ __forceinline__ void gf256_acc(gf256& acc, const gf256& x) {
+  acc.r[0] ^= x.r[0]; acc.r[1] ^= x.r[1]; acc.r[2] ^= x.r[2]; acc.r[3] ^= x.r[3];
+}
+__device__ __forceinline__ gf128 gf256_reduce(const gf256& x) { return gf_reduce(x.r[0], x.r[1], x.r[2], x.r[3]); }
+
+__device__ __forceinline__ gf128 gf_mul(gf128 a, gf128 b) { return gf256_reduce(gf_mul_wide(a, b)); }
+
+// Multiply by x.
+__device__ __forceinline__ gf128 gf_mul_x(gf128 a) {
+  uint32_t carry = a.w[3] >> 31;
+  gf128 r;
+  r.w[3] = (a.w[3] << 1) | (a.w[2] >> 31);
+  r.w[2] = (a.w[2] << 1) | (a.w[1] >> 31);
+  r.w[1] = (a.w[1] << 1) | (a.w[0] >> 31);
+  r.w[0] = (a.w[0] << 1) ^ (0x87u & (0u - carry));
+  return r;
+}

@@ -1,0 +1,184 @@
+// Interleaved additive NTT over GF(2^128) (LCH novel basis, neighbours-last).
+//
+// Restates AdditiveNttF128::forward_transform_interleaved_from_layer
+// (crates/flock-core/src/ntt/additive_ntt_f128.rs:599-622, scalar form at
+// :1281-1312): data[pos * num_ntts + lane]; at layer l the pair distance is
+// 2^(log_d-l-1) positions and block b = pos >> (log_d - l) uses twiddle
+// t(l, b) = table[2^l - 1 + b]; butterfly u += v*t, v += u.
+//
+// GB300 mapping: a pass applies F consecutive layers to a tile of 2^F
+// positions x 16 lanes held in shared memory. The tile's positions differ only
+// in the F pair bits of those layers, so every butterfly of the pass stays in
+// the tile and the pass costs one HBM read and one write of the codeword.
+// Each tile row (16 lanes x 16 B) is a contiguous 256-byte run, read and
+// written with 16-byte vector accesses. A pass may read its input from a
+// separate source with a position mask: the first pass of a rate-1/2^r code
+// reads the message directly, position p taking row p mod 2^(log_d - r), which
+// is the replicated state after the r copy layers (pcs/commit.rs:451-473).
+#include <cstdio>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "flock_internal.h"
+#include "gf128.cuh"
+#include "host_field.h"
+
+namespace {
+
+constexpr int TILE_LANES = 16;
+constexpr int NTT_THREADS = 256;
+
+template <int F>
+__global__ void __launch_bounds__(NTT_THREADS)
+ntt_pass_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t src_pos_mask,
+                const gf128* __restrict__ tw, int log_d, int log_lanes, int l0) {
+  __shared__ gf128 tile[(1 << F) * TILE_LANES];
+  const int lane_groups = (1 << log_lanes) / TILE_LANES;
+  const size_t tile_id = blockIdx.x / lane_groups;
+  const int lg = blockIdx.x % lane_groups;
+  const int lo_bits = log_d - l0 - F;
+  const size_t lo = tile_id & (((size_t)1 << lo_bits) - 1);
+  const size_t hi = tile_id >> lo_bits;
+  const size_t nl = (size_t)1 << log_lanes;
+
+  // Load 2^F rows of 16 lanes.
+  for (int e = threadIdx.x; e < (1 << F) * TILE_LANES; e += NTT_THREADS) {
+    int i = e / TILE_LANES, ln = e % TILE_LANES;
+    size_t p = (hi << (log_d - l0)) | ((size_t)i << lo_bits) | lo;
+    size_t sp = p & src_pos_mask;
+    tile[e] = gf_load(&src[sp * nl + (size_t)lg * TILE_LANES + ln]);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int s = 0; s < F; s++) {
+    const int pb = F - 1 - s;  // pair bit inside the tile index
+    for (int e = threadIdx.x; e < (1 << (F - 1)) * TILE_LANES; e += NTT_THREADS) {
+      int pair = e / TILE_LANES, ln = e % TILE_LANES;
+      int i0 = ((pair >> pb) << (pb + 1)) | (pair & ((1 << pb) - 1));
+      int i1 = i0 | (1 << pb);
+      size_t blk = (hi << s) | ((size_t)i0 >> (F - s));
+      gf128 t = gf_load(&tw[(((size_t)1) << (l0 + s)) - 1 + blk]);
+      gf128 u = tile[i0 * TILE_LANES + ln], v = tile[i1 * TILE_LANES + ln];
+      u = gf_add(u, gf_mul(v, t));
+      v = gf_add(v, u);
+      tile[i0 * TILE_LANES + ln] = u;
+      tile[i1 * TILE_LANES + ln] = v;
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < (1 << F) * TILE_LANES; e += NTT_THREADS) {
+    int i = e / TILE_LANES, ln = e % TILE_LANES;
+    size_t p = (hi << (log_d - l0)) | ((size_t)i << lo_bits) | lo;
+    gf_store(&dst[p * nl + (size_t)lg * TILE_LANES + ln], tile[e]);
+  }
+}
+
+// Twiddle table of the standard basis {1, x, ..., x^(d-1)}:
+// normalized subspace-polynomial evaluations (additive_ntt_f128.rs:57-88),
+// expanded breadth-first (additive_ntt_f128.rs:106-129).
+std::vector<hf::F> host_twiddles(int d) {
+  std::vector<std::vector<hf::F>> ev(d);
+  for (int i = 0; i < d; i++) ev[0].push_back(i < 64 ? hf::F(1ULL << i, 0) : hf::F(0, 1ULL << (i - 64)));
+  for (int i = 1; i < d; i++)
+    for (size_t k = 1; k < ev[i - 1].size(); k++) ev[i].push_back(ev[i - 1][k] * (ev[i - 1][k] + ev[i - 1][0]));
+  for (auto& row : ev) {
+    hf::F iv = hf::inv(row[0]);
+    for (auto& v : row) v = v * iv;
+  }
+  std::vector<hf::F> tw;
+  tw.reserve(((size_t)1 << d) - 1);
+  for (int layer = 0; layer < d; layer++) {
+    size_t start = tw.size();
+    const auto& row = ev[d - layer - 1];
+    tw.push_back(hf::F());
+    for (size_t bit = 0; bit + 1 < row.size(); bit++) {
+      size_t half = (size_t)1 << bit;
+      for (size_t b = 0; b < half; b++) tw.push_back(tw[start + b] + row[bit + 1]);
+    }
+  }
+  return tw;
+}
+
+std::mutex g_tw_mu;
+std::map<std::pair<int, int>, void*> g_tw;  // (device, log_d) -> device table
+
+template <int F>
+int launch_pass(gf128* dst, const gf128* src, size_t mask, const gf128* tw, int log_d, int log_lanes, int l0,
+                cudaStream_t st) {
+  size_t tiles = (size_t)1 << (log_d - F);
+  size_t blocks = tiles * ((1 << log_lanes) / TILE_LANES);
+  ntt_pass_kernel<F><<<(unsigned)blocks, NTT_THREADS, 0, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int run_pass(int f, gf128* dst, const gf128* src, size_t mask, const gf128* tw, int log_d, int log_lanes, int l0,
+             cudaStream_t st) {
+  switch (f) {
+    case 1: return launch_pass<1>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 2: return launch_pass<2>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 3: return launch_pass<3>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 4: return launch_pass<4>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 5: return launch_pass<5>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 6: return launch_pass<6>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    default: return FLOCK_ERR_SHAPE;
+  }
+}
+
+}  // namespace
+
+const void* flock_ntt_twiddles(int log_d) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_tw_mu);
+  auto key = std::make_pair(dev, log_d);
+  auto it = g_tw.find(key);
+  if (it != g_tw.end()) return it->second;
+  std::vector<hf::F> tw = host_twiddles(log_d);
+  void* d = nullptr;
+  if (cudaMalloc(&d, tw.size() * 16 + 16) != cudaSuccess) return nullptr;
+  if (cudaMemcpy(d, tw.data(), tw.size() * 16, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(d);
+    return nullptr;
+  }
+  g_tw[key] = d;
+  return d;
+}
+
+// Applies layers [start_layer, log_d) in passes of up to 6 layers. d_src (may
+// equal d_data) holds the input rows addressed with position mask
+// 2^(log_d - start_layer) - 1, so a distinct d_src supplies the replicated
+// message of a rate-1/2^start_layer code.
+int flock_launch_ntt(void* d_data, const void* d_src, int log_d, int log_lanes, int start_layer,
+                     cudaStream_t stream) {
+  if (log_lanes < 4 || log_lanes > 10 || log_d < 1 || log_d > 30 || start_layer < 0 || start_layer > log_d)
+    return FLOCK_ERR_SHAPE;
+  const gf128* tw = (const gf128*)flock_ntt_twiddles(log_d);
+  if (!tw) return FLOCK_ERR_OOM;
+  gf128* data = (gf128*)d_data;
+  const gf128* src = d_src ? (const gf128*)d_src : data;
+  size_t mask = d_src ? ((size_t)1 << (log_d - start_layer)) - 1 : ~(size_t)0;
+  if (start_layer == log_d) {
+    // No layers left: the output is the replicated source.
+    if (src != data) {
+      size_t row_bytes = ((size_t)1 << log_lanes) * 16;
+      size_t chunk = (mask + 1) * row_bytes;
+      for (size_t off = 0; off < ((size_t)1 << log_d) * row_bytes; off += chunk)
+        if (cudaMemcpyAsync((char*)data + off, src, chunk, cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
+          return FLOCK_ERR_CUDA;
+    }
+    return FLOCK_OK;
+  }
+  int remaining = log_d - start_layer;
+  int passes = (remaining + 5) / 6;
+  int l = start_layer;
+  for (int q = 0; q < passes; q++) {
+    int f = (remaining - (l - start_layer) + (passes - q) - 1) / (passes - q);
+    int rc = run_pass(f, data, src, mask, tw, log_d, log_lanes, l, stream);
+    if (rc != FLOCK_OK) return rc;
+    src = data;
+    mask = ~(size_t)0;
+    l += f;
+  }
+  return FLOCK_OK;
+}

@@ -1,0 +1,94 @@
+/*
+ * flock_gpu.h - C ABI of the GB300 (sm_103a) prover for batched BLAKE3
+ * compressions (Flock: R1CS over GF(2), zerocheck + lincheck + Ligerito PCS).
+ *
+ * Plain C types only: host pointers, device pointers (void*), sizes and
+ * cudaStream_t passed as void*. Every function returns an int status
+ * (FLOCK_OK = 0, negative on error) and never throws across the boundary.
+ *
+ * Each entry point names the reference interface it replaces (paths relative
+ * to the Layr-Labs/flock-challenge project root).
+ */
+#ifndef FLOCK_GPU_H
+#define FLOCK_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  FLOCK_OK = 0,
+  FLOCK_ERR_SHAPE = -1,   /* size / shape outside the supported range */
+  FLOCK_ERR_CUDA = -2,    /* a CUDA call failed */
+  FLOCK_ERR_OOM = -3,     /* device allocation failed / over budget */
+  FLOCK_ERR_ARG = -4,     /* null or inconsistent argument */
+  FLOCK_ERR_CAPACITY = -5,/* output buffer too small */
+  FLOCK_ERR_TIMEOUT = -6, /* a bounded device wait expired */
+  FLOCK_ERR_VERIFY = -7   /* an internal consistency check failed */
+};
+
+/* One BLAKE3 compression input (112 bytes). Mirrors the reference tuple
+ * `Compression = ([u32; 8], [u32; 16], u64, u32, u32)` of
+ * crates/flock-prover/src/r1cs_hashes/blake3.rs:1087 and the benchmark's
+ * RawCompression (benchmark-tools/common/src/lib.rs:1). */
+typedef struct flock_compression {
+  uint32_t cv[8];
+  uint32_t m[16];
+  uint64_t counter;
+  uint32_t block_len;
+  uint32_t flags;
+} flock_compression;
+
+typedef struct flock_ctx flock_ctx;
+
+/* Library version string. */
+const char* flock_version(void);
+
+/* Create / destroy a device context bound to `device`. `hbm_budget` bounds the
+ * device memory the context may hold (0 = no limit).
+ * Replaces the process-level setup of the reference worker
+ * (benchmark-tools/worker/src/main.rs:45-57) and the Metal context of
+ * crates/flock-core/src/gpu_commit.rs:1454-1478. */
+int flock_create(int device, size_t hbm_budget, flock_ctx** out);
+void flock_destroy(flock_ctx* ctx);
+
+/* ---- Stage entry points on device buffers ------------------------------ */
+
+/* Witness generation for 2^n_blocks_log compression slots (slots >= n are
+ * the all-zero padding compression). d_in: n device records. Outputs
+ * (device): z, a, b each 2^(n_blocks_log+14)/8 bytes in the packed F128
+ * layout; d_a/d_b may both be null; stripe 2^(n_blocks_log+14)/8 bytes in the
+ * lincheck byte-stripe layout, may be null.
+ * Replaces generate_witness_with_ab_packed_and_lincheck
+ * (crates/flock-prover/src/r1cs_hashes/blake3.rs:2948-3180). */
+int flock_witness(const flock_compression* d_in, size_t n, int n_blocks_log, void* d_z, void* d_a,
+                  void* d_b, void* d_stripe, void* stream);
+
+/* Interleaved additive NTT (LCH novel basis, standard subspace {1, x, ...})
+ * in place on d_data[pos * num_ntts + lane], 2^log_d positions, from layer
+ * start_layer. Replaces AdditiveNttF128::forward_transform_interleaved_from_layer
+ * (crates/flock-core/src/ntt/additive_ntt_f128.rs:599-622). */
+int flock_ntt(flock_ctx* ctx, void* d_data, int log_d, int log_num_ntts, int start_layer, void* stream);
+
+/* Flat BLAKE3 Merkle tree (leaves first, root last; 2*n_leaves-1 nodes of 32
+ * bytes) over n_leaves equal leaves of leaf_bytes (a multiple of 64, at most
+ * 4096). Replaces merkle::merkle_tree (crates/flock-core/src/merkle.rs:733-765). */
+int flock_merkle_tree(const void* d_data, size_t n_leaves, size_t leaf_bytes, void* d_tree, void* stream);
+
+/* PCS commit of a packed witness d_z (2^(m-7) F128): replicate into
+ * 2^log_inv_rate blocks, NTT from layer log_inv_rate, Merkle over one leaf
+ * per position. d_codeword: 2^(m-7+log_inv_rate) F128; d_tree:
+ * 2*2^(m-7-log_batch_size+log_inv_rate)-1 nodes. root (host, 32 bytes).
+ * Replaces pcs::commit (crates/flock-core/src/pcs/commit.rs:250-289) and the
+ * Metal offload seam commit_l0_or_fallback (crates/flock-core/src/gpu_commit.rs:1467). */
+int flock_commit(flock_ctx* ctx, const void* d_z, int m, int log_inv_rate, int log_batch_size,
+                 void* d_codeword, void* d_tree, uint8_t root[32], void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLOCK_GPU_H */

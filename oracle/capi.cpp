@@ -1,0 +1,126 @@
+// C entry points of the oracle library for the test harness (ctypes).
+// Test infrastructure only.
+#include <cstring>
+
+#include "oracle.h"
+
+using namespace oracle;
+
+extern "C" {
+
+void oracle_gf_mul(const uint64_t* a, const uint64_t* b, uint64_t* out) {
+  F128 r = gf_mul(f128(a[0], a[1]), f128(b[0], b[1]));
+  out[0] = r.lo;
+  out[1] = r.hi;
+}
+void oracle_gf_inv(const uint64_t* a, uint64_t* out) {
+  F128 r = gf_inv(f128(a[0], a[1]));
+  out[0] = r.lo;
+  out[1] = r.hi;
+}
+void oracle_phi8(uint8_t v, uint64_t* out) {
+  F128 r = phi8(v);
+  out[0] = r.lo;
+  out[1] = r.hi;
+}
+uint8_t oracle_gf8_mul(uint8_t a, uint8_t b) { return gf8_mul(a, b); }
+
+void oracle_b3_compress(const uint32_t* cv, const uint32_t* block, uint64_t counter, uint32_t block_len,
+                        uint32_t flags, uint32_t* out16) {
+  b3_compress(cv, block, counter, block_len, flags, out16);
+}
+void oracle_b3_hash(const uint8_t* data, size_t len, uint8_t* out32) { b3_hash(data, len, out32); }
+void oracle_b3_xof(const uint8_t* data, size_t len, uint8_t* out, size_t out_len) {
+  Blake3 h;
+  h.update(data, len);
+  h.finalize_xof(out, out_len);
+}
+void oracle_leaf_cv(const uint8_t* data, size_t len, uint8_t* out32) {
+  Hash32 h = leaf_cv(data, len);
+  memcpy(out32, h.b, 32);
+}
+
+// Compression records are 8+16 u32, u64 counter, u32 block_len, u32 flags
+// (112 bytes, matching the C-ABI flock_compression layout).
+void oracle_generate_compressions(uint32_t log2_size, uint64_t seed, int canary, Compression* out) {
+  auto v = canary ? canary_compressions(log2_size) : generate_compressions(log2_size, seed);
+  memcpy(out, v.data(), v.size() * sizeof(Compression));
+}
+size_t oracle_compression_size() { return sizeof(Compression); }
+
+// z/a/b: 2^(m-7) * 16 bytes each; stripe: 2^m / 8 bytes (may be null).
+void oracle_witness(const Compression* blocks, size_t n, int n_blocks_log, uint64_t* z, uint64_t* a,
+                    uint64_t* b, uint8_t* stripe) {
+  std::vector<Compression> v(blocks, blocks + n);
+  Witness w = build_witness(v, n_blocks_log, stripe != nullptr);
+  size_t bytes = w.z.size() * 16;
+  memcpy(z, w.z.data(), bytes);
+  if (a) memcpy(a, w.a.data(), bytes);
+  if (b) memcpy(b, w.b.data(), bytes);
+  if (stripe) memcpy(stripe, w.stripe.data(), w.stripe.size());
+}
+
+void oracle_statement_digest(int m, uint8_t* out32) {
+  SparseRows A, B;
+  build_matrices(A, B);
+  statement_digest(m, A, B, out32);
+}
+
+// Returns the total nonzero count; fills per-row lengths (K entries each) and,
+// when cols != null, the concatenated column indices of A then B.
+size_t oracle_matrices(uint32_t* a_len, uint32_t* b_len, uint32_t* cols) {
+  SparseRows A, B;
+  build_matrices(A, B);
+  size_t nnz = 0, at = 0;
+  for (int i = 0; i < K; i++) {
+    if (a_len) a_len[i] = (uint32_t)A.rows[i].size();
+    nnz += A.rows[i].size();
+  }
+  for (int i = 0; i < K; i++) {
+    if (b_len) b_len[i] = (uint32_t)B.rows[i].size();
+    nnz += B.rows[i].size();
+  }
+  if (cols) {
+    for (int i = 0; i < K; i++)
+      for (uint32_t c : A.rows[i]) cols[at++] = c;
+    for (int i = 0; i < K; i++)
+      for (uint32_t c : B.rows[i]) cols[at++] = c;
+  }
+  return nnz;
+}
+
+void oracle_ntt_twiddles(int dim, uint64_t* out) {
+  NttF128 ntt(dim);
+  memcpy(out, ntt.twiddles.data(), ntt.twiddles.size() * 16);
+}
+
+void oracle_ntt_interleaved(uint64_t* data, size_t n_total, size_t num_ntts, int start_layer) {
+  size_t n = n_total / num_ntts;
+  int ld = 0;
+  while (((size_t)1 << ld) < n) ld++;
+  NttF128 ntt(ld);
+  ntt.forward_interleaved((F128*)data, n_total, num_ntts, start_layer);
+}
+
+// Flat Merkle tree of n_leaves equal leaves over data (2*n_leaves-1 nodes).
+void oracle_merkle_tree(const uint8_t* data, size_t len, size_t n_leaves, uint8_t* tree_out) {
+  auto t = merkle_tree(data, len, n_leaves);
+  memcpy(tree_out, t.data(), t.size() * 32);
+}
+
+// PCS commit of a packed witness z (2^(m-7) F128). Writes the 32-byte root,
+// and the codeword / flat tree when the pointers are non-null.
+void oracle_commit(const uint64_t* z, int m, int log_inv_rate, int log_batch_size, uint8_t* root,
+                   uint64_t* codeword_out, uint8_t* tree_out) {
+  PcsParams p;
+  p.m = m;
+  p.log_inv_rate = log_inv_rate;
+  p.log_batch_size = log_batch_size;
+  std::vector<F128> zv((const F128*)z, (const F128*)z + ((size_t)1 << (m - 7)));
+  CommitData c = commit(zv, p);
+  memcpy(root, c.root().b, 32);
+  if (codeword_out) memcpy(codeword_out, c.codeword.data(), c.codeword.size() * 16);
+  if (tree_out) memcpy(tree_out, c.tree.data(), c.tree.size() * 32);
+}
+
+}  // extern "C"

@@ -1,0 +1,169 @@
+"""ctypes binding of the CPU oracle (oracle/_build/liboracle.so).
+
+Test infrastructure: used by tests/, __graft_entry__.smoke() and the CPU
+baseline leg of bench.py only. Builds the oracle with make on first use.
+"""
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+LIB_PATH = os.path.join(ORACLE_DIR, "_build", "liboracle.so")
+
+_lock = threading.Lock()
+_lib = None
+
+COMP_DTYPE = np.dtype([("cv", "<u4", 8), ("m", "<u4", 16), ("counter", "<u8"),
+                       ("block_len", "<u4"), ("flags", "<u4")])
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR, "-j8"], check=True)
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = ctypes.CDLL(LIB_PATH)
+            P = ctypes.c_void_p
+            sz = ctypes.c_size_t
+            L.oracle_generate_compressions.argtypes = [ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int, P]
+            L.oracle_compression_size.restype = sz
+            L.oracle_witness.argtypes = [P, sz, ctypes.c_int, P, P, P, P]
+            L.oracle_statement_digest.argtypes = [ctypes.c_int, P]
+            L.oracle_matrices.argtypes = [P, P, P]
+            L.oracle_matrices.restype = sz
+            L.oracle_ntt_twiddles.argtypes = [ctypes.c_int, P]
+            L.oracle_ntt_interleaved.argtypes = [P, sz, sz, ctypes.c_int]
+            L.oracle_merkle_tree.argtypes = [P, sz, sz, P]
+            L.oracle_commit.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P]
+            L.oracle_gf_mul.argtypes = [P, P, P]
+            L.oracle_gf_inv.argtypes = [P, P]
+            L.oracle_phi8.argtypes = [ctypes.c_uint8, P]
+            L.oracle_gf8_mul.argtypes = [ctypes.c_uint8, ctypes.c_uint8]
+            L.oracle_gf8_mul.restype = ctypes.c_uint8
+            L.oracle_b3_compress.argtypes = [P, P, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, P]
+            L.oracle_b3_hash.argtypes = [P, sz, P]
+            L.oracle_b3_xof.argtypes = [P, sz, P, sz]
+            L.oracle_leaf_cv.argtypes = [P, sz, P]
+            assert L.oracle_compression_size() == COMP_DTYPE.itemsize
+            _lib = L
+    return _lib
+
+
+def ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def gf_mul(a, b):
+    out = np.zeros(2, np.uint64)
+    lib().oracle_gf_mul(ptr(np.array(a, np.uint64)), ptr(np.array(b, np.uint64)), ptr(out))
+    return (int(out[0]), int(out[1]))
+
+
+def gf_inv(a):
+    out = np.zeros(2, np.uint64)
+    lib().oracle_gf_inv(ptr(np.array(a, np.uint64)), ptr(out))
+    return (int(out[0]), int(out[1]))
+
+
+def phi8(v):
+    out = np.zeros(2, np.uint64)
+    lib().oracle_phi8(v, ptr(out))
+    return (int(out[0]), int(out[1]))
+
+
+def compressions(log2_size, seed, canary=False):
+    out = np.zeros(1 << log2_size, COMP_DTYPE)
+    lib().oracle_generate_compressions(log2_size, seed, int(canary), ptr(out))
+    return out
+
+
+def witness(blocks, n_blocks_log, want_ab=True, want_stripe=True):
+    m = 14 + n_blocks_log
+    n128 = 1 << (m - 7)
+    z = np.zeros(2 * n128, np.uint64)
+    a = np.zeros(2 * n128, np.uint64) if want_ab else None
+    b = np.zeros(2 * n128, np.uint64) if want_ab else None
+    s = np.zeros((1 << m) // 8, np.uint8) if want_stripe else None
+    blocks = np.ascontiguousarray(blocks)
+    lib().oracle_witness(ptr(blocks), len(blocks), n_blocks_log, ptr(z), ptr(a), ptr(b), ptr(s))
+    return z, a, b, s
+
+
+def statement_digest(m):
+    out = np.zeros(32, np.uint8)
+    lib().oracle_statement_digest(m, ptr(out))
+    return out.tobytes()
+
+
+def matrices():
+    a_len = np.zeros(1 << 14, np.uint32)
+    b_len = np.zeros(1 << 14, np.uint32)
+    nnz = lib().oracle_matrices(ptr(a_len), ptr(b_len), None)
+    cols = np.zeros(nnz, np.uint32)
+    lib().oracle_matrices(ptr(a_len), ptr(b_len), ptr(cols))
+    return a_len, b_len, cols
+
+
+def ntt_twiddles(dim):
+    out = np.zeros(2 * ((1 << dim) - 1), np.uint64)
+    lib().oracle_ntt_twiddles(dim, ptr(out))
+    return out
+
+
+def ntt_interleaved(data_u64, num_ntts, start_layer):
+    d = np.ascontiguousarray(data_u64, dtype=np.uint64).copy()
+    lib().oracle_ntt_interleaved(ptr(d), d.size // 2, num_ntts, start_layer)
+    return d
+
+
+def merkle_tree(data_u8, n_leaves):
+    d = np.ascontiguousarray(data_u8, dtype=np.uint8)
+    out = np.zeros(32 * (2 * n_leaves - 1), np.uint8)
+    lib().oracle_merkle_tree(ptr(d), d.size, n_leaves, ptr(out))
+    return out.reshape(-1, 32)
+
+
+def commit(z_u64, m, log_inv_rate=1, log_batch_size=6, want_codeword=False, want_tree=False):
+    root = np.zeros(32, np.uint8)
+    n_pos = 1 << (m - 7 - log_batch_size + log_inv_rate)
+    cw = np.zeros(2 * n_pos * (1 << log_batch_size), np.uint64) if want_codeword else None
+    tree = np.zeros(32 * (2 * n_pos - 1), np.uint8) if want_tree else None
+    z = np.ascontiguousarray(z_u64, dtype=np.uint64)
+    lib().oracle_commit(ptr(z), m, log_inv_rate, log_batch_size, ptr(root), ptr(cw), ptr(tree))
+    return root.tobytes(), cw, (tree.reshape(-1, 32) if tree is not None else None)
+
+
+def b3_compress(cv, block, counter, block_len, flags):
+    out = np.zeros(16, np.uint32)
+    lib().oracle_b3_compress(ptr(np.array(cv, np.uint32)), ptr(np.array(block, np.uint32)),
+                             counter, block_len, flags, ptr(out))
+    return out
+
+
+def b3_hash(data):
+    d = np.frombuffer(bytes(data), np.uint8).copy() if len(data) else np.zeros(1, np.uint8)
+    out = np.zeros(32, np.uint8)
+    lib().oracle_b3_hash(ptr(d), len(data), ptr(out))
+    return out.tobytes()
+
+
+def b3_xof(data, n):
+    d = np.frombuffer(bytes(data), np.uint8).copy() if len(data) else np.zeros(1, np.uint8)
+    out = np.zeros(n, np.uint8)
+    lib().oracle_b3_xof(ptr(d), len(data), ptr(out), n)
+    return out.tobytes()
+
+
+def leaf_cv(data):
+    d = np.frombuffer(bytes(data), np.uint8).copy()
+    out = np.zeros(32, np.uint8)
+    lib().oracle_leaf_cv(ptr(d), len(data), ptr(out))
+    return out.tobytes()

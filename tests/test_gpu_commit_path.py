@@ -1,0 +1,75 @@
+"""GPU parity: witness, NTT, Merkle and PCS commit against the CPU oracle (bit-exact)."""
+import numpy as np
+import pytest
+
+import flock_challenge_gb300 as F
+import oracle_lib as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx(cuda_device):
+    return F.Context(0)
+
+
+def to_dev(arr):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(arr).view(np.uint8).reshape(-1).copy()).cuda()
+
+
+def host(t):
+    return t.cpu().numpy()
+
+
+@pytest.mark.parametrize("n_log,n", [(3, 8), (3, 5), (5, 32), (6, 50), (9, 512), (10, 700)])
+def test_witness_matches_oracle(cuda_device, n_log, n):
+    blocks = O.compressions(max(n_log, 3), 1234 + n)[:n]
+    z, a, b, s = F.generate_witness(to_dev(blocks), n, n_log)
+    oz, oa, ob, os_ = O.witness(blocks, n_log)
+    assert np.array_equal(host(z), oz.view(np.uint8))
+    assert np.array_equal(host(a), oa.view(np.uint8))
+    assert np.array_equal(host(b), ob.view(np.uint8))
+    assert np.array_equal(host(s), os_)
+
+
+def test_witness_z_only(cuda_device):
+    blocks = O.compressions(6, 9)
+    z, a, b, s = F.generate_witness(to_dev(blocks), 64, 6, want_ab=False, want_stripe=False)
+    oz, _, _, _ = O.witness(blocks, 6, want_ab=False, want_stripe=False)
+    assert a is None and s is None
+    assert np.array_equal(host(z), oz.view(np.uint8))
+
+
+@pytest.mark.parametrize("log_d,log_lanes,start", [(1, 4, 0), (5, 4, 0), (7, 6, 1), (12, 6, 1), (13, 4, 3)])
+def test_ntt_matches_oracle(ctx, log_d, log_lanes, start):
+    rng = np.random.default_rng(log_d * 7 + start)
+    data = rng.integers(0, 2**63, (1 << (log_d + log_lanes)) * 2, dtype=np.uint64)
+    data |= rng.integers(0, 2, data.shape, dtype=np.uint64) << np.uint64(63)
+    d = to_dev(data)
+    F.ntt(ctx, d, log_d, log_lanes, start)
+    ref = O.ntt_interleaved(data, 1 << log_lanes, start)
+    assert np.array_equal(host(d).view(np.uint64), ref)
+
+
+@pytest.mark.parametrize("n,leaf", [(1, 1024), (2, 64), (8, 128), (64, 1024), (1024, 128), (32, 4096),
+                                    (16, 2048), (4, 48), (2048, 1024)])
+def test_merkle_matches_oracle(cuda_device, n, leaf):
+    rng = np.random.default_rng(n + leaf)
+    data = rng.integers(0, 256, n * leaf, dtype=np.uint8)
+    tree = F.merkle_tree(to_dev(data), n, leaf)
+    ref = O.merkle_tree(data, n)
+    assert np.array_equal(host(tree).reshape(-1, 32), ref)
+
+
+@pytest.mark.parametrize("n_log", [3, 6, 8])
+def test_commit_matches_oracle(ctx, n_log):
+    m = 14 + n_log
+    blocks = O.compressions(n_log, 99 + n_log)
+    z, _, _, _ = F.generate_witness(to_dev(blocks), len(blocks), n_log, want_ab=False, want_stripe=False)
+    root, cw, tree = F.commit(ctx, z, m)
+    oz, _, _, _ = O.witness(blocks, n_log, want_ab=False, want_stripe=False)
+    oroot, ocw, otree = O.commit(oz, m, want_codeword=True, want_tree=True)
+    assert np.array_equal(host(cw).view(np.uint64), ocw)
+    assert np.array_equal(host(tree).reshape(-1, 32), otree)
+    assert root == oroot
