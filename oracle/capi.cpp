@@ -1,5 +1,6 @@
 // C entry points of the oracle library for the test harness (ctypes).
 // Test infrastructure only.
+#include <cstdio>
 #include <cstring>
 
 #include "oracle.h"
@@ -121,6 +122,85 @@ void oracle_commit(const uint64_t* z, int m, int log_inv_rate, int log_batch_siz
   memcpy(root, c.root().b, 32);
   if (codeword_out) memcpy(codeword_out, c.codeword.data(), c.codeword.size() * 16);
   if (tree_out) memcpy(tree_out, c.tree.data(), c.tree.size() * 32);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Protocol entry points.
+// ---------------------------------------------------------------------------
+#include "protocol.h"
+
+namespace {
+struct Mats {
+  SparseRows A, B;
+  Mats() { build_matrices(A, B); }
+};
+const Mats& mats() {
+  static const Mats m;
+  return m;
+}
+}  // namespace
+
+extern "C" {
+
+// Proves n compressions (padded to 2^n_blocks_log slots); writes the wire bytes.
+// Returns 0, or -5 when cap is too small (len receives the needed size).
+int oracle_prove(const Compression* blocks, size_t n, int n_blocks_log, uint8_t* out, size_t cap, size_t* len) {
+  std::vector<Compression> v(blocks, blocks + n);
+  uint8_t dg[32];
+  mats();
+  statement_digest(K_LOG + n_blocks_log, mats().A, mats().B, dg);
+  Bundle b = prove(v, n_blocks_log, dg);
+  auto bytes = encode_bundle(b);
+  *len = bytes.size();
+  if (bytes.size() > cap) return -5;
+  memcpy(out, bytes.data(), bytes.size());
+  return 0;
+}
+
+// 0 = accepted; -1 = malformed bytes; -2 = rejected. why (may be null) gets a
+// short reason.
+int oracle_verify(const uint8_t* bytes, size_t len, int m, char* why, size_t why_cap) {
+  Bundle b;
+  if (!decode_bundle(bytes, len, b)) {
+    if (why && why_cap) snprintf(why, why_cap, "malformed");
+    return -1;
+  }
+  uint8_t dg[32];
+  statement_digest(m, mats().A, mats().B, dg);
+  std::string w;
+  bool ok = verify(b, m, dg, mats().A, mats().B, "flock-bench-v0", &w);
+  if (why && why_cap) snprintf(why, why_cap, "%s", ok ? "ok" : w.c_str());
+  return ok ? 0 : -2;
+}
+
+// F8 NTT extension S -> Lambda of one 64-bit row through the reference's
+// recursive additive NTT (inverse on S = {0..63}, forward on 64 + span).
+void oracle_f8_extend_ntt(uint64_t row, uint8_t* out64) {
+  uint8_t v[64];
+  for (int s = 0; s < 64; s++) v[s] = (uint8_t)((row >> s) & 1);
+  f8_ntt_inverse(v, 6, 0);
+  f8_ntt_forward(v, 6, 64);
+  memcpy(out64, v, 64);
+}
+
+// Direct Lagrange extension used by the oracle's round-1 message.
+void oracle_f8_extend_lagrange(uint64_t row, uint8_t* out64) {
+  for (int i = 0; i < 64; i++) {
+    uint8_t lam = (uint8_t)(64 + i), acc = 0;
+    for (int s = 0; s < 64; s++) {
+      if (!((row >> s) & 1)) continue;
+      uint8_t num = 1, den = 1;
+      for (int t = 0; t < 64; t++) {
+        if (t == s) continue;
+        num = gf8_mul(num, lam ^ (uint8_t)t);
+        den = gf8_mul(den, (uint8_t)(s ^ t));
+      }
+      acc ^= gf8_mul(num, gf8_inv(den));
+    }
+    out64[i] = acc;
+  }
 }
 
 }  // extern "C"

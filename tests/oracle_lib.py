@@ -167,3 +167,44 @@ def leaf_cv(data):
     out = np.zeros(32, np.uint8)
     lib().oracle_leaf_cv(ptr(d), len(data), ptr(out))
     return out.tobytes()
+
+
+def _proto():
+    L = lib()
+    if not getattr(L, "_proto_ready", False):
+        P = ctypes.c_void_p
+        L.oracle_prove.argtypes = [P, ctypes.c_size_t, ctypes.c_int, P, ctypes.c_size_t,
+                                   ctypes.POINTER(ctypes.c_size_t)]
+        L.oracle_verify.argtypes = [P, ctypes.c_size_t, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]
+        L.oracle_f8_extend_ntt.argtypes = [ctypes.c_uint64, P]
+        L.oracle_f8_extend_lagrange.argtypes = [ctypes.c_uint64, P]
+        L._proto_ready = True
+    return L
+
+
+def prove(blocks, n_blocks_log):
+    """Full oracle proof; returns the wire bytes."""
+    L = _proto()
+    blocks = np.ascontiguousarray(blocks)
+    cap = 4_000_000
+    out = np.zeros(cap, np.uint8)
+    ln = ctypes.c_size_t()
+    rc = L.oracle_prove(ptr(blocks), len(blocks), n_blocks_log, ptr(out), cap, ctypes.byref(ln))
+    assert rc == 0, rc
+    return out[:ln.value].tobytes()
+
+
+def verify(proof_bytes, m):
+    """Oracle verifier: returns (accepted, reason)."""
+    L = _proto()
+    buf = np.frombuffer(proof_bytes, np.uint8).copy()
+    why = ctypes.create_string_buffer(256)
+    rc = L.oracle_verify(ptr(buf), len(proof_bytes), m, why, 256)
+    return rc == 0, why.value.decode()
+
+
+def f8_extend(row, via="ntt"):
+    L = _proto()
+    out = np.zeros(64, np.uint8)
+    (L.oracle_f8_extend_ntt if via == "ntt" else L.oracle_f8_extend_lagrange)(row, ptr(out))
+    return out
