@@ -1,0 +1,74 @@
+// Proof-of-work grind (crates/flock-core/src/challenger.rs:440-704, :1246-1310).
+//
+// The nonce is the smallest n >= 0 whose BLAKE3 hash of the 64-byte pre-image
+// digest || n_le64 || 0^24 (one block, CHUNK_START | CHUNK_END | ROOT) has at
+// least `bits` leading zero bits, read MSB-first from byte 0. Each thread
+// tests one nonce of a window and lowers a device minimum with atomicMin; the
+// host scans windows in increasing order and stops at the first window with a
+// hit, so the result is the global minimum.
+#include "blake3.cuh"
+#include "flock_internal.h"
+
+namespace {
+
+__device__ __forceinline__ bool leading_zeros_ok(const uint32_t h[8], uint32_t bits) {
+  // byte k of the hash is byte (k & 3) of word k >> 2 (little-endian words)
+  for (uint32_t k = 0; k < 32 && bits > 0; k++) {
+    uint32_t byte = (h[k >> 2] >> (8 * (k & 3))) & 255;
+    if (bits >= 8) {
+      if (byte) return false;
+      bits -= 8;
+    } else {
+      return (byte >> (8 - bits)) == 0;
+    }
+  }
+  return true;
+}
+
+__global__ void grind_kernel(const uint32_t* __restrict__ digest, uint64_t start, uint64_t count, uint32_t bits,
+                             unsigned long long* __restrict__ best) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  uint64_t nonce = start + i;
+  uint32_t m[16];
+#pragma unroll
+  for (int k = 0; k < 8; k++) m[k] = digest[k];
+  m[8] = (uint32_t)nonce;
+  m[9] = (uint32_t)(nonce >> 32);
+#pragma unroll
+  for (int k = 10; k < 16; k++) m[k] = 0;
+  uint32_t cv[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) cv[k] = b3::IV(k);
+  b3::compress_cv(cv, m, 64, b3::CHUNK_START | b3::CHUNK_END | b3::ROOT);
+  if (leading_zeros_ok(cv, bits)) atomicMin(best, (unsigned long long)nonce);
+}
+
+}  // namespace
+
+// Returns the smallest satisfying nonce. d_scratch: >= 40 bytes of device memory.
+int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, cudaStream_t st, uint64_t* nonce) {
+  if (bits == 0) {
+    *nonce = 0;
+    return FLOCK_OK;
+  }
+  if (bits > 60) return FLOCK_ERR_SHAPE;
+  unsigned long long* d_best = (unsigned long long*)d_scratch;
+  uint32_t* d_dig = (uint32_t*)((char*)d_scratch + 8);
+  const unsigned long long none = ~0ull;
+  if (cudaMemcpyAsync(d_dig, digest, 32, cudaMemcpyHostToDevice, st) != cudaSuccess) return FLOCK_ERR_CUDA;
+  if (cudaMemcpyAsync(d_best, &none, 8, cudaMemcpyHostToDevice, st) != cudaSuccess) return FLOCK_ERR_CUDA;
+  uint64_t window = (uint64_t)1 << (bits + 2 < 22 ? 22 : (bits + 2 > 30 ? 30 : bits + 2));
+  for (uint64_t start = 0;; start += window) {
+    grind_kernel<<<(unsigned)((window + 255) / 256), 256, 0, st>>>(d_dig, start, window, bits, d_best);
+    if (cudaGetLastError() != cudaSuccess) return FLOCK_ERR_CUDA;
+    unsigned long long best = 0;
+    if (cudaMemcpyAsync(&best, d_best, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess) return FLOCK_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return FLOCK_ERR_CUDA;
+    if (best != none) {
+      *nonce = best;
+      return FLOCK_OK;
+    }
+    if (start > ((uint64_t)1 << 62)) return FLOCK_ERR_TIMEOUT;
+  }
+}

@@ -1,0 +1,225 @@
+// Ligerito PCS prover kernels (crates/flock-core/src/pcs/ligerito.rs).
+//
+//  * round message (ligerito.rs:3725-3773): u0 = sum f0 b0, u2 = sum (f0+f1)(b0+b1)
+//    over LSB pairs, fused with the preceding fold f' = f0 + r (f0 + f1)
+//    (ligerito.rs:5517-5566, partial_eval_lsb :1673-1691);
+//  * OOD introduction with b_new = eq(z) evaluated on the fly from split
+//    tables, returning the message and h = sum f eq (ligerito.rs:5684-5702),
+//    and its glue b += beta eq(z);
+//  * induced basis (ligerito.rs:1989-2160): basis[j] = sum_i alpha_i Xhat_j(q_i)
+//    with Xhat_j = prod_{k in bits(j)} What_k; computed as a sum over queries of
+//    products of low/high tensor halves;
+//  * glue b += beta * basis, row and tree-node gathers for openings.
+#include "flock_internal.h"
+#include "gf128.cuh"
+
+namespace {
+
+constexpr int LG_THREADS = 256;
+
+__device__ __forceinline__ void block_reduce_write(gf256 a, gf256 b, gf256 c, gf128* out) {
+  __shared__ gf256 red[3][LG_THREADS / 32];
+  for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      a.r[k] ^= __shfl_xor_sync(0xffffffffu, a.r[k], off);
+      b.r[k] ^= __shfl_xor_sync(0xffffffffu, b.r[k], off);
+      c.r[k] ^= __shfl_xor_sync(0xffffffffu, c.r[k], off);
+    }
+  int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { red[0][w] = a; red[1][w] = b; red[2][w] = c; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    gf256 s0 = {{0, 0, 0, 0}}, s1 = s0, s2 = s0;
+    for (int k = 0; k < LG_THREADS / 32; k++) { gf256_acc(s0, red[0][k]); gf256_acc(s1, red[1][k]); gf256_acc(s2, red[2][k]); }
+    out[3 * blockIdx.x] = gf256_reduce(s0);
+    out[3 * blockIdx.x + 1] = gf256_reduce(s1);
+    out[3 * blockIdx.x + 2] = gf256_reduce(s2);
+  }
+}
+
+// If fold: in has 2 * n_out elements, bound at r into out (n_out elements);
+// message over the n_out-element state. Partials: (u0, u2, 0) per block.
+__global__ void __launch_bounds__(LG_THREADS)
+lig_fold_msg_kernel(const gf128* __restrict__ f, const gf128* __restrict__ b, size_t n_out, int fold, gf128 r,
+                    gf128* __restrict__ fo, gf128* __restrict__ bo, gf128* __restrict__ partials) {
+  gf256 u0 = {{0, 0, 0, 0}}, u2 = u0, zz = u0;
+  size_t pairs = n_out / 2;
+  for (size_t j = (size_t)blockIdx.x * LG_THREADS + threadIdx.x; j < pairs; j += (size_t)gridDim.x * LG_THREADS) {
+    gf128 f0, f1, b0, b1;
+    if (fold) {
+      gf128 x0 = f[4 * j], x1 = f[4 * j + 1], x2 = f[4 * j + 2], x3 = f[4 * j + 3];
+      f0 = gf_add(x0, gf_mul(r, gf_add(x0, x1)));
+      f1 = gf_add(x2, gf_mul(r, gf_add(x2, x3)));
+      gf128 y0 = b[4 * j], y1 = b[4 * j + 1], y2 = b[4 * j + 2], y3 = b[4 * j + 3];
+      b0 = gf_add(y0, gf_mul(r, gf_add(y0, y1)));
+      b1 = gf_add(y2, gf_mul(r, gf_add(y2, y3)));
+      fo[2 * j] = f0; fo[2 * j + 1] = f1;
+      bo[2 * j] = b0; bo[2 * j + 1] = b1;
+    } else {
+      f0 = f[2 * j]; f1 = f[2 * j + 1]; b0 = b[2 * j]; b1 = b[2 * j + 1];
+    }
+    gf256_acc(u0, gf_mul_wide(f0, b0));
+    gf256_acc(u2, gf_mul_wide(gf_add(f0, f1), gf_add(b0, b1)));
+  }
+  block_reduce_write(u0, u2, zz, partials);
+}
+
+// Message of (f, eq(z)) and h = sum f * eq(z); eq(z)[j] = lo[j & mask] * hi[j >> lo_bits].
+__global__ void __launch_bounds__(LG_THREADS)
+lig_intro_eq_kernel(const gf128* __restrict__ f, size_t n, const gf128* __restrict__ lo,
+                    const gf128* __restrict__ hi, int lo_bits, gf128* __restrict__ partials) {
+  gf256 u0 = {{0, 0, 0, 0}}, u2 = u0, h = u0;
+  size_t mask = ((size_t)1 << lo_bits) - 1;
+  for (size_t j = (size_t)blockIdx.x * LG_THREADS + threadIdx.x; j < n / 2; j += (size_t)gridDim.x * LG_THREADS) {
+    size_t i0 = 2 * j, i1 = 2 * j + 1;
+    gf128 e0 = gf_mul(lo[i0 & mask], hi[i0 >> lo_bits]);
+    gf128 e1 = gf_mul(lo[i1 & mask], hi[i1 >> lo_bits]);
+    gf128 f0 = f[i0], f1 = f[i1];
+    gf256 p0 = gf_mul_wide(f0, e0);
+    gf256_acc(u0, p0);
+    gf256_acc(h, p0);
+    gf256_acc(h, gf_mul_wide(f1, e1));
+    gf256_acc(u2, gf_mul_wide(gf_add(f0, f1), gf_add(e0, e1)));
+  }
+  block_reduce_write(u0, u2, h, partials);
+}
+
+__global__ void glue_eq_kernel(gf128* __restrict__ b, size_t n, const gf128* __restrict__ lo,
+                               const gf128* __restrict__ hi, int lo_bits, gf128 beta) {
+  size_t mask = ((size_t)1 << lo_bits) - 1;
+  for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x)
+    b[j] = gf_add(b[j], gf_mul(beta, gf_mul(lo[j & mask], hi[j >> lo_bits])));
+}
+
+__global__ void glue_kernel(gf128* __restrict__ b, const gf128* __restrict__ add, size_t n, gf128 beta) {
+  for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x)
+    b[j] = gf_add(b[j], gf_mul(beta, add[j]));
+}
+
+// What_k(q_i) for k < n (ligerito.rs:1776-1824): s_0 = q, s_k = s^2 + s_{k-1}(v_{k-1}) s,
+// normalized by 1 / s_k(v_k).
+__global__ void what_kernel(const uint32_t* __restrict__ queries, int nq, int n, const gf128* __restrict__ sks,
+                            const gf128* __restrict__ inv_sks, gf128* __restrict__ W) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  gf128 s = gf_zero();
+  s.w[0] = queries[i];
+  for (int k = 0; k < n; k++) {
+    if (k > 0) s = gf_add(gf_mul(s, s), gf_mul(sks[k - 1], s));
+    W[(size_t)i * n + k] = gf_mul(s, inv_sks[k]);
+  }
+}
+
+// T[i][j] = scale_i * prod_{k < bits, bit k of j} W[i][k0 + k]; scale_i = alpha_i or 1.
+__global__ void tensor_kernel(const gf128* __restrict__ W, int nq, int n, int k0, int bits,
+                              const gf128* __restrict__ scale, gf128* __restrict__ T) {
+  size_t len = (size_t)1 << bits;
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)nq * len) return;
+  int i = (int)(e / len);
+  size_t j = e % len;
+  gf128 acc = scale ? scale[i] : gf_one();
+  for (int k = 0; k < bits; k++)
+    if ((j >> k) & 1) acc = gf_mul(acc, W[(size_t)i * n + k0 + k]);
+  T[e] = acc;
+}
+
+// basis[j] = sum_i LO[i][j & mask] * HI[i][j >> lo_bits]
+__global__ void __launch_bounds__(256)
+basis_kernel(const gf128* __restrict__ LO, const gf128* __restrict__ HI, int nq, int lo_bits, int hi_bits,
+             gf128* __restrict__ basis) {
+  size_t n = (size_t)1 << (lo_bits + hi_bits);
+  size_t lo_n = (size_t)1 << lo_bits, hi_n = (size_t)1 << hi_bits;
+  for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    size_t jl = j & (lo_n - 1), jh = j >> lo_bits;
+    gf256 acc = {{0, 0, 0, 0}};
+    for (int i = 0; i < nq; i++) gf256_acc(acc, gf_mul_wide(LO[(size_t)i * lo_n + jl], HI[(size_t)i * hi_n + jh]));
+    basis[j] = gf256_reduce(acc);
+  }
+}
+
+__global__ void gather_rows_kernel(const gf128* __restrict__ mat, const uint32_t* __restrict__ rows, int n_rows,
+                                   int width, gf128* __restrict__ out) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)n_rows * width) return;
+  size_t r = e / width, c = e % width;
+  out[e] = mat[(size_t)rows[r] * width + c];
+}
+
+__global__ void gather_nodes_kernel(const uint4* __restrict__ tree, const uint32_t* __restrict__ idx, int n,
+                                    uint4* __restrict__ out) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= 2 * n) return;
+  out[e] = tree[2 * (size_t)idx[e >> 1] + (e & 1)];
+}
+
+inline gf128 to_gf(const uint64_t v[2]) {
+  gf128 r;
+  r.w[0] = (uint32_t)v[0]; r.w[1] = (uint32_t)(v[0] >> 32); r.w[2] = (uint32_t)v[1]; r.w[3] = (uint32_t)(v[1] >> 32);
+  return r;
+}
+inline unsigned grid_for(size_t work, size_t threads, size_t cap) {
+  size_t g = (work + threads - 1) / threads;
+  if (g < 1) g = 1;
+  return (unsigned)(g > cap ? cap : g);
+}
+
+}  // namespace
+
+int flock_lig_grid(size_t n_pairs) { return (int)grid_for(n_pairs, LG_THREADS, 152 * 4); }
+
+int flock_launch_lig_fold_msg(const void* f, const void* b, size_t n_out, int fold, const uint64_t r[2], void* fo,
+                              void* bo, void* partials, int grid, cudaStream_t st) {
+  lig_fold_msg_kernel<<<grid, LG_THREADS, 0, st>>>((const gf128*)f, (const gf128*)b, n_out, fold, to_gf(r),
+                                                   (gf128*)fo, (gf128*)bo, (gf128*)partials);
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_launch_lig_intro_eq(const void* f, size_t n, const void* lo, const void* hi, int lo_bits, void* partials,
+                              int grid, cudaStream_t st) {
+  lig_intro_eq_kernel<<<grid, LG_THREADS, 0, st>>>((const gf128*)f, n, (const gf128*)lo, (const gf128*)hi, lo_bits,
+                                                   (gf128*)partials);
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_launch_glue_eq(void* b, size_t n, const void* lo, const void* hi, int lo_bits, const uint64_t beta[2],
+                         cudaStream_t st) {
+  glue_eq_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, st>>>((gf128*)b, n, (const gf128*)lo, (const gf128*)hi,
+                                                             lo_bits, to_gf(beta));
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_launch_glue(void* b, const void* add, size_t n, const uint64_t beta[2], cudaStream_t st) {
+  glue_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, st>>>((gf128*)b, (const gf128*)add, n, to_gf(beta));
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_launch_induce_basis(const uint32_t* d_queries, int nq, int n, const void* sks, const void* inv_sks,
+                              const void* alpha_w, void* W, void* LO, void* HI, void* basis, cudaStream_t st) {
+  what_kernel<<<(nq + 127) / 128, 128, 0, st>>>(d_queries, nq, n, (const gf128*)sks, (const gf128*)inv_sks,
+                                                (gf128*)W);
+  int lo_bits = (n + 1) / 2, hi_bits = n - lo_bits;
+  size_t nlo = (size_t)nq << lo_bits, nhi = (size_t)nq << hi_bits;
+  tensor_kernel<<<grid_for(nlo, 256, 1u << 30), 256, 0, st>>>((const gf128*)W, nq, n, 0, lo_bits,
+                                                               (const gf128*)alpha_w, (gf128*)LO);
+  tensor_kernel<<<grid_for(nhi, 256, 1u << 30), 256, 0, st>>>((const gf128*)W, nq, n, lo_bits, hi_bits, nullptr,
+                                                               (gf128*)HI);
+  basis_kernel<<<grid_for((size_t)1 << n, 256, 152 * 8), 256, 0, st>>>((const gf128*)LO, (const gf128*)HI, nq,
+                                                                       lo_bits, hi_bits, (gf128*)basis);
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_launch_gather_rows(const void* mat, const uint32_t* rows, int n_rows, int width, void* out,
+                             cudaStream_t st) {
+  size_t n = (size_t)n_rows * width;
+  gather_rows_kernel<<<grid_for(n, 256, 1u << 30), 256, 0, st>>>((const gf128*)mat, rows, n_rows, width,
+                                                                  (gf128*)out);
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_launch_gather_nodes(const void* tree, const uint32_t* idx, int n, void* out, cudaStream_t st) {
+  if (n == 0) return FLOCK_OK;
+  gather_nodes_kernel<<<(2 * n + 255) / 256, 256, 0, st>>>((const uint4*)tree, idx, n, (uint4*)out);
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}

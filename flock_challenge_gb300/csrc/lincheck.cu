@@ -1,0 +1,163 @@
+// Lincheck kernels (crates/flock-core/src/lincheck.rs:1480-1660).
+//
+//  * partial fold: z_vec[i] = sum_outer z[i, outer] eq(x_outer, outer), read
+//    from the byte stripe (byte (outer/8)*2^14 + i holds 8 outer bits), one
+//    256-entry subset-sum table of eq per stripe (lincheck.rs:655-720);
+//  * comb: alpha * A0^T eq_inner + B0^T eq_inner (+ beta at the constant
+//    column) gathered column-wise from a CSC copy of the base matrices;
+//  * product sumcheck rounds over (comb, z_vec), binding the top variable
+//    (lincheck.rs:1242-1300), in one CTA per round.
+#include "flock_internal.h"
+#include "gf128.cuh"
+
+namespace {
+
+constexpr int PF_THREADS = 1024;
+constexpr int PF_PER_THREAD = FLOCK_K / PF_THREADS;  // 16
+
+__global__ void __launch_bounds__(PF_THREADS, 1)
+lc_partial_fold_kernel(const uint8_t* __restrict__ stripe, size_t n_stripes, const gf128* __restrict__ eq_lo,
+                       const gf128* __restrict__ eq_hi, int lo_bits, gf128* __restrict__ partials) {
+  __shared__ gf128 t8[256];
+  __shared__ gf128 e8v[8];
+  gf128 acc[PF_PER_THREAD];
+#pragma unroll
+  for (int k = 0; k < PF_PER_THREAD; k++) acc[k] = gf_zero();
+  const size_t lo_mask = ((size_t)1 << lo_bits) - 1;
+  for (size_t s = blockIdx.x; s < n_stripes; s += gridDim.x) {
+    if (threadIdx.x < 8) {
+      size_t o = 8 * s + threadIdx.x;
+      e8v[threadIdx.x] = gf_mul(eq_lo[o & lo_mask], eq_hi[o >> lo_bits]);
+    }
+    __syncthreads();
+    if (threadIdx.x < 256) {
+      gf128 v = gf_zero();
+      for (int r = 0; r < 8; r++)
+        if ((threadIdx.x >> r) & 1) v = gf_add(v, e8v[r]);
+      t8[threadIdx.x] = v;
+    }
+    __syncthreads();
+    const uint8_t* row = stripe + s * FLOCK_K;
+    // each thread: 16 consecutive bytes (one uint4) of the 2^14-byte stripe
+    uint4 bytes = reinterpret_cast<const uint4*>(row)[threadIdx.x];
+    uint32_t wds[4] = {bytes.x, bytes.y, bytes.z, bytes.w};
+#pragma unroll
+    for (int k = 0; k < PF_PER_THREAD; k++) {
+      uint32_t b = (wds[k >> 2] >> (8 * (k & 3))) & 255;
+      if (b) acc[k] = gf_add(acc[k], t8[b]);
+    }
+    __syncthreads();
+  }
+  gf128* out = partials + (size_t)blockIdx.x * FLOCK_K + (size_t)threadIdx.x * PF_PER_THREAD;
+#pragma unroll
+  for (int k = 0; k < PF_PER_THREAD; k++) out[k] = acc[k];
+}
+
+// comb[c] = alpha * sum_{r in colA(c)} eq[r] + sum_{r in colB(c)} eq[r] (+ beta at pin)
+__global__ void lc_comb_kernel(const uint32_t* __restrict__ a_ptr, const uint32_t* __restrict__ a_idx,
+                               const uint32_t* __restrict__ b_ptr, const uint32_t* __restrict__ b_idx,
+                               const gf128* __restrict__ eq, gf128 alpha, gf128 beta, int pin,
+                               gf128* __restrict__ comb) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= FLOCK_K) return;
+  gf128 sa = gf_zero(), sb = gf_zero();
+  for (uint32_t k = a_ptr[c]; k < a_ptr[c + 1]; k++) sa = gf_add(sa, eq[a_idx[k]]);
+  for (uint32_t k = b_ptr[c]; k < b_ptr[c + 1]; k++) sb = gf_add(sb, eq[b_idx[k]]);
+  gf128 v = gf_add(gf_mul(alpha, sa), sb);
+  if (c == pin) v = gf_add(v, beta);
+  comb[c] = v;
+}
+
+// Quirky eq table (lincheck.rs:1127-1143): out[s + 64 * j] = lag[s] * eq(x_inner_rest)[j].
+__global__ void lc_quirky_eq_kernel(const gf128* __restrict__ lag, const gf128* __restrict__ x_rest, int n_rest,
+                                    gf128* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (64 << n_rest)) return;
+  int s = i & 63, j = i >> 6;
+  gf128 e = gf_one();
+  for (int k = 0; k < n_rest; k++) {
+    gf128 r = x_rest[k];
+    if (!((j >> k) & 1)) r.w[0] ^= 1;
+    e = gf_mul(e, r);
+  }
+  out[i] = gf_mul(lag[s], e);
+}
+
+// One product-sumcheck round on (c, z) of length n (top-variable split), with
+// the previous round's top bind fused in when bind != 0:
+//   bind: v[i] <- v[i] + r (v[i + n] + v[i]) for the incoming length 2n
+//   msg:  e1 = sum c_hi z_hi, einf = sum (c_hi + c_lo)(z_hi + z_lo)
+// Single CTA; msg written to out[0..2].
+constexpr int LR_THREADS = 1024;
+__global__ void __launch_bounds__(LR_THREADS)
+lc_round_kernel(gf128* __restrict__ c, gf128* __restrict__ z, size_t n, int bind, gf128 r, int emit,
+                gf128* __restrict__ out) {
+  if (bind) {
+    for (size_t i = threadIdx.x; i < n; i += LR_THREADS) {
+      gf128 c0 = c[i], c1 = c[i + n], z0 = z[i], z1 = z[i + n];
+      c[i] = gf_add(c0, gf_mul(r, gf_add(c1, c0)));
+      z[i] = gf_add(z0, gf_mul(r, gf_add(z1, z0)));
+    }
+    __syncthreads();
+  }
+  if (!emit) return;
+  size_t half = n / 2;
+  gf256 e1 = {{0, 0, 0, 0}}, ei = {{0, 0, 0, 0}};
+  for (size_t i = threadIdx.x; i < half; i += LR_THREADS) {
+    gf128 cl = c[i], ch = c[i + half], zl = z[i], zh = z[i + half];
+    gf256_acc(e1, gf_mul_wide(ch, zh));
+    gf256_acc(ei, gf_mul_wide(gf_add(ch, cl), gf_add(zh, zl)));
+  }
+  __shared__ gf256 red[2][LR_THREADS / 32];
+  for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      e1.r[k] ^= __shfl_xor_sync(0xffffffffu, e1.r[k], off);
+      ei.r[k] ^= __shfl_xor_sync(0xffffffffu, ei.r[k], off);
+    }
+  int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { red[0][w] = e1; red[1][w] = ei; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    gf256 s1 = {{0, 0, 0, 0}}, si = {{0, 0, 0, 0}};
+    for (int k = 0; k < LR_THREADS / 32; k++) { gf256_acc(s1, red[0][k]); gf256_acc(si, red[1][k]); }
+    out[0] = gf256_reduce(s1);
+    out[1] = gf256_reduce(si);
+  }
+}
+
+inline gf128 to_gf(const uint64_t v[2]) {
+  gf128 r;
+  r.w[0] = (uint32_t)v[0]; r.w[1] = (uint32_t)(v[0] >> 32); r.w[2] = (uint32_t)v[1]; r.w[3] = (uint32_t)(v[1] >> 32);
+  return r;
+}
+
+}  // namespace
+
+int flock_launch_lc_partial_fold(const void* stripe, size_t n_stripes, const void* eq_lo, const void* eq_hi,
+                                 int lo_bits, void* partials, int grid, cudaStream_t st) {
+  lc_partial_fold_kernel<<<grid, PF_THREADS, 0, st>>>((const uint8_t*)stripe, n_stripes, (const gf128*)eq_lo,
+                                                      (const gf128*)eq_hi, lo_bits, (gf128*)partials);
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_launch_lc_comb(const uint32_t* a_ptr, const uint32_t* a_idx, const uint32_t* b_ptr, const uint32_t* b_idx,
+                         const void* eq, const uint64_t alpha[2], const uint64_t beta[2], int pin, void* comb,
+                         cudaStream_t st) {
+  lc_comb_kernel<<<FLOCK_K / 128, 128, 0, st>>>(a_ptr, a_idx, b_ptr, b_idx, (const gf128*)eq, to_gf(alpha),
+                                                to_gf(beta), pin, (gf128*)comb);
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_launch_lc_quirky_eq(const void* lag, const void* x_rest, int n_rest, void* out, cudaStream_t st) {
+  int n = 64 << n_rest;
+  lc_quirky_eq_kernel<<<(n + 255) / 256, 256, 0, st>>>((const gf128*)lag, (const gf128*)x_rest, n_rest,
+                                                       (gf128*)out);
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_launch_lc_round(void* c, void* z, size_t n, int bind, const uint64_t r[2], int emit, void* out,
+                          cudaStream_t st) {
+  lc_round_kernel<<<1, LR_THREADS, 0, st>>>((gf128*)c, (gf128*)z, n, bind, to_gf(r), emit, (gf128*)out);
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}

@@ -1,0 +1,389 @@
+// Zerocheck kernels: univariate-skip round 1 and the multilinear rounds.
+//
+// Protocol: crates/flock-core/src/zerocheck.rs:482-1360 (verifier :1365-1517).
+// Round 1 sends, for the 64 points lambda_i = 64 + i of GF(2^8) (embedded by
+// phi8), P^AB(l) = sum_x eq(r_rest, x) phi8(a^(l,x) b^(l,x)) and
+// P^C(l) = sum_x eq(r_rest, x) phi8(c^(l,x)), where a^(., x) is the degree<64
+// extension of the 64 witness bits of row x from S = {0..63}
+// (zerocheck/univariate_skip.rs:84-138).
+//
+// GB300 formulation. The first seven rest variables carry fixed challenges
+// (zerocheck/univariate_skip_optimized.rs:85-130): three phi8 constants and
+// four g/(1+g) with g = x^(2^j). Their eq weight factors as
+//   eq_in(xs, xm) = phi8(e8[xs]) * x^xm * Dinv,
+// so per outer index xo (128 rows) the kernel needs no F128 multiply until
+//   V_i(xo) = sum_xm x^xm phi8( sum_xs e8[xs] * y_i(xs, xm, xo) ),
+// which is a 143-bit shifted XOR of table values, reduced once and multiplied
+// by eq_out(xo). The F8 values y_i = a^_i b^_i are computed bit-sliced over the
+// 64 lambda points (eight 64-bit planes), so one product handles all points.
+// P^C uses linearity: C_s = sum_x eq(x) c_s(x) for the 64 skip positions s,
+// mapped to Lambda on the host.
+#include "flock_internal.h"
+#include "gf128.cuh"
+#include "zc_tables.h"
+
+namespace {
+
+constexpr int R1_THREADS = 512;
+
+// 143-bit accumulator (five 32-bit words) for shifted table values.
+struct Acc5 {
+  uint32_t w[5];
+};
+
+__device__ __forceinline__ void acc_shift_xor(Acc5& a, const uint4 v, int sh) {
+  // a ^= v << sh, 0 <= sh < 16
+  if (sh == 0) {
+    a.w[0] ^= v.x; a.w[1] ^= v.y; a.w[2] ^= v.z; a.w[3] ^= v.w;
+  } else {
+    a.w[0] ^= v.x << sh;
+    a.w[1] ^= __funnelshift_l(v.x, v.y, sh);
+    a.w[2] ^= __funnelshift_l(v.y, v.z, sh);
+    a.w[3] ^= __funnelshift_l(v.z, v.w, sh);
+    a.w[4] ^= v.w >> (32 - sh);
+  }
+}
+
+__device__ __forceinline__ gf128 acc_reduce(const Acc5& a) {
+  // bits 128..143 live in w[4] (< 2^15): fold with x^128 = x^7 + x^2 + x + 1
+  uint32_t ov = a.w[4];
+  uint32_t f = ov ^ (ov << 1) ^ (ov << 2) ^ (ov << 7);  // < 2^22, no further overflow
+  gf128 r;
+  r.w[0] = a.w[0] ^ f;
+  r.w[1] = a.w[1];
+  r.w[2] = a.w[2];
+  r.w[3] = a.w[3];
+  return r;
+}
+
+// Bit-sliced GF(2^8) product of 64 lane pairs (planes p[j] = bit j over lanes).
+__device__ __forceinline__ void f8_mul_planes(const uint64_t* a, const uint64_t* b, uint64_t* out) {
+  uint64_t p[15];
+#pragma unroll
+  for (int k = 0; k < 15; k++) p[k] = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++)
+#pragma unroll
+    for (int j = 0; j < 8; j++) p[i + j] ^= a[i] & b[j];
+#pragma unroll
+  for (int k = 14; k >= 8; k--) {
+    p[k - 4] ^= p[k];
+    p[k - 5] ^= p[k];
+    p[k - 7] ^= p[k];
+    p[k - 8] ^= p[k];
+  }
+#pragma unroll
+  for (int k = 0; k < 8; k++) out[k] = p[k];
+}
+
+__device__ __forceinline__ uint32_t byte_from_planes(const uint64_t* pl, int i) {
+  uint32_t v = 0;
+#pragma unroll
+  for (int j = 0; j < 8; j++) v |= (uint32_t)((pl[j] >> i) & 1) << j;
+  return v;
+}
+
+// grid: each warp walks pairs of outer blocks; lane: xm = lane & 15, xo half = lane >> 4.
+__global__ void __launch_bounds__(R1_THREADS, 1)
+zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B, const uint64_t* __restrict__ C,
+                 size_t n_outer, const gf128* __restrict__ eq_out, const ZcRound1Tables* __restrict__ T,
+                 gf128* __restrict__ partials) {
+  extern __shared__ uint4 sm[];
+  uint64_t* ext = reinterpret_cast<uint64_t*>(sm);                  // [8][256][8]
+  uint4* phi = sm + (8 * 256 * 8 * 8) / 16;                         // [256]
+  uint64_t* xch = reinterpret_cast<uint64_t*>(phi + 256);           // per warp [2][16][16]
+  const uint64_t* ext_src = &T->ext[0][0][0];
+  for (int i = threadIdx.x; i < 8 * 256 * 8; i += R1_THREADS) ext[i] = ext_src[i];
+  for (int i = threadIdx.x; i < 256; i += R1_THREADS) phi[i] = reinterpret_cast<const uint4*>(T->phi8)[i];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int xm = lane & 15, half = lane >> 4;
+  uint64_t* my_x = xch + warp * (2 * 16 * 16);
+  gf128 sum_ab[4], sum_c[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) { sum_ab[q] = gf_zero(); sum_c[q] = gf_zero(); }
+
+  const size_t total_warps = (size_t)gridDim.x * (R1_THREADS / 32);
+  const size_t gwarp = (size_t)blockIdx.x * (R1_THREADS / 32) + warp;
+  for (size_t pair = gwarp; 2 * pair < n_outer; pair += total_warps) {
+    const size_t xo = 2 * pair + half;
+    const bool live = xo < n_outer;
+    uint64_t w[8], t[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) { w[j] = 0; t[j] = 0; }
+    if (live) {
+      const size_t row0 = xo * 128 + (size_t)xm * 8;
+#pragma unroll 1
+      for (int xs = 0; xs < 8; xs++) {
+        uint64_t ra = A[row0 + xs], rb = B[row0 + xs], rc = C[row0 + xs];
+        uint64_t ea[8], eb[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) { ea[j] = 0; eb[j] = 0; }
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+          const uint4* pa = reinterpret_cast<const uint4*>(ext + ((c * 256 + ((ra >> (8 * c)) & 255)) << 3));
+          const uint4* pb = reinterpret_cast<const uint4*>(ext + ((c * 256 + ((rb >> (8 * c)) & 255)) << 3));
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            uint4 va = pa[q], vb = pb[q];
+            ea[2 * q] ^= ((uint64_t)va.y << 32) | va.x;
+            ea[2 * q + 1] ^= ((uint64_t)va.w << 32) | va.z;
+            eb[2 * q] ^= ((uint64_t)vb.y << 32) | vb.x;
+            eb[2 * q + 1] ^= ((uint64_t)vb.w << 32) | vb.z;
+          }
+        }
+        uint64_t y[8];
+        f8_mul_planes(ea, eb, y);
+        // w += e8[xs] * y (constant multiply as an 8x8 plane matrix);
+        // t += e8[xs] * c_s (c_s in {0,1}: plane j takes c where bit j of e8 is set).
+        const uint8_t* mm = T->e8_mat[xs];
+        const uint8_t e8 = T->e8[xs];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          uint64_t acc = 0;
+#pragma unroll
+          for (int k = 0; k < 8; k++)
+            if ((mm[j] >> k) & 1) acc ^= y[k];
+          w[j] ^= acc;
+          if ((e8 >> j) & 1) t[j] ^= rc;
+        }
+      }
+    }
+    // Exchange the w / t planes of the 16 xm lanes of each half.
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      my_x[(half * 16 + xm) * 16 + j] = w[j];
+      my_x[(half * 16 + xm) * 16 + 8 + j] = t[j];
+    }
+    __syncwarp();
+    if (live) {
+      // this lane handles points / skip positions 4*xm .. 4*xm+3 of its half
+      Acc5 va[4], vc[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+#pragma unroll
+        for (int k = 0; k < 5; k++) { va[q].w[k] = 0; vc[q].w[k] = 0; }
+#pragma unroll 4
+      for (int mm2 = 0; mm2 < 16; mm2++) {
+        const uint64_t* pw = my_x + (half * 16 + mm2) * 16;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          int i = 4 * xm + q;
+          acc_shift_xor(va[q], phi[byte_from_planes(pw, i)], mm2);
+          acc_shift_xor(vc[q], phi[byte_from_planes(pw + 8, i)], mm2);
+        }
+      }
+      gf128 e = gf_load(&eq_out[xo]);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        sum_ab[q] = gf_add(sum_ab[q], gf_mul(acc_reduce(va[q]), e));
+        sum_c[q] = gf_add(sum_c[q], gf_mul(acc_reduce(vc[q]), e));
+      }
+    }
+    __syncwarp();
+  }
+  // lanes l and l + 16 hold the same points: combine, then write this warp's partials.
+#pragma unroll
+  for (int q = 0; q < 4; q++)
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      sum_ab[q].w[k] ^= __shfl_xor_sync(0xffffffffu, sum_ab[q].w[k], 16);
+      sum_c[q].w[k] ^= __shfl_xor_sync(0xffffffffu, sum_c[q].w[k], 16);
+    }
+  if (half == 0) {
+    gf128* out = partials + gwarp * 128;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      out[4 * xm + q] = sum_ab[q];
+      out[64 + 4 * xm + q] = sum_c[q];
+    }
+  }
+}
+
+// XOR-reduce `count` rows of `width` F128 into out (one thread per column).
+__global__ void reduce_rows_kernel(const gf128* __restrict__ in, size_t count, int width, gf128* __restrict__ out) {
+  int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= width) return;
+  gf128 acc = gf_zero();
+  for (size_t r = 0; r < count; r++) acc = gf_add(acc, in[r * width + col]);
+  out[col] = acc;
+}
+
+// Skip fold at z: out[x] = sum_s bit_s(W[x]) L_s(z), with 8 byte tables of the
+// 64 Lagrange weights (multilinear.rs:598-630).
+__global__ void __launch_bounds__(256)
+fold_skip_kernel(const uint64_t* __restrict__ W0, const uint64_t* __restrict__ W1, size_t rows,
+                 const gf128* __restrict__ lag, gf128* __restrict__ out0, gf128* __restrict__ out1) {
+  __shared__ gf128 tab[8 * 256];
+  for (int e = threadIdx.x; e < 8 * 256; e += blockDim.x) {
+    int c = e >> 8, v = e & 255;
+    gf128 acc = gf_zero();
+    for (int j = 0; j < 8; j++)
+      if ((v >> j) & 1) acc = gf_add(acc, lag[8 * c + j]);
+    tab[e] = acc;
+  }
+  __syncthreads();
+  for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < rows; x += (size_t)gridDim.x * blockDim.x) {
+    uint64_t a = W0[x], b = W1[x];
+    gf128 ra = gf_zero(), rb = gf_zero();
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      ra = gf_add(ra, tab[c * 256 + ((a >> (8 * c)) & 255)]);
+      rb = gf_add(rb, tab[c * 256 + ((b >> (8 * c)) & 255)]);
+    }
+    out0[x] = ra;
+    out1[x] = rb;
+  }
+}
+
+// eq table split: lo[i] = prod_{k<lo_bits} f(r_k, bit k of i), hi[i] over the
+// next hi_bits variables; f(r, 1) = r, f(r, 0) = 1 + r.
+__global__ void eq_split_kernel(const gf128* __restrict__ r, int lo_bits, int hi_bits, gf128* __restrict__ lo,
+                                gf128* __restrict__ hi) {
+  size_t nlo = (size_t)1 << lo_bits, nhi = (size_t)1 << hi_bits;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < nlo + nhi; e += (size_t)gridDim.x * blockDim.x) {
+    bool is_lo = e < nlo;
+    size_t idx = is_lo ? e : e - nlo;
+    int nb = is_lo ? lo_bits : hi_bits;
+    const gf128* rr = is_lo ? r : r + lo_bits;
+    gf128 acc = gf_one();
+    for (int k = 0; k < nb; k++) {
+      gf128 rk = rr[k];
+      if (!((idx >> k) & 1)) rk.w[0] ^= 1;
+      acc = gf_mul(acc, rk);
+    }
+    if (is_lo) lo[idx] = acc;
+    else hi[idx] = acc;
+  }
+}
+
+// One multilinear round (zerocheck.rs:690-760, multilinear.rs:632-675), with
+// the previous round's bind fused in when rho != null:
+//   in:  A, B of length 2*n_pairs_in (bound to A' = A0 + rho (A0 + A1) first)
+//   msg: G(1) = sum_j eq[j] a1 b1,  G(inf) = sum_j eq[j] (a0+a1)(b0+b1)
+// eq[j] = eq_lo[j & lo_mask] * eq_hi[j >> lo_bits]: the inner sums run over
+// eq_lo only and are multiplied by eq_hi once per CTA row block.
+constexpr int RND_THREADS = 256;
+__global__ void __launch_bounds__(RND_THREADS)
+zc_round_kernel(const gf128* __restrict__ A, const gf128* __restrict__ B, size_t n_pairs, int bind,
+                gf128 rho, gf128* __restrict__ Aout, gf128* __restrict__ Bout, const gf128* __restrict__ eq_lo,
+                const gf128* __restrict__ eq_hi, int lo_bits, gf128* __restrict__ partials) {
+  // grid-stride over hi blocks: each CTA handles whole hi indices
+  const size_t lo_n = (size_t)1 << lo_bits;
+  const size_t n_hi = (n_pairs + lo_n - 1) / lo_n;
+  gf256 g1 = {{0, 0, 0, 0}}, gi = {{0, 0, 0, 0}};
+  for (size_t h = blockIdx.x; h < n_hi; h += gridDim.x) {
+    gf256 l1 = {{0, 0, 0, 0}}, li = {{0, 0, 0, 0}};
+    size_t base = h * lo_n;
+    size_t end = base + lo_n < n_pairs ? base + lo_n : n_pairs;
+    for (size_t j = base + threadIdx.x; j < end; j += RND_THREADS) {
+      gf128 a0, a1, b0, b1;
+      if (bind) {
+        gf128 p0 = A[4 * j], p1 = A[4 * j + 1], p2 = A[4 * j + 2], p3 = A[4 * j + 3];
+        a0 = gf_add(p0, gf_mul(rho, gf_add(p0, p1)));
+        a1 = gf_add(p2, gf_mul(rho, gf_add(p2, p3)));
+        gf128 q0 = B[4 * j], q1 = B[4 * j + 1], q2 = B[4 * j + 2], q3 = B[4 * j + 3];
+        b0 = gf_add(q0, gf_mul(rho, gf_add(q0, q1)));
+        b1 = gf_add(q2, gf_mul(rho, gf_add(q2, q3)));
+        Aout[2 * j] = a0; Aout[2 * j + 1] = a1;
+        Bout[2 * j] = b0; Bout[2 * j + 1] = b1;
+      } else {
+        a0 = A[2 * j]; a1 = A[2 * j + 1]; b0 = B[2 * j]; b1 = B[2 * j + 1];
+      }
+      gf128 e = eq_lo[j - base];
+      gf256_acc(l1, gf_mul_wide(e, gf_mul(a1, b1)));
+      gf256_acc(li, gf_mul_wide(e, gf_mul(gf_add(a0, a1), gf_add(b0, b1))));
+    }
+    gf128 eh = eq_hi[h];
+    gf256_acc(g1, gf_mul_wide(eh, gf256_reduce(l1)));
+    gf256_acc(gi, gf_mul_wide(eh, gf256_reduce(li)));
+  }
+  // block reduction of the two unreduced sums
+  __shared__ gf256 red[2][RND_THREADS / 32];
+  for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      g1.r[k] ^= __shfl_xor_sync(0xffffffffu, g1.r[k], off);
+      gi.r[k] ^= __shfl_xor_sync(0xffffffffu, gi.r[k], off);
+    }
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { red[0][warp] = g1; red[1][warp] = gi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    gf256 s1 = {{0, 0, 0, 0}}, si = {{0, 0, 0, 0}};
+    for (int w = 0; w < RND_THREADS / 32; w++) { gf256_acc(s1, red[0][w]); gf256_acc(si, red[1][w]); }
+    partials[2 * blockIdx.x] = gf256_reduce(s1);
+    partials[2 * blockIdx.x + 1] = gf256_reduce(si);
+  }
+}
+
+// Final bind of the last round: out[j] = A0 + rho (A0 + A1).
+__global__ void bind_pairs_kernel(const gf128* __restrict__ A, const gf128* __restrict__ B, size_t n, gf128 rho,
+                                  gf128* __restrict__ Aout, gf128* __restrict__ Bout) {
+  for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+    gf128 p0 = A[2 * j], p1 = A[2 * j + 1], q0 = B[2 * j], q1 = B[2 * j + 1];
+    Aout[j] = gf_add(p0, gf_mul(rho, gf_add(p0, p1)));
+    Bout[j] = gf_add(q0, gf_mul(rho, gf_add(q0, q1)));
+  }
+}
+
+}  // namespace
+
+int flock_launch_zc_round1(const void* a, const void* b, const void* c, size_t n_outer, const void* eq_out,
+                           const ZcRound1Tables* d_tables, void* partials, int grid, cudaStream_t st) {
+  size_t smem = 8 * 256 * 8 * 8 + 256 * 16 + (R1_THREADS / 32) * 2 * 16 * 16 * 8;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(zc_round1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  zc_round1_kernel<<<grid, R1_THREADS, smem, st>>>((const uint64_t*)a, (const uint64_t*)b, (const uint64_t*)c,
+                                                   n_outer, (const gf128*)eq_out, d_tables, (gf128*)partials);
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+int flock_zc_round1_warps(int grid) { return grid * (R1_THREADS / 32); }
+
+int flock_launch_reduce_rows(const void* in, size_t count, int width, void* out, cudaStream_t st) {
+  reduce_rows_kernel<<<(width + 127) / 128, 128, 0, st>>>((const gf128*)in, count, width, (gf128*)out);
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_launch_fold_skip(const void* a, const void* b, size_t rows, const void* lag, void* out_a, void* out_b,
+                           cudaStream_t st) {
+  size_t grid = (rows + 255) / 256;
+  if (grid > 152 * 16) grid = 152 * 16;
+  fold_skip_kernel<<<(unsigned)grid, 256, 0, st>>>((const uint64_t*)a, (const uint64_t*)b, rows, (const gf128*)lag,
+                                                   (gf128*)out_a, (gf128*)out_b);
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_launch_eq_split(const void* r, int lo_bits, int hi_bits, void* lo, void* hi, cudaStream_t st) {
+  size_t n = ((size_t)1 << lo_bits) + ((size_t)1 << hi_bits);
+  size_t grid = (n + 255) / 256;
+  if (grid > 4096) grid = 4096;
+  eq_split_kernel<<<(unsigned)grid, 256, 0, st>>>((const gf128*)r, lo_bits, hi_bits, (gf128*)lo, (gf128*)hi);
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_launch_zc_round(const void* A, const void* B, size_t n_pairs, int bind, const uint64_t rho[2],
+                          void* Aout, void* Bout, const void* eq_lo, const void* eq_hi, int lo_bits, void* partials,
+                          int grid, cudaStream_t st) {
+  gf128 r;
+  r.w[0] = (uint32_t)rho[0]; r.w[1] = (uint32_t)(rho[0] >> 32); r.w[2] = (uint32_t)rho[1]; r.w[3] = (uint32_t)(rho[1] >> 32);
+  zc_round_kernel<<<grid, RND_THREADS, 0, st>>>((const gf128*)A, (const gf128*)B, n_pairs, bind, r, (gf128*)Aout,
+                                                (gf128*)Bout, (const gf128*)eq_lo, (const gf128*)eq_hi, lo_bits,
+                                                (gf128*)partials);
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_launch_bind_pairs(const void* A, const void* B, size_t n, const uint64_t rho[2], void* Aout, void* Bout,
+                            cudaStream_t st) {
+  gf128 r;
+  r.w[0] = (uint32_t)rho[0]; r.w[1] = (uint32_t)(rho[0] >> 32); r.w[2] = (uint32_t)rho[1]; r.w[3] = (uint32_t)(rho[1] >> 32);
+  size_t grid = (n + 255) / 256;
+  if (grid > 152 * 8) grid = 152 * 8;
+  bind_pairs_kernel<<<(unsigned)grid, 256, 0, st>>>((const gf128*)A, (const gf128*)B, n, r, (gf128*)Aout,
+                                                    (gf128*)Bout);
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
