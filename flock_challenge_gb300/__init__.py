@@ -135,3 +135,59 @@ def merkle_tree(d_data, n_leaves, leaf_bytes, stream=None):
     check(lib().flock_merkle_tree(_dptr(d_data), n_leaves, leaf_bytes, _dptr(tree), _stream_ptr(stream)),
           "flock_merkle_tree")
     return tree
+
+
+def _proto_lib():
+    L = lib()
+    if not getattr(L, "_proto_ready", False):
+        P = ctypes.c_void_p
+        L.flock_setup.argtypes = [P, ctypes.c_size_t]
+        L.flock_prove.argtypes = [P, P, ctypes.c_size_t, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+        L.flock_last_phase_times.argtypes = [P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+        L._proto_ready = True
+    return L
+
+
+PHASES = ["setup", "commit", "zerocheck_round1", "zerocheck_rounds", "lincheck", "ring_switch", "ligerito",
+          "serialize"]
+
+
+class Blake3Setup:
+    """Prover for batched BLAKE3 compressions on one GPU.
+
+    Mirrors crates/flock-prover/src/r1cs_hashes/blake3.rs `Blake3Setup`:
+    ``Blake3Setup(n_blocks)`` then ``prove_fast(blocks)`` returning the
+    serialized proof bundle (R1csProofBundleLigerito::to_bytes). Blocks are a
+    numpy array of COMPRESSION_DTYPE records (cv, m, counter, block_len, flags).
+    """
+
+    def __init__(self, n_blocks, device=0):
+        if n_blocks < 1:
+            raise ValueError("n_blocks must be >= 1")
+        self.n_blocks = n_blocks
+        n = max(n_blocks, 8)
+        self.n_blocks_log = (n - 1).bit_length()
+        self.m = 14 + self.n_blocks_log
+        self.ctx = Context(device)
+        check(_proto_lib().flock_setup(self.ctx.handle, n_blocks), "flock_setup")
+        self._buf = np.zeros(1 << 20, np.uint8)
+
+    def prove_fast(self, blocks):
+        blocks = np.ascontiguousarray(blocks, dtype=COMPRESSION_DTYPE)
+        if len(blocks) != self.n_blocks:
+            raise ValueError(f"expected {self.n_blocks} blocks, got {len(blocks)}")
+        L = _proto_lib()
+        ln = ctypes.c_size_t()
+        rc = L.flock_prove(self.ctx.handle, blocks.ctypes.data_as(ctypes.c_void_p), len(blocks),
+                           self._buf.ctypes.data_as(ctypes.c_void_p), self._buf.size, ctypes.byref(ln))
+        if rc == -5:
+            self._buf = np.zeros(ln.value, np.uint8)
+            rc = L.flock_prove(self.ctx.handle, blocks.ctypes.data_as(ctypes.c_void_p), len(blocks),
+                               self._buf.ctypes.data_as(ctypes.c_void_p), self._buf.size, ctypes.byref(ln))
+        check(rc, "flock_prove")
+        return self._buf[:ln.value].tobytes()
+
+    def phase_times(self):
+        arr = (ctypes.c_double * 8)()
+        check(_proto_lib().flock_last_phase_times(self.ctx.handle, arr, 8), "flock_last_phase_times")
+        return dict(zip(PHASES, list(arr)))

@@ -1,12 +1,17 @@
 // C ABI entry points (include/flock_gpu.h) over the CUDA kernels.
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "flock_internal.h"
+#include "prover.h"
+#include "r1cs_setup.h"
 
 struct flock_ctx {
   int device = 0;
   size_t hbm_budget = 0;
+  ProverState* prover = nullptr;
+  std::vector<uint8_t> last_proof;
 };
 
 namespace {
@@ -31,7 +36,11 @@ int flock_create(int device, size_t hbm_budget, flock_ctx** out) {
   return FLOCK_OK;
 }
 
-void flock_destroy(flock_ctx* ctx) { delete ctx; }
+void flock_destroy(flock_ctx* ctx) {
+  if (!ctx) return;
+  flock_prover_destroy(ctx->prover);
+  delete ctx;
+}
 
 int flock_witness(const flock_compression* d_in, size_t n, int n_blocks_log, void* d_z, void* d_a, void* d_b,
                   void* d_stripe, void* stream) {
@@ -68,6 +77,44 @@ int flock_commit(flock_ctx* ctx, const void* d_z, int m, int log_inv_rate, int l
     if (cudaMemcpyAsync(root, d_root, 32, cudaMemcpyDeviceToHost, st) != cudaSuccess) return FLOCK_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return FLOCK_ERR_CUDA;
   }
+  return FLOCK_OK;
+}
+
+int flock_setup(flock_ctx* ctx, size_t n_blocks) {
+  if (!ctx || n_blocks == 0 || n_blocks > ((size_t)1 << 24)) return FLOCK_ERR_ARG;
+  size_t n = n_blocks < 8 ? 8 : n_blocks;
+  int n_log = 0;
+  while (((size_t)1 << n_log) < n) n_log++;
+  uint8_t d[32];
+  flock_statement_digest(14 + n_log, d);
+  flock_host_csc();
+  if (!ctx->prover) ctx->prover = flock_prover_create(ctx->device);
+  return ctx->prover ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_prove(flock_ctx* ctx, const flock_compression* in, size_t n, uint8_t* out, size_t cap, size_t* len) {
+  if (!ctx || !len || (n && !in)) return FLOCK_ERR_ARG;
+  size_t nn = n < 8 ? 8 : n;
+  int n_log = 0;
+  while (((size_t)1 << n_log) < nn) n_log++;
+  if (!ctx->prover) {
+    ctx->prover = flock_prover_create(ctx->device);
+    if (!ctx->prover) return FLOCK_ERR_CUDA;
+  }
+  int rc = flock_prover_prove(ctx->prover, in, n, n_log, ctx->last_proof);
+  if (rc != FLOCK_OK) return rc;
+  *len = ctx->last_proof.size();
+  if (!out || cap < ctx->last_proof.size()) return FLOCK_ERR_CAPACITY;
+  memcpy(out, ctx->last_proof.data(), ctx->last_proof.size());
+  return FLOCK_OK;
+}
+
+int flock_last_phase_times(const flock_ctx* ctx, double* ms, int n) {
+  if (!ctx || !ctx->prover || !ms) return FLOCK_ERR_ARG;
+  const FlockPhaseTimes& t = flock_prover_times(ctx->prover);
+  double v[8] = {t.setup_ms, t.commit_ms, t.zc_round1_ms, t.zc_rounds_ms, t.lincheck_ms, t.ring_switch_ms,
+                 t.ligerito_ms, t.serialize_ms};
+  for (int i = 0; i < n && i < 8; i++) ms[i] = v[i];
   return FLOCK_OK;
 }
 

@@ -21,3 +21,48 @@ int flock_launch_ntt(void* d_data, const void* d_src, int log_d, int log_num_ntt
 
 int flock_launch_merkle(const void* d_data, size_t n_leaves, size_t leaf_bytes, void* d_tree,
                         cudaStream_t stream);
+
+// ---- protocol kernels ------------------------------------------------------
+struct ZcRound1Tables;
+int flock_launch_zc_round1(const void* a, const void* b, const void* c, size_t n_outer, const void* eq_out,
+                           const ZcRound1Tables* d_tables, void* partials, int grid, cudaStream_t st);
+int flock_zc_round1_warps(int grid);
+int flock_launch_reduce_rows(const void* in, size_t count, int width, void* out, cudaStream_t st);
+int flock_launch_fold_skip(const void* a, const void* b, size_t rows, const void* lag, void* out_a, void* out_b,
+                           cudaStream_t st);
+int flock_launch_eq_split(const void* r, int lo_bits, int hi_bits, void* lo, void* hi, cudaStream_t st);
+int flock_launch_zc_round(const void* A, const void* B, size_t n_pairs, int bind, const uint64_t rho[2], void* Aout,
+                          void* Bout, const void* eq_lo, const void* eq_hi, int lo_bits, void* partials, int grid,
+                          cudaStream_t st);
+int flock_launch_bind_pairs(const void* A, const void* B, size_t n, const uint64_t rho[2], void* Aout, void* Bout,
+                            cudaStream_t st);
+
+int flock_launch_lc_partial_fold(const void* stripe, size_t n_stripes, const void* eq_lo, const void* eq_hi,
+                                 int lo_bits, void* partials, int grid, cudaStream_t st);
+int flock_launch_lc_comb(const uint32_t* a_ptr, const uint32_t* a_idx, const uint32_t* b_ptr,
+                         const uint32_t* b_idx, const void* eq, const uint64_t alpha[2], const uint64_t beta[2],
+                         int pin, void* comb, cudaStream_t st);
+int flock_launch_lc_quirky_eq(const void* lag, const void* x_rest, int n_rest, void* out, cudaStream_t st);
+int flock_launch_lc_round(void* c, void* z, size_t n, int bind, const uint64_t r[2], int emit, void* out,
+                          cudaStream_t st);
+
+int flock_launch_s_hat_v(const void* z, size_t n, const void* t_lo, const void* t_hi, int lo_bits, void* partials,
+                         int grid, cudaStream_t st);
+int flock_s_hat_v_warps(int grid);
+int flock_launch_combined_basis(size_t n, const void* t0_lo, const void* t0_hi, const void* t1_lo,
+                                const void* t1_hi, int lo_bits, const void* tables, void* b, cudaStream_t st);
+
+int flock_lig_grid(size_t n_pairs);
+int flock_launch_lig_fold_msg(const void* f, const void* b, size_t n_out, int fold, const uint64_t r[2], void* fo,
+                              void* bo, void* partials, int grid, cudaStream_t st);
+int flock_launch_lig_intro_eq(const void* f, size_t n, const void* lo, const void* hi, int lo_bits, void* partials,
+                              int grid, cudaStream_t st);
+int flock_launch_glue_eq(void* b, size_t n, const void* lo, const void* hi, int lo_bits, const uint64_t beta[2],
+                         cudaStream_t st);
+int flock_launch_glue(void* b, const void* add, size_t n, const uint64_t beta[2], cudaStream_t st);
+int flock_launch_induce_basis(const uint32_t* d_queries, int nq, int n, const void* sks, const void* inv_sks,
+                              const void* alpha_w, void* W, void* LO, void* HI, void* basis, cudaStream_t st);
+int flock_launch_gather_rows(const void* mat, const uint32_t* rows, int n_rows, int width, void* out,
+                             cudaStream_t st);
+int flock_launch_gather_nodes(const void* tree, const uint32_t* idx, int n, void* out, cudaStream_t st);
+int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, cudaStream_t st, uint64_t* nonce);

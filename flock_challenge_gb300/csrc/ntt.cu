@@ -7,7 +7,7 @@
 // t(l, b) = table[2^l - 1 + b]; butterfly u += v*t, v += u.
 //
 // GB300 mapping: a pass applies F consecutive layers to a tile of 2^F
-// positions x 16 lanes held in shared memory. The tile's positions differ only
+// positions x 16 lanes (8 when the code has 8 lanes) held in shared memory. The tile's positions differ only
 // in the F pair bits of those layers, so every butterfly of the pass stays in
 // the tile and the pass costs one HBM read and one write of the codeword.
 // Each tile row (16 lanes x 16 B) is a contiguous 256-byte run, read and
@@ -26,10 +26,9 @@
 
 namespace {
 
-constexpr int TILE_LANES = 16;
 constexpr int NTT_THREADS = 256;
 
-template <int F>
+template <int F, int TILE_LANES>
 __global__ void __launch_bounds__(NTT_THREADS)
 ntt_pass_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t src_pos_mask,
                 const gf128* __restrict__ tw, int log_d, int log_lanes, int l0) {
@@ -107,8 +106,13 @@ template <int F>
 int launch_pass(gf128* dst, const gf128* src, size_t mask, const gf128* tw, int log_d, int log_lanes, int l0,
                 cudaStream_t st) {
   size_t tiles = (size_t)1 << (log_d - F);
-  size_t blocks = tiles * ((1 << log_lanes) / TILE_LANES);
-  ntt_pass_kernel<F><<<(unsigned)blocks, NTT_THREADS, 0, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
+  if (log_lanes >= 4) {
+    size_t blocks = tiles * ((1 << log_lanes) / 16);
+    ntt_pass_kernel<F, 16><<<(unsigned)blocks, NTT_THREADS, 0, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
+  } else {
+    size_t blocks = tiles * ((1 << log_lanes) / 8);
+    ntt_pass_kernel<F, 8><<<(unsigned)blocks, NTT_THREADS, 0, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
+  }
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
@@ -151,7 +155,7 @@ const void* flock_ntt_twiddles(int log_d) {
 // message of a rate-1/2^start_layer code.
 int flock_launch_ntt(void* d_data, const void* d_src, int log_d, int log_lanes, int start_layer,
                      cudaStream_t stream) {
-  if (log_lanes < 4 || log_lanes > 10 || log_d < 1 || log_d > 30 || start_layer < 0 || start_layer > log_d)
+  if (log_lanes < 3 || log_lanes > 10 || log_d < 1 || log_d > 30 || start_layer < 0 || start_layer > log_d)
     return FLOCK_ERR_SHAPE;
   const gf128* tw = (const gf128*)flock_ntt_twiddles(log_d);
   if (!tw) return FLOCK_ERR_OOM;

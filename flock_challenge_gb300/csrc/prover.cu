@@ -1,0 +1,852 @@
+// Full proof orchestration on one GPU.
+//
+// Follows Blake3Setup::prove_fast (crates/flock-prover/src/r1cs_hashes/blake3.rs:3405-3642)
+// and prove_ligerito (crates/flock-prover/src/prover.rs:194-289): witness ->
+// PCS commit -> bind_statement -> zerocheck -> lincheck -> ring switch of the
+// [ab, c] claims -> recursive Ligerito opening -> wire bytes
+// (crates/flock-prover/src/proof_io.rs:161-208). All bulk work runs in the
+// kernels of this library; the host keeps the Fiat-Shamir transcript and the
+// O(1)-sized algebra between rounds (Lagrange weights, 64/128-entry vectors).
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <set>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "flock_internal.h"
+#include "host_field.h"
+#include "prover.h"
+#include "r1cs_setup.h"
+#include "transcript.h"
+#include "zc_tables.h"
+
+namespace {
+
+using hf::F;
+
+#include "ligerito_params.inc"
+
+struct LigCfg {
+  int initial_k = 0, yr_log_n = 0, steps = 0;
+  std::vector<int> rates, ks, queries, grind_bits, fold_bits, ood;
+};
+
+bool lig_config(int m, int profile, LigCfg& c) {
+  for (int i = 0; i < LIGERITO_N_CONFIGS; i++) {
+    const int* row = LIGERITO_CONFIGS[i];
+    if (row[0] != m || row[1] != profile) continue;
+    c = LigCfg();
+    c.initial_k = row[2];
+    c.yr_log_n = row[3];
+    int nl = row[4];
+    c.steps = nl - 1;
+    for (int l = 0; l < nl; l++) {
+      const int* L = row + 5 + 8 * l;
+      c.rates.push_back(L[0]);
+      if (l > 0) c.ks.push_back(L[3]);
+      c.queries.push_back(L[4]);
+      c.grind_bits.push_back(L[5]);
+      c.fold_bits.push_back(L[6]);
+      c.ood.push_back(L[7]);
+    }
+    return true;
+  }
+  return false;
+}
+
+struct Fail : std::runtime_error {
+  int code;
+  Fail(int c, const std::string& w) : std::runtime_error(w), code(c) {}
+};
+#define CK(x)                                                              \
+  do {                                                                     \
+    cudaError_t e_ = (x);                                                  \
+    if (e_ != cudaSuccess) throw Fail(FLOCK_ERR_CUDA, cudaGetErrorString(e_)); \
+  } while (0)
+#define FK(x)                                      \
+  do {                                             \
+    int r_ = (x);                                  \
+    if (r_ != FLOCK_OK) throw Fail(r_, #x);        \
+  } while (0)
+
+struct DBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  ~DBuf() {
+    if (p) cudaFree(p);
+  }
+  void* get(size_t b) {
+    if (b > bytes) {
+      if (p) cudaFree(p);
+      p = nullptr;
+      bytes = 0;
+      if (cudaMalloc(&p, b) != cudaSuccess) throw Fail(FLOCK_ERR_OOM, "cudaMalloc");
+      bytes = b;
+    }
+    return p;
+  }
+};
+
+inline int ilog2(size_t n) {
+  int l = 0;
+  while (((size_t)1 << l) < n) l++;
+  return l;
+}
+
+// ---------------------------------------------------------------- host algebra
+std::vector<F> eq_table(const std::vector<F>& r) {
+  std::vector<F> t((size_t)1 << r.size());
+  t[0] = F::one();
+  for (size_t i = 0; i < r.size(); i++) {
+    size_t h = (size_t)1 << i;
+    for (size_t j = 0; j < h; j++) {
+      F vr = t[j] * r[i];
+      t[j + h] = vr;
+      t[j] = t[j] + vr;
+    }
+  }
+  return t;
+}
+
+// Lagrange weights on 64 nodes phi8(off..off+63) (multilinear.rs:361-520),
+// prefix/suffix products with cached denominators.
+struct Lagrange {
+  std::vector<F> den_inv[2];
+  Lagrange() {
+    for (int k = 0; k < 2; k++) {
+      den_inv[k].resize(64);
+      for (int i = 0; i < 64; i++) {
+        F si = hf::phi8((uint8_t)(64 * k + i)), d = F::one();
+        for (int j = 0; j < 64; j++)
+          if (j != i) d = d * (si + hf::phi8((uint8_t)(64 * k + j)));
+        den_inv[k][i] = hf::inv(d);
+      }
+    }
+  }
+  std::vector<F> at(F z, int which) const {
+    std::vector<F> w(64);
+    F pre = F::one();
+    for (int i = 0; i < 64; i++) {
+      w[i] = pre;
+      pre = pre * (z + hf::phi8((uint8_t)(64 * which + i)));
+    }
+    F suf = F::one();
+    for (int i = 63; i >= 0; i--) {
+      w[i] = w[i] * suf * den_inv[which][i];
+      suf = suf * (z + hf::phi8((uint8_t)(64 * which + i)));
+    }
+    return w;
+  }
+};
+const Lagrange& lagrange() {
+  static const Lagrange L;
+  return L;
+}
+
+// phi8(M[i][s]) for the S -> Lambda extension matrix, cached.
+const std::vector<F>& phi_ext_matrix() {
+  static const std::vector<F> pm = [] {
+    auto M = zc::ext_matrix();
+    std::vector<F> v(64 * 64);
+    for (int i = 0; i < 64 * 64; i++) v[i] = hf::phi8(M[i]);
+    return v;
+  }();
+  return pm;
+}
+
+F dot(const F* a, const F* b, size_t n) {
+  F s;
+  for (size_t i = 0; i < n; i++) s += a[i] * b[i];
+  return s;
+}
+
+std::vector<F> transpose128(const std::vector<F>& v) {
+  std::vector<F> u(128);
+  for (int i = 0; i < 128; i++)
+    for (int b = 0; b < 128; b++) {
+      uint64_t bit = b < 64 ? (v[i].lo >> b) & 1 : (v[i].hi >> (b - 64)) & 1;
+      if (bit) {
+        if (i < 64) u[b].lo |= 1ULL << i;
+        else u[b].hi |= 1ULL << (i - 64);
+      }
+    }
+  return u;
+}
+
+// s_k(v_k) and inverses, ligerito.rs:1747-1774.
+struct Sks {
+  std::vector<F> s, inv;
+};
+const Sks& sks_for(int n) {
+  static std::vector<Sks> cache(64);
+  static std::vector<bool> have(64, false);
+  if (!have[n]) {
+    Sks r;
+    r.s.assign(n + 1, F());
+    r.s[0] = F::one();
+    std::vector<F> layer;
+    for (int i = 1; i <= n; i++) layer.push_back(F(1ULL << i, 0));
+    int cur = n;
+    for (int i = 0; i < n; i++) {
+      for (int j = 0; j < cur; j++) {
+        F v = layer[j] * layer[j] + r.s[i] * layer[j];
+        if (j == 0) r.s[i + 1] = v;
+        else layer[j - 1] = v;
+      }
+      cur--;
+    }
+    for (auto& v : r.s) r.inv.push_back(v.zero() ? F() : hf::inv(v));
+    cache[n] = r;
+    have[n] = true;
+  }
+  return cache[n];
+}
+
+std::vector<uint32_t> sample_queries(fs::Transcript& tr, size_t block_len, size_t count) {
+  std::set<uint32_t> seen;
+  std::vector<uint32_t> out;
+  while (out.size() < count) {
+    F v = tr.sample();
+    uint32_t q = (uint32_t)(v.lo % block_len);
+    if (seen.insert(q).second) out.push_back(q);
+  }
+  std::sort(out.begin(), out.end());
+  return out;
+}
+
+// Node indices of the octopus multi-proof (crates/flock-core/src/merkle.rs:879-928)
+// in emission order, for sorted unique positions.
+std::vector<uint32_t> multiproof_nodes(size_t n_leaves, const std::vector<uint32_t>& pos) {
+  std::vector<uint32_t> out;
+  if (pos.empty() || n_leaves == 1) return out;
+  std::vector<uint32_t> act(pos);
+  size_t ls = 0, ll = n_leaves;
+  while (ll > 1) {
+    std::vector<uint32_t> nxt;
+    size_t i = 0;
+    while (i < act.size()) {
+      uint32_t p = act[i];
+      bool sib = i + 1 < act.size() && act[i + 1] == (p ^ 1u);
+      if (sib) i += 2;
+      else {
+        out.push_back((uint32_t)(ls + (p ^ 1u)));
+        i += 1;
+      }
+      nxt.push_back(p >> 1);
+    }
+    act.swap(nxt);
+    ls += ll;
+    ll >>= 1;
+  }
+  return out;
+}
+
+// ---------------------------------------------------------------- wire writer
+struct Wire {
+  std::vector<uint8_t> v;
+  void raw(const void* p, size_t n) { v.insert(v.end(), (const uint8_t*)p, (const uint8_t*)p + n); }
+  void u32(uint32_t x) { raw(&x, 4); }
+  void u64(uint64_t x) { raw(&x, 8); }
+  void f(F x) { u64(x.lo); u64(x.hi); }
+  void fv(const F* p, size_t n) { u64(n); raw(p, 16 * n); }
+  void fv(const std::vector<F>& x) { fv(x.data(), x.size()); }
+  void pv(const std::vector<std::pair<F, F>>& x) {
+    u64(x.size());
+    for (auto& e : x) { f(e.first); f(e.second); }
+  }
+};
+
+struct Open {
+  std::vector<F> rows;  // q x width
+  size_t width = 0;
+  std::vector<uint8_t> nodes;  // 32-byte hashes
+};
+
+}  // namespace
+
+// ============================================================================
+struct ProverState {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  ZcRound1Tables* d_r1t = nullptr;
+  DBuf in, z, a, b, stripe, cw, tree, A0, B0, A1, B1, eqlo, eqhi, eqout, rdev, part, red, lag, small, eqin, comb,
+      zvec, lcmsg, tlo0, thi0, tlo1, thi1, tables, bc, f1, b1, W, LO, HI, basis, qbuf, abuf, rows, nidx, nodes,
+      grind, lvl_cw[2], lvl_tree[2];
+  DBuf csc_ap, csc_ai, csc_bp, csc_bi;
+  bool csc_ready = false;
+  FlockPhaseTimes times;
+};
+
+namespace {
+
+void h2d(void* d, const void* h, size_t n, cudaStream_t st) { CK(cudaMemcpyAsync(d, h, n, cudaMemcpyHostToDevice, st)); }
+void d2h(void* h, const void* d, size_t n, cudaStream_t st) {
+  CK(cudaMemcpyAsync(h, d, n, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+}
+void u2(const F& x, uint64_t out[2]) { out[0] = x.lo; out[1] = x.hi; }
+
+struct Clock {
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  double lap() {
+    auto n = std::chrono::steady_clock::now();
+    double ms = std::chrono::duration<double, std::milli>(n - t).count();
+    t = n;
+    return ms;
+  }
+};
+
+// Ligero commit of poly (device, length 2^(lmc+lni)) into (cw, tree); returns root.
+void ligero_commit(ProverState& S, const void* poly, int lmc, int lni, int rate, void* cw, void* tree,
+                   uint8_t root[32]) {
+  int log_d = lmc + rate;
+  FK(flock_launch_ntt(cw, poly, log_d, lni, rate, S.st));
+  size_t leaves = (size_t)1 << log_d;
+  FK(flock_launch_merkle(cw, leaves, (size_t)16 << lni, tree, S.st));
+  d2h(root, (const uint8_t*)tree + (2 * leaves - 2) * 32, 32, S.st);
+}
+
+Open open_rows(ProverState& S, const void* cw, const void* tree, size_t block_len, int width,
+               const std::vector<uint32_t>& q) {
+  Open o;
+  o.width = width;
+  uint32_t* dq = (uint32_t*)S.qbuf.get(q.size() * 4);
+  h2d(dq, q.data(), q.size() * 4, S.st);
+  void* dr = S.rows.get(q.size() * width * 16);
+  FK(flock_launch_gather_rows(cw, dq, (int)q.size(), width, dr, S.st));
+  o.rows.resize(q.size() * width);
+  d2h(o.rows.data(), dr, o.rows.size() * 16, S.st);
+  auto idx = multiproof_nodes(block_len, q);
+  o.nodes.resize(idx.size() * 32);
+  if (!idx.empty()) {
+    uint32_t* di = (uint32_t*)S.nidx.get(idx.size() * 4);
+    h2d(di, idx.data(), idx.size() * 4, S.st);
+    void* dn = S.nodes.get(idx.size() * 32);
+    FK(flock_launch_gather_nodes(tree, di, (int)idx.size(), dn, S.st));
+    d2h(o.nodes.data(), dn, o.nodes.size(), S.st);
+  }
+  return o;
+}
+
+void write_open(Wire& w, const Open& o) {
+  size_t nq = o.width ? o.rows.size() / o.width : 0;
+  w.u64(nq);
+  for (size_t i = 0; i < nq; i++) w.fv(&o.rows[i * o.width], o.width);
+  w.u64(o.nodes.size() / 32);
+  w.raw(o.nodes.data(), o.nodes.size());
+}
+
+// Reduce `count` partial rows of `width` F128 on the device, copy to host.
+std::vector<F> reduce_partials(ProverState& S, const void* part, size_t count, int width) {
+  void* r = S.red.get((size_t)width * 16);
+  FK(flock_launch_reduce_rows(part, count, width, r, S.st));
+  std::vector<F> out(width);
+  d2h(out.data(), r, (size_t)width * 16, S.st);
+  return out;
+}
+
+void eq_split_dev(ProverState& S, const std::vector<F>& r, int lo_bits, DBuf& lo, DBuf& hi) {
+  int hi_bits = (int)r.size() - lo_bits;
+  void* dr = S.rdev.get(r.size() * 16 + 16);
+  h2d(dr, r.data(), r.size() * 16, S.st);
+  FK(flock_launch_eq_split(dr, lo_bits, hi_bits, lo.get((size_t)16 << lo_bits), hi.get((size_t)16 << hi_bits), S.st));
+}
+
+}  // namespace
+
+ProverState* flock_prover_create(int device) {
+  ProverState* S = new ProverState;
+  S->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&S->st, cudaStreamNonBlocking) != cudaSuccess) {
+    delete S;
+    return nullptr;
+  }
+  return S;
+}
+
+void flock_prover_destroy(ProverState* S) {
+  if (!S) return;
+  cudaSetDevice(S->device);
+  if (S->d_r1t) cudaFree(S->d_r1t);
+  if (S->st) cudaStreamDestroy(S->st);
+  delete S;
+}
+
+const FlockPhaseTimes& flock_prover_times(const ProverState* S) { return S->times; }
+
+int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, int n_log, std::vector<uint8_t>& out) {
+  try {
+    CK(cudaSetDevice(S->device));
+    const int m = 14 + n_log;
+    LigCfg cfg;
+    if (!lig_config(m, 0, cfg)) return FLOCK_ERR_SHAPE;
+    if (n > ((size_t)1 << n_log) || n_log < 8) return FLOCK_ERR_SHAPE;
+    cudaStream_t st = S->st;
+    FlockPhaseTimes& T = S->times;
+    T = FlockPhaseTimes();
+    Clock clk;
+    // ---- setup constants (cached) ----
+    uint8_t digest[32];
+    flock_statement_digest(m, digest);
+    if (!S->d_r1t) {
+      ZcRound1Tables* h = new ZcRound1Tables;
+      zc::build_round1_tables(*h);
+      CK(cudaMalloc(&S->d_r1t, sizeof(ZcRound1Tables)));
+      CK(cudaMemcpy(S->d_r1t, h, sizeof(ZcRound1Tables), cudaMemcpyHostToDevice));
+      delete h;
+    }
+    if (!S->csc_ready) {
+      const HostCsc& c = flock_host_csc();
+      h2d(S->csc_ap.get(c.a_ptr.size() * 4), c.a_ptr.data(), c.a_ptr.size() * 4, st);
+      h2d(S->csc_ai.get(c.a_idx.size() * 4), c.a_idx.data(), c.a_idx.size() * 4, st);
+      h2d(S->csc_bp.get(c.b_ptr.size() * 4), c.b_ptr.data(), c.b_ptr.size() * 4, st);
+      h2d(S->csc_bi.get(c.b_idx.size() * 4), c.b_idx.data(), c.b_idx.size() * 4, st);
+      CK(cudaStreamSynchronize(st));
+      S->csc_ready = true;
+    }
+    const Lagrange& LG = lagrange();
+    T.setup_ms = clk.lap();
+
+    // ---- witness + commit ----
+    const size_t nbits = (size_t)1 << m, nbytes = nbits / 8, n128 = nbits / 128;
+    void* d_in = S->in.get(std::max<size_t>(n, 1) * sizeof(flock_compression));
+    if (n) h2d(d_in, h_in, n * sizeof(flock_compression), st);
+    void *dz = S->z.get(nbytes), *da = S->a.get(nbytes), *db = S->b.get(nbytes), *ds = S->stripe.get(nbytes);
+    FK(flock_launch_witness((const flock_compression*)d_in, n, n_log, dz, da, db, ds, st));
+    const int lbs = 6, rate0 = 1;
+    const int log_d0 = m - 7 - lbs + rate0;
+    const size_t block0 = (size_t)1 << log_d0;
+    void* dcw = S->cw.get((n128 << rate0) * 16);
+    void* dtree = S->tree.get((2 * block0 - 1) * 32);
+    FK(flock_launch_ntt(dcw, dz, log_d0, lbs, rate0, st));
+    FK(flock_launch_merkle(dcw, block0, (size_t)16 << lbs, dtree, st));
+    uint8_t root0[32];
+    d2h(root0, (const uint8_t*)dtree + (2 * block0 - 2) * 32, 32, st);
+    T.commit_ms = clk.lap();
+
+    Wire w;
+    w.raw("FLOCK", 5);
+    uint8_t ver[2] = {4, 2};
+    w.raw(ver, 2);
+    w.raw(root0, 32);
+    w.u64(m);
+    w.u64(rate0);
+    w.u64(lbs);
+    w.u32(0);  // LigeritoProfile::Fast
+    w.u32(1);  // HashKind::Blake3
+
+    fs::Transcript tr("flock-bench-v0");
+    // bind_statement (crates/flock-core/src/proof.rs:51-59)
+    tr.label("flock-r1cs-v0");
+    tr.observe_bytes(digest, 32);
+    tr.observe_bytes(root0, 32);
+
+    // ---- zerocheck ----
+    tr.label("flock-zerocheck-v0");
+    std::vector<F> r(m);
+    {
+      auto rs = tr.sample_vec(6);
+      auto ro = tr.sample_vec(m - 13);
+      for (int i = 0; i < 6; i++) r[i] = rs[i];
+      for (int i = 0; i < 3; i++) r[6 + i] = hf::phi8(zc::SMALL_CHAL[i]);
+      for (int i = 0; i < 4; i++) {
+        F g(1ULL << (1 << i), 0);
+        r[9 + i] = g * hf::inv(F::one() + g);
+      }
+      for (int i = 13; i < m; i++) r[i] = ro[i - 13];
+    }
+    std::vector<F> p_ab(64), p_c(64);
+    {
+      const size_t rows = nbits / 64, n_outer = rows / 128;
+      std::vector<F> rout(r.begin() + 13, r.end());
+      int nv = (int)rout.size();
+      void* dr = S->rdev.get(rout.size() * 16 + 16);
+      h2d(dr, rout.data(), rout.size() * 16, st);
+      void* deq = S->eqout.get(n_outer * 16);
+      FK(flock_launch_eq_split(dr, nv, 0, deq, S->eqhi.get(16), st));
+      const int grid = 152;
+      int nw = flock_zc_round1_warps(grid);
+      void* dpart = S->part.get((size_t)nw * 128 * 16);
+      FK(flock_launch_zc_round1(da, db, dz, n_outer, deq, S->d_r1t, dpart, grid, st));
+      auto sums = reduce_partials(*S, dpart, nw, 128);
+      F dinv = zc::medium_dinv();
+      const std::vector<F>& PM = phi_ext_matrix();
+      std::vector<F> cs(64);
+      for (int s = 0; s < 64; s++) cs[s] = dinv * sums[64 + s];
+      for (int i = 0; i < 64; i++) {
+        p_ab[i] = dinv * sums[i];
+        p_c[i] = dot(&PM[i * 64], cs.data(), 64);
+      }
+    }
+    T.zc_round1_ms = clk.lap();
+    tr.observe_slice(p_ab.data(), 64);
+    tr.observe_slice(p_c.data(), 64);
+    F zc_z = tr.sample();
+    F final_c;
+    {
+      auto wl = LG.at(zc_z, 1);
+      final_c = dot(wl.data(), p_c.data(), 64);
+    }
+    auto lag_z = LG.at(zc_z, 0);
+    const size_t rows0 = nbits / 64;
+    void *dA0 = S->A0.get(rows0 * 16), *dB0 = S->B0.get(rows0 * 16);
+    void *dA1 = S->A1.get(rows0 / 2 * 16), *dB1 = S->B1.get(rows0 / 2 * 16);
+    void* dlag = S->lag.get(64 * 16);
+    h2d(dlag, lag_z.data(), 64 * 16, st);
+    FK(flock_launch_fold_skip(da, db, rows0, dlag, dA0, dB0, st));
+    const int n_mlv = m - 6;
+    std::vector<std::pair<F, F>> zc_rounds;
+    std::vector<F> rho;
+    void *curA = dA0, *curB = dB0, *nxtA = dA1, *nxtB = dB1;
+    for (int i = 0; i < n_mlv; i++) {
+      size_t n_pairs = rows0 >> (i + 1);  // pairs of the round-i table
+      std::vector<F> rr(r.begin() + 6 + i + 1, r.end());
+      int nv = (int)rr.size();
+      int lob = std::min(nv, 12);
+      eq_split_dev(*S, rr, lob, S->eqlo, S->eqhi);
+      int grid = (int)std::min<size_t>(((n_pairs >> lob) + 0), 152 * 4);
+      if (grid < 1) grid = 1;
+      void* dpart = S->part.get((size_t)grid * 2 * 16);
+      uint64_t rp[2] = {0, 0};
+      if (i > 0) u2(rho.back(), rp);
+      FK(flock_launch_zc_round(curA, curB, n_pairs, i > 0, rp, nxtA, nxtB, S->eqlo.p, S->eqhi.p, lob, dpart, grid, st));
+      if (i > 0) {
+        std::swap(curA, nxtA);
+        std::swap(curB, nxtB);
+      }
+      auto g = reduce_partials(*S, dpart, grid, 2);
+      zc_rounds.push_back({g[0], g[1]});
+      tr.observe(g[0]);
+      tr.observe(g[1]);
+      rho.push_back(tr.sample());
+    }
+    F fa, fb;
+    {
+      uint64_t rp[2];
+      u2(rho.back(), rp);
+      FK(flock_launch_bind_pairs(curA, curB, 1, rp, nxtA, nxtB, st));
+      d2h(&fa, nxtA, 16, st);
+      d2h(&fb, nxtB, 16, st);
+    }
+    tr.observe(fa);
+    tr.observe(fb);
+    T.zc_rounds_ms = clk.lap();
+    w.fv(p_ab);
+    w.fv(p_c);
+    w.pv(zc_rounds);
+    w.f(fa);
+    w.f(fb);
+    w.f(final_c);
+
+    // ---- lincheck ----
+    const int inner_rest = 14 - 6, n_outer_log = m - 14;
+    std::vector<F> x_in(rho.begin(), rho.begin() + inner_rest), x_out(rho.begin() + inner_rest, rho.end());
+    tr.label("flock-lincheck-v0");
+    F alpha = tr.sample();
+    F beta = tr.sample();
+    std::vector<F> lc_rr;
+    std::vector<std::pair<F, F>> lc_rounds;
+    std::vector<F> z_partial(64);
+    {
+      void* dxr = S->small.get(inner_rest * 16);
+      h2d(dxr, x_in.data(), inner_rest * 16, st);
+      void* deqin = S->eqin.get(FLOCK_K * 16);
+      FK(flock_launch_lc_quirky_eq(dlag, dxr, inner_rest, deqin, st));
+      void* dcomb = S->comb.get(FLOCK_K * 16);
+      uint64_t al[2], be[2];
+      u2(alpha, al);
+      u2(beta, be);
+      FK(flock_launch_lc_comb((const uint32_t*)S->csc_ap.p, (const uint32_t*)S->csc_ai.p, (const uint32_t*)S->csc_bp.p,
+                              (const uint32_t*)S->csc_bi.p, deqin, al, be, 512, dcomb, st));
+      int lob = n_outer_log / 2;
+      eq_split_dev(*S, x_out, lob, S->eqlo, S->eqhi);
+      size_t n_stripes = ((size_t)1 << n_outer_log) / 8;
+      int grid = (int)std::min<size_t>(n_stripes, 152);
+      void* dpart = S->part.get((size_t)grid * FLOCK_K * 16);
+      FK(flock_launch_lc_partial_fold(ds, n_stripes, S->eqlo.p, S->eqhi.p, lob, dpart, grid, st));
+      void* dzv = S->zvec.get(FLOCK_K * 16);
+      FK(flock_launch_reduce_rows(dpart, grid, FLOCK_K, dzv, st));
+      void* dmsg = S->lcmsg.get(32);
+      size_t len = FLOCK_K;
+      for (int t = 0; t < inner_rest; t++) {
+        uint64_t rp[2] = {0, 0};
+        if (t > 0) u2(lc_rr.back(), rp);
+        if (t > 0) len /= 2;
+        FK(flock_launch_lc_round(dcomb, dzv, len, t > 0, rp, 1, dmsg, st));
+        F msg[2];
+        d2h(msg, dmsg, 32, st);
+        tr.observe(msg[0]);
+        tr.observe(msg[1]);
+        lc_rounds.push_back({msg[0], msg[1]});
+        lc_rr.push_back(tr.sample());
+      }
+      uint64_t rp[2];
+      u2(lc_rr.back(), rp);
+      FK(flock_launch_lc_round(dcomb, dzv, len / 2, 1, rp, 0, dmsg, st));
+      d2h(z_partial.data(), dzv, 64 * 16, st);
+    }
+    tr.observe_slice(z_partial.data(), 64);
+    F r_inner_skip = tr.sample();
+    F lc_w;
+    {
+      auto l2 = LG.at(r_inner_skip, 0);
+      lc_w = dot(l2.data(), z_partial.data(), 64);
+    }
+    std::vector<F> r_inner_rest(lc_rr.rbegin(), lc_rr.rend());
+    (void)lc_w;
+    T.lincheck_ms = clk.lap();
+    w.pv(lc_rounds);
+    w.fv(z_partial);
+
+    // ---- PCS open: ring switch of [ab, c] (pcs.rs:1025-1110) ----
+    tr.label("flock-pcs-open-batch-v0");
+    std::vector<F> x_ab(r_inner_rest);
+    x_ab.insert(x_ab.end(), x_out.begin(), x_out.end());
+    std::vector<F> x_c(r.begin() + 6, r.end());
+    const std::vector<F>* xs[2] = {&x_ab, &x_c};
+    DBuf* tlo[2] = {&S->tlo0, &S->tlo1};
+    DBuf* thi[2] = {&S->thi0, &S->thi1};
+    std::vector<F> s_hat[2], eqr[2];
+    F claims[2];
+    const int L = m - 7;
+    const int rs_lo = std::min(13, L - 1);
+    for (int k = 0; k < 2; k++) {
+      tr.label("flock-ring-switch-v0");
+      std::vector<F> suffix(xs[k]->begin() + 1, xs[k]->end());
+      eq_split_dev(*S, suffix, rs_lo, *tlo[k], *thi[k]);
+      int grid = 512;
+      int nwp = flock_s_hat_v_warps(grid);
+      void* dpart = S->part.get((size_t)nwp * 128 * 16);
+      FK(flock_launch_s_hat_v(dz, n128, tlo[k]->p, thi[k]->p, rs_lo, dpart, grid, st));
+      s_hat[k] = reduce_partials(*S, dpart, nwp, 128);
+      tr.observe_slice(s_hat[k].data(), 128);
+      auto rpp = tr.sample_vec(7);
+      eqr[k] = eq_table(rpp);
+      auto u = transpose128(s_hat[k]);
+      claims[k] = dot(u.data(), eqr[k].data(), 128);
+    }
+    F gam[2] = {tr.sample(), tr.sample()};
+    F target = gam[0] * claims[0] + gam[1] * claims[1];
+    void* dbc = S->bc.get(n128 * 16);
+    {
+      std::vector<F> tabs(2 * 16 * 256);
+      for (int k = 0; k < 2; k++) {
+        for (int q = 0; q < 16; q++) {
+          F* t = &tabs[(k * 16 + q) * 256];
+          t[0] = F();
+          for (int v = 1; v < 256; v++) {
+            int low = __builtin_ctz(v);
+            t[v] = t[v & (v - 1)] + gam[k] * eqr[k][8 * q + low];
+          }
+        }
+      }
+      void* dt = S->tables.get(tabs.size() * 16);
+      h2d(dt, tabs.data(), tabs.size() * 16, st);
+      FK(flock_launch_combined_basis(n128, S->tlo0.p, S->thi0.p, S->tlo1.p, S->thi1.p, rs_lo, dt, dbc, st));
+    }
+    T.ring_switch_ms = clk.lap();
+    w.u64(2);
+    w.fv(s_hat[0]);
+    w.fv(s_hat[1]);
+
+    // ---- Ligerito (ligerito.rs:6222-6980) ----
+    tr.label("flock-ligerito-basis-v0");
+    tr.observe(target);
+    tr.observe_bytes(root0, 32);
+    std::vector<std::pair<F, F>> msgs;
+    std::vector<uint64_t> grind_nonces, fold_nonces;
+    std::vector<F> ood_vals;
+    void* dgr = S->grind.get(64);
+    auto grind = [&](uint32_t bits) {
+      uint8_t dg[32];
+      tr.digest(dg);
+      uint64_t nonce = 0;
+      FK(flock_grind(dg, bits, dgr, st, &nonce));
+      tr.absorb_nonce(nonce);
+      return nonce;
+    };
+    const int log_n = m - 7;
+    // state: f in (fa_buf), b in (fb_buf), length len
+    void* fcur = dz;  // the packed witness is consumed by the opening
+    void* bcur = dbc;
+    void* falt = S->f1.get(n128 / 2 * 16);
+    void* balt = S->b1.get(n128 / 2 * 16);
+    size_t len = n128;
+    auto run_msg = [&](int fold, F rr) {
+      size_t n_out = fold ? len / 2 : len;
+      int grid = flock_lig_grid(n_out / 2);
+      void* dpart = S->part.get((size_t)grid * 3 * 16);
+      uint64_t rp[2];
+      u2(rr, rp);
+      if (fold) {
+        FK(flock_launch_lig_fold_msg(fcur, bcur, n_out, 1, rp, falt, balt, dpart, grid, st));
+        std::swap(fcur, falt);
+        std::swap(bcur, balt);
+        len = n_out;
+      } else {
+        FK(flock_launch_lig_fold_msg(fcur, bcur, n_out, 0, rp, nullptr, nullptr, dpart, grid, st));
+      }
+      auto s = reduce_partials(*S, dpart, grid, 3);
+      msgs.push_back({s[0], s[1]});
+      tr.observe(s[0]);
+      tr.observe(s[1]);
+    };
+    auto introduce = [&](const void* dbasis) {
+      int grid = flock_lig_grid(len / 2);
+      void* dpart = S->part.get((size_t)grid * 3 * 16);
+      uint64_t rp[2] = {0, 0};
+      FK(flock_launch_lig_fold_msg(fcur, dbasis, len, 0, rp, nullptr, nullptr, dpart, grid, st));
+      auto s = reduce_partials(*S, dpart, grid, 3);
+      msgs.push_back({s[0], s[1]});
+      tr.observe(s[0]);
+      tr.observe(s[1]);
+      F bt = tr.sample();
+      uint64_t bp[2];
+      u2(bt, bp);
+      FK(flock_launch_glue(bcur, dbasis, len, bp, st));
+    };
+    auto ood = [&](int count) {
+      for (int o = 0; o < count; o++) {
+        int nv = ilog2(len);
+        auto zp = tr.sample_vec(nv);
+        int lob = std::min(nv, 12);
+        eq_split_dev(*S, zp, lob, S->eqlo, S->eqhi);
+        int grid = flock_lig_grid(len / 2);
+        void* dpart = S->part.get((size_t)grid * 3 * 16);
+        FK(flock_launch_lig_intro_eq(fcur, len, S->eqlo.p, S->eqhi.p, lob, dpart, grid, st));
+        auto s = reduce_partials(*S, dpart, grid, 3);
+        tr.observe(s[2]);
+        ood_vals.push_back(s[2]);
+        msgs.push_back({s[0], s[1]});
+        tr.observe(s[0]);
+        tr.observe(s[1]);
+        F bt = tr.sample();
+        uint64_t bp[2];
+        u2(bt, bp);
+        FK(flock_launch_glue_eq(bcur, len, S->eqlo.p, S->eqhi.p, lob, bp, st));
+      }
+    };
+    auto induce = [&](int nvars, const std::vector<Open>::value_type& op, const std::vector<uint32_t>& q,
+                      const std::vector<F>& alpha_v) {
+      (void)op;
+      const Sks& sk = sks_for(nvars);
+      auto aw = eq_table(alpha_v);
+      aw.resize(q.size());
+      void* dsk = S->small.get((size_t)(2 * (nvars + 1)) * 16);
+      h2d(dsk, sk.s.data(), (nvars + 1) * 16, st);
+      h2d((char*)dsk + (nvars + 1) * 16, sk.inv.data(), (nvars + 1) * 16, st);
+      uint32_t* dq = (uint32_t*)S->qbuf.get(q.size() * 4);
+      h2d(dq, q.data(), q.size() * 4, st);
+      void* dal = S->abuf.get(q.size() * 16);
+      h2d(dal, aw.data(), q.size() * 16, st);
+      int lo_bits = (nvars + 1) / 2, hi_bits = nvars - lo_bits;
+      void* dW = S->W.get(q.size() * nvars * 16);
+      void* dLO = S->LO.get((q.size() << lo_bits) * 16);
+      void* dHI = S->HI.get((q.size() << hi_bits) * 16);
+      void* dbs = S->basis.get(((size_t)16) << nvars);
+      FK(flock_launch_induce_basis(dq, (int)q.size(), nvars, dsk, (const char*)dsk + (nvars + 1) * 16, dal, dW, dLO,
+                                   dHI, dbs, st));
+      return dbs;
+    };
+
+    run_msg(0, F());
+    for (int j = 0; j < cfg.initial_k; j++) {
+      int bits = cfg.fold_bits[0] - j;
+      if (bits > 0) fold_nonces.push_back(grind((uint32_t)bits));
+      F rr = tr.sample();
+      run_msg(1, rr);
+    }
+    int n1 = log_n - cfg.initial_k;
+    int lni = cfg.ks[0];
+    int cur_rate = cfg.rates[1];
+    int slot = 0;
+    uint8_t root_prev[32];
+    std::vector<std::vector<uint8_t>> roots;
+    void* pcw = S->lvl_cw[slot].get(((size_t)16 << (n1 + cur_rate)));
+    void* ptree = S->lvl_tree[slot].get((2 * ((size_t)1 << (n1 - lni + cur_rate)) - 1) * 32);
+    ligero_commit(*S, fcur, n1 - lni, lni, cur_rate, pcw, ptree, root_prev);
+    roots.emplace_back(root_prev, root_prev + 32);
+    tr.observe_bytes(root_prev, 32);
+    size_t prev_block = (size_t)1 << (n1 - lni + cur_rate);
+    int prev_width = 1 << lni;
+    ood(cfg.ood[1]);
+    grind_nonces.push_back(grind((uint32_t)cfg.grind_bits[0]));
+    auto q0 = sample_queries(tr, block0, cfg.queries[0]);
+    auto a0 = tr.sample_vec(ilog2(cfg.queries[0]));
+    Open open0 = open_rows(*S, dcw, dtree, block0, 1 << lbs, q0);
+    {
+      void* dbs = induce(n1, open0, q0, a0);
+      introduce(dbs);
+    }
+    std::vector<Open> rec_opens;
+    std::vector<F> yr;
+    Open final_open;
+    for (int i = 0; i < cfg.steps; i++) {
+      int ki = cfg.ks[i];
+      for (int j = 0; j < ki; j++) {
+        int bits = cfg.fold_bits[i + 1] - j;
+        if (bits > 0) fold_nonces.push_back(grind((uint32_t)bits));
+        F rr = tr.sample();
+        run_msg(1, rr);
+      }
+      if (i == cfg.steps - 1) {
+        yr.resize(len);
+        d2h(yr.data(), fcur, len * 16, st);
+        for (auto& v : yr) tr.observe(v);
+        grind_nonces.push_back(grind((uint32_t)cfg.grind_bits[i + 1]));
+        auto ql = sample_queries(tr, prev_block, cfg.queries[i + 1]);
+        final_open = open_rows(*S, S->lvl_cw[slot].p, S->lvl_tree[slot].p, prev_block, prev_width, ql);
+        break;
+      }
+      int n_next = ilog2(len);
+      int lni2 = cfg.ks[i + 1];
+      int rate2 = cfg.rates[i + 2];
+      int ns = slot ^ 1;
+      void* ncw = S->lvl_cw[ns].get(((size_t)16 << (n_next + rate2)));
+      void* ntree = S->lvl_tree[ns].get((2 * ((size_t)1 << (n_next - lni2 + rate2)) - 1) * 32);
+      uint8_t rootn[32];
+      ligero_commit(*S, fcur, n_next - lni2, lni2, rate2, ncw, ntree, rootn);
+      roots.emplace_back(rootn, rootn + 32);
+      tr.observe_bytes(rootn, 32);
+      ood(cfg.ood[i + 2]);
+      grind_nonces.push_back(grind((uint32_t)cfg.grind_bits[i + 1]));
+      auto qi = sample_queries(tr, prev_block, cfg.queries[i + 1]);
+      auto ai = tr.sample_vec(ilog2(cfg.queries[i + 1]));
+      Open oi = open_rows(*S, S->lvl_cw[slot].p, S->lvl_tree[slot].p, prev_block, prev_width, qi);
+      void* dbs = induce(n_next, oi, qi, ai);
+      rec_opens.push_back(std::move(oi));
+      introduce(dbs);
+      slot = ns;
+      prev_block = (size_t)1 << (n_next - lni2 + rate2);
+      prev_width = 1 << lni2;
+    }
+    T.ligerito_ms = clk.lap();
+
+    // ---- bundle tail: BatchOpeningProofLigerito.ligerito ----
+    w.raw(root0, 32);  // initial_root
+    write_open(w, open0);
+    w.u64(roots.size());
+    for (auto& rt : roots) w.raw(rt.data(), 32);
+    w.u64(rec_opens.size());
+    for (auto& o : rec_opens) write_open(w, o);
+    w.fv(yr);
+    write_open(w, final_open);
+    w.pv(msgs);
+    w.u64(grind_nonces.size());
+    for (auto x : grind_nonces) w.u64(x);
+    w.fv(ood_vals);
+    w.u64(fold_nonces.size());
+    for (auto x : fold_nonces) w.u64(x);
+    out.swap(w.v);
+    T.serialize_ms = clk.lap();
+    return FLOCK_OK;
+  } catch (const Fail& f) {
+    return f.code;
+  } catch (const std::bad_alloc&) {
+    return FLOCK_ERR_OOM;
+  }
+}

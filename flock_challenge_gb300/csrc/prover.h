@@ -1,0 +1,20 @@
+// Full-proof orchestration (prover.cu).
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include "../../include/flock_gpu.h"
+
+struct ProverState;
+
+// Host wall time of each phase of the last proof, in milliseconds.
+struct FlockPhaseTimes {
+  double setup_ms = 0, commit_ms = 0, zc_round1_ms = 0, zc_rounds_ms = 0, lincheck_ms = 0, ring_switch_ms = 0,
+         ligerito_ms = 0, serialize_ms = 0;
+};
+
+ProverState* flock_prover_create(int device);
+void flock_prover_destroy(ProverState* s);
+// Proves n host compressions in 2^n_log slots; `out` receives the wire bytes.
+int flock_prover_prove(ProverState* s, const flock_compression* h_in, size_t n, int n_log, std::vector<uint8_t>& out);
+const FlockPhaseTimes& flock_prover_times(const ProverState* s);

@@ -87,6 +87,30 @@ int flock_merkle_tree(const void* d_data, size_t n_leaves, size_t leaf_bytes, vo
 int flock_commit(flock_ctx* ctx, const void* d_z, int m, int log_inv_rate, int log_batch_size,
                  void* d_codeword, void* d_tree, uint8_t root[32], void* stream);
 
+/* ---- Full proof --------------------------------------------------------- */
+
+/* Builds (and caches) the setup for proofs of n_blocks compressions: the
+ * statement digest of the block R1CS (crates/flock-core/src/r1cs.rs:343-365)
+ * and the device copies of the base matrices. Replaces Blake3Setup::new
+ * (crates/flock-prover/src/r1cs_hashes/blake3.rs:3295-3347). Optional: the
+ * first flock_prove does the same work. */
+int flock_setup(flock_ctx* ctx, size_t n_blocks);
+
+/* Proves n host compressions (padded to 2^max(3, ceil(log2 n)) slots with the
+ * all-zero compression) and writes the serialized proof bundle
+ * ("FLOCK" 0x04 0x02 + bincode, crates/flock-prover/src/proof_io.rs:161-208)
+ * to out. *len receives the size; FLOCK_ERR_CAPACITY when cap is too small.
+ * Replaces Blake3Setup::prove_fast + R1csProofBundleLigerito::to_bytes
+ * (blake3.rs:3405-3480, proof_io.rs:161). Transcript domain "flock-bench-v0",
+ * BLAKE3 Merkle/Fiat-Shamir, Fast profile, rate 1/2, 64 lanes. */
+int flock_prove(flock_ctx* ctx, const flock_compression* in, size_t n, uint8_t* out, size_t cap, size_t* len);
+
+/* Host wall time (ms) of the phases of the last proof: setup, commit,
+ * zerocheck round 1, zerocheck rounds, lincheck, ring switch, Ligerito,
+ * serialization (first n entries). No reference counterpart (the reference's
+ * FLOCK_PHASE_TIMING prints, crates/flock-prover/src/prover.rs:958-1216). */
+int flock_last_phase_times(const flock_ctx* ctx, double* ms, int n);
+
 #ifdef __cplusplus
 }
 #endif
