@@ -144,6 +144,13 @@ def _proto_lib():
         L.flock_setup.argtypes = [P, ctypes.c_size_t]
         L.flock_prove.argtypes = [P, P, ctypes.c_size_t, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
         L.flock_last_phase_times.argtypes = [P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+        L.flock_prove_seed.argtypes = [P, ctypes.c_uint32, ctypes.c_uint64, P, ctypes.c_size_t,
+                                       ctypes.POINTER(ctypes.c_size_t)]
+        L.flock_prove_device.argtypes = [P, P, ctypes.c_size_t, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+        L.flock_generate_inputs.argtypes = [ctypes.c_uint32, ctypes.c_uint64, P, P]
+        L.flock_kernel_launches.restype = ctypes.c_uint64
+        L.flock_stream.argtypes = [P]
+        L.flock_stream.restype = P
         L._proto_ready = True
     return L
 
@@ -187,7 +194,45 @@ class Blake3Setup:
         check(rc, "flock_prove")
         return self._buf[:ln.value].tobytes()
 
+    def _call(self, fn, *args):
+        ln = ctypes.c_size_t()
+        rc = fn(self.ctx.handle, *args, self._buf.ctypes.data_as(ctypes.c_void_p), self._buf.size, ctypes.byref(ln))
+        if rc == -5:
+            self._buf = np.zeros(ln.value, np.uint8)
+            rc = fn(self.ctx.handle, *args, self._buf.ctypes.data_as(ctypes.c_void_p), self._buf.size,
+                    ctypes.byref(ln))
+        check(rc, fn.__name__)
+        return self._buf[:ln.value].tobytes()
+
+    def prove_seed(self, seed):
+        """Seed -> proof bytes: inputs generated on the device from `seed` with the
+        reference generator (benchmark-tools/common/src/lib.rs:20-33), then proven."""
+        if self.n_blocks != 1 << self.n_blocks_log:
+            raise ValueError("prove_seed needs a power-of-two n_blocks")
+        return self._call(_proto_lib().flock_prove_seed, self.n_blocks_log, seed)
+
+    def prove_device(self, d_blocks):
+        """Proof of n_blocks records already in device memory (uint8 CUDA tensor)."""
+        return self._call(_proto_lib().flock_prove_device, ctypes.c_void_p(d_blocks.data_ptr()), self.n_blocks)
+
+    def stream_handle(self):
+        """cudaStream_t the prover launches on (for event timing)."""
+        return _proto_lib().flock_stream(self.ctx.handle)
+
     def phase_times(self):
         arr = (ctypes.c_double * 8)()
         check(_proto_lib().flock_last_phase_times(self.ctx.handle, arr, 8), "flock_last_phase_times")
         return dict(zip(PHASES, list(arr)))
+
+
+def kernel_launches():
+    """Number of kernels this library has launched in the process."""
+    return int(_proto_lib().flock_kernel_launches())
+
+
+def generate_inputs(log2_size, seed, device="cuda"):
+    """The reference's 2^log2_size benchmark compressions for `seed`, generated on the device."""
+    import torch
+    out = torch.empty((1 << log2_size) * 112, dtype=torch.uint8, device=device)
+    check(_proto_lib().flock_generate_inputs(log2_size, seed, _dptr(out), None), "flock_generate_inputs")
+    return out

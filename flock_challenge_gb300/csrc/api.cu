@@ -7,6 +7,11 @@
 #include "prover.h"
 #include "r1cs_setup.h"
 
+#include <atomic>
+
+static std::atomic<unsigned long long> g_launches{0};
+void flock_count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
 struct flock_ctx {
   int device = 0;
   size_t hbm_budget = 0;
@@ -21,6 +26,8 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 extern "C" {
 
 const char* flock_version(void) { return "flock-gb300 0.1 (sm_103a)"; }
+
+uint64_t flock_kernel_launches(void) { return g_launches.load(); }
 
 int flock_create(int device, size_t hbm_budget, flock_ctx** out) {
   if (!out) return FLOCK_ERR_ARG;
@@ -92,7 +99,8 @@ int flock_setup(flock_ctx* ctx, size_t n_blocks) {
   return ctx->prover ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
-int flock_prove(flock_ctx* ctx, const flock_compression* in, size_t n, uint8_t* out, size_t cap, size_t* len) {
+static int prove_impl(flock_ctx* ctx, const flock_compression* in, size_t n, uint8_t* out, size_t cap, size_t* len,
+                      bool on_device) {
   if (!ctx || !len || (n && !in)) return FLOCK_ERR_ARG;
   size_t nn = n < 8 ? 8 : n;
   int n_log = 0;
@@ -101,12 +109,47 @@ int flock_prove(flock_ctx* ctx, const flock_compression* in, size_t n, uint8_t* 
     ctx->prover = flock_prover_create(ctx->device);
     if (!ctx->prover) return FLOCK_ERR_CUDA;
   }
-  int rc = flock_prover_prove(ctx->prover, in, n, n_log, ctx->last_proof);
+  int rc = flock_prover_prove(ctx->prover, in, n, n_log, ctx->last_proof, on_device);
   if (rc != FLOCK_OK) return rc;
   *len = ctx->last_proof.size();
   if (!out || cap < ctx->last_proof.size()) return FLOCK_ERR_CAPACITY;
   memcpy(out, ctx->last_proof.data(), ctx->last_proof.size());
   return FLOCK_OK;
+}
+
+int flock_prove(flock_ctx* ctx, const flock_compression* in, size_t n, uint8_t* out, size_t cap, size_t* len) {
+  return prove_impl(ctx, in, n, out, cap, len, false);
+}
+
+int flock_prove_device(flock_ctx* ctx, const flock_compression* d_in, size_t n, uint8_t* out, size_t cap,
+                       size_t* len) {
+  return prove_impl(ctx, d_in, n, out, cap, len, true);
+}
+
+int flock_generate_inputs(uint32_t log2_size, uint64_t seed, void* d_out, void* stream) {
+  if (!d_out || log2_size > 30) return FLOCK_ERR_ARG;
+  uint64_t l = log2_size;
+  return flock_launch_gen_inputs(seed ^ ((l << 29) | (l >> 35)), (size_t)1 << log2_size, d_out, as_stream(stream));
+}
+
+int flock_prove_seed(flock_ctx* ctx, uint32_t log2_size, uint64_t seed, uint8_t* out, size_t cap, size_t* len) {
+  if (!ctx || !len || log2_size < 8 || log2_size > 21) return FLOCK_ERR_ARG;
+  if (!ctx->prover) {
+    ctx->prover = flock_prover_create(ctx->device);
+    if (!ctx->prover) return FLOCK_ERR_CUDA;
+  }
+  int rc = flock_prover_prove_seed(ctx->prover, (int)log2_size, seed, ctx->last_proof);
+  if (rc != FLOCK_OK) return rc;
+  *len = ctx->last_proof.size();
+  if (!out || cap < ctx->last_proof.size()) return FLOCK_ERR_CAPACITY;
+  memcpy(out, ctx->last_proof.data(), ctx->last_proof.size());
+  return FLOCK_OK;
+}
+
+void* flock_stream(flock_ctx* ctx) {
+  if (!ctx) return nullptr;
+  if (!ctx->prover) ctx->prover = flock_prover_create(ctx->device);
+  return ctx->prover ? (void*)flock_prover_stream(ctx->prover) : nullptr;
 }
 
 int flock_last_phase_times(const flock_ctx* ctx, double* ms, int n) {

@@ -66,3 +66,9 @@ int flock_launch_gather_rows(const void* mat, const uint32_t* rows, int n_rows, 
                              cudaStream_t st);
 int flock_launch_gather_nodes(const void* tree, const uint32_t* idx, int n, void* out, cudaStream_t st);
 int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, cudaStream_t st, uint64_t* nonce);
+
+// Launch counter of this library's kernels (read through flock_kernel_launches).
+void flock_count_launch();
+
+// Benchmark inputs (inputs.cu): n records from SplitMix64 state `state0`.
+int flock_launch_gen_inputs(uint64_t state0, size_t n, void* d_out, cudaStream_t st);

@@ -58,9 +58,14 @@ int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, cudaSt
   const unsigned long long none = ~0ull;
   if (cudaMemcpyAsync(d_dig, digest, 32, cudaMemcpyHostToDevice, st) != cudaSuccess) return FLOCK_ERR_CUDA;
   if (cudaMemcpyAsync(d_best, &none, 8, cudaMemcpyHostToDevice, st) != cudaSuccess) return FLOCK_ERR_CUDA;
-  uint64_t window = (uint64_t)1 << (bits + 2 < 22 ? 22 : (bits + 2 > 30 ? 30 : bits + 2));
+  // About two expected hits per window: a miss costs one more window, an
+  // oversized window wastes work on every grind (most grinds are 2..14 bits).
+  int wlog = (int)bits + 1;
+  if (wlog < 12) wlog = 12;
+  if (wlog > 26) wlog = 26;
+  uint64_t window = (uint64_t)1 << wlog;
   for (uint64_t start = 0;; start += window) {
-    grind_kernel<<<(unsigned)((window + 255) / 256), 256, 0, st>>>(d_dig, start, window, bits, d_best);
+    grind_kernel<<<(unsigned)((window + 255) / 256), 256, 0, st>>>(d_dig, start, window, bits, d_best); flock_count_launch();
     if (cudaGetLastError() != cudaSuccess) return FLOCK_ERR_CUDA;
     unsigned long long best = 0;
     if (cudaMemcpyAsync(&best, d_best, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess) return FLOCK_ERR_CUDA;

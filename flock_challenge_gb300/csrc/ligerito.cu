@@ -172,41 +172,41 @@ int flock_lig_grid(size_t n_pairs) { return (int)grid_for(n_pairs, LG_THREADS, 1
 int flock_launch_lig_fold_msg(const void* f, const void* b, size_t n_out, int fold, const uint64_t r[2], void* fo,
                               void* bo, void* partials, int grid, cudaStream_t st) {
   lig_fold_msg_kernel<<<grid, LG_THREADS, 0, st>>>((const gf128*)f, (const gf128*)b, n_out, fold, to_gf(r),
-                                                   (gf128*)fo, (gf128*)bo, (gf128*)partials);
+                                                   (gf128*)fo, (gf128*)bo, (gf128*)partials); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
 int flock_launch_lig_intro_eq(const void* f, size_t n, const void* lo, const void* hi, int lo_bits, void* partials,
                               int grid, cudaStream_t st) {
   lig_intro_eq_kernel<<<grid, LG_THREADS, 0, st>>>((const gf128*)f, n, (const gf128*)lo, (const gf128*)hi, lo_bits,
-                                                   (gf128*)partials);
+                                                   (gf128*)partials); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
 int flock_launch_glue_eq(void* b, size_t n, const void* lo, const void* hi, int lo_bits, const uint64_t beta[2],
                          cudaStream_t st) {
   glue_eq_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, st>>>((gf128*)b, n, (const gf128*)lo, (const gf128*)hi,
-                                                             lo_bits, to_gf(beta));
+                                                             lo_bits, to_gf(beta)); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
 int flock_launch_glue(void* b, const void* add, size_t n, const uint64_t beta[2], cudaStream_t st) {
-  glue_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, st>>>((gf128*)b, (const gf128*)add, n, to_gf(beta));
+  glue_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, st>>>((gf128*)b, (const gf128*)add, n, to_gf(beta)); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
 int flock_launch_induce_basis(const uint32_t* d_queries, int nq, int n, const void* sks, const void* inv_sks,
                               const void* alpha_w, void* W, void* LO, void* HI, void* basis, cudaStream_t st) {
   what_kernel<<<(nq + 127) / 128, 128, 0, st>>>(d_queries, nq, n, (const gf128*)sks, (const gf128*)inv_sks,
-                                                (gf128*)W);
+                                                (gf128*)W); flock_count_launch();
   int lo_bits = (n + 1) / 2, hi_bits = n - lo_bits;
   size_t nlo = (size_t)nq << lo_bits, nhi = (size_t)nq << hi_bits;
   tensor_kernel<<<grid_for(nlo, 256, 1u << 30), 256, 0, st>>>((const gf128*)W, nq, n, 0, lo_bits,
-                                                               (const gf128*)alpha_w, (gf128*)LO);
+                                                               (const gf128*)alpha_w, (gf128*)LO); flock_count_launch();
   tensor_kernel<<<grid_for(nhi, 256, 1u << 30), 256, 0, st>>>((const gf128*)W, nq, n, lo_bits, hi_bits, nullptr,
-                                                               (gf128*)HI);
+                                                               (gf128*)HI); flock_count_launch();
   basis_kernel<<<grid_for((size_t)1 << n, 256, 152 * 8), 256, 0, st>>>((const gf128*)LO, (const gf128*)HI, nq,
-                                                                       lo_bits, hi_bits, (gf128*)basis);
+                                                                       lo_bits, hi_bits, (gf128*)basis); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
@@ -214,12 +214,12 @@ int flock_launch_gather_rows(const void* mat, const uint32_t* rows, int n_rows, 
                              cudaStream_t st) {
   size_t n = (size_t)n_rows * width;
   gather_rows_kernel<<<grid_for(n, 256, 1u << 30), 256, 0, st>>>((const gf128*)mat, rows, n_rows, width,
-                                                                  (gf128*)out);
+                                                                  (gf128*)out); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
 int flock_launch_gather_nodes(const void* tree, const uint32_t* idx, int n, void* out, cudaStream_t st) {
   if (n == 0) return FLOCK_OK;
-  gather_nodes_kernel<<<(2 * n + 255) / 256, 256, 0, st>>>((const uint4*)tree, idx, n, (uint4*)out);
+  gather_nodes_kernel<<<(2 * n + 255) / 256, 256, 0, st>>>((const uint4*)tree, idx, n, (uint4*)out); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }

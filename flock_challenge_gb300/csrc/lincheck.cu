@@ -137,7 +137,7 @@ inline gf128 to_gf(const uint64_t v[2]) {
 int flock_launch_lc_partial_fold(const void* stripe, size_t n_stripes, const void* eq_lo, const void* eq_hi,
                                  int lo_bits, void* partials, int grid, cudaStream_t st) {
   lc_partial_fold_kernel<<<grid, PF_THREADS, 0, st>>>((const uint8_t*)stripe, n_stripes, (const gf128*)eq_lo,
-                                                      (const gf128*)eq_hi, lo_bits, (gf128*)partials);
+                                                      (const gf128*)eq_hi, lo_bits, (gf128*)partials); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
@@ -145,19 +145,19 @@ int flock_launch_lc_comb(const uint32_t* a_ptr, const uint32_t* a_idx, const uin
                          const void* eq, const uint64_t alpha[2], const uint64_t beta[2], int pin, void* comb,
                          cudaStream_t st) {
   lc_comb_kernel<<<FLOCK_K / 128, 128, 0, st>>>(a_ptr, a_idx, b_ptr, b_idx, (const gf128*)eq, to_gf(alpha),
-                                                to_gf(beta), pin, (gf128*)comb);
+                                                to_gf(beta), pin, (gf128*)comb); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
 int flock_launch_lc_quirky_eq(const void* lag, const void* x_rest, int n_rest, void* out, cudaStream_t st) {
   int n = 64 << n_rest;
   lc_quirky_eq_kernel<<<(n + 255) / 256, 256, 0, st>>>((const gf128*)lag, (const gf128*)x_rest, n_rest,
-                                                       (gf128*)out);
+                                                       (gf128*)out); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
 int flock_launch_lc_round(void* c, void* z, size_t n, int bind, const uint64_t r[2], int emit, void* out,
                           cudaStream_t st) {
-  lc_round_kernel<<<1, LR_THREADS, 0, st>>>((gf128*)c, (gf128*)z, n, bind, to_gf(r), emit, (gf128*)out);
+  lc_round_kernel<<<1, LR_THREADS, 0, st>>>((gf128*)c, (gf128*)z, n, bind, to_gf(r), emit, (gf128*)out); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }

@@ -178,7 +178,7 @@ int flock_launch_merkle(const void* d_data, size_t n_leaves, size_t leaf_bytes, 
     return FLOCK_ERR_SHAPE;
   size_t blocks = (n_leaves + LEAF_THREADS - 1) / LEAF_THREADS;
   leaf_kernel<<<(unsigned)blocks, LEAF_THREADS, 0, st>>>((const uint8_t*)d_data, n_leaves, (uint32_t)leaf_bytes,
-                                                         (uint32_t*)d_tree);
+                                                         (uint32_t*)d_tree); flock_count_launch();
   if (cudaGetLastError() != cudaSuccess) return FLOCK_ERR_CUDA;
   size_t off = 0, len = n_leaves;
   while (len > 1) {
@@ -187,7 +187,7 @@ int flock_launch_merkle(const void* d_data, size_t n_leaves, size_t leaf_bytes, 
     size_t span = len < per ? len : per;
     while (((size_t)1 << (lv + 1)) <= span) lv++;  // log2(span)
     size_t grid = (len + per - 1) / per;
-    parent_kernel<<<(unsigned)grid, PARENT_THREADS, 0, st>>>((uint32_t*)d_tree, off, len, lv);
+    parent_kernel<<<(unsigned)grid, PARENT_THREADS, 0, st>>>((uint32_t*)d_tree, off, len, lv); flock_count_launch();
     if (cudaGetLastError() != cudaSuccess) return FLOCK_ERR_CUDA;
     for (int i = 0; i < lv; i++) {
       off += len;

@@ -108,10 +108,10 @@ int launch_pass(gf128* dst, const gf128* src, size_t mask, const gf128* tw, int 
   size_t tiles = (size_t)1 << (log_d - F);
   if (log_lanes >= 4) {
     size_t blocks = tiles * ((1 << log_lanes) / 16);
-    ntt_pass_kernel<F, 16><<<(unsigned)blocks, NTT_THREADS, 0, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
+    ntt_pass_kernel<F, 16><<<(unsigned)blocks, NTT_THREADS, 0, st>>>(dst, src, mask, tw, log_d, log_lanes, l0); flock_count_launch();
   } else {
     size_t blocks = tiles * ((1 << log_lanes) / 8);
-    ntt_pass_kernel<F, 8><<<(unsigned)blocks, NTT_THREADS, 0, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
+    ntt_pass_kernel<F, 8><<<(unsigned)blocks, NTT_THREADS, 0, st>>>(dst, src, mask, tw, log_d, log_lanes, l0); flock_count_launch();
   }
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }

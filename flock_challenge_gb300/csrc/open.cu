@@ -96,7 +96,7 @@ combined_basis_kernel(size_t n, const gf128* __restrict__ t0_lo, const gf128* __
 int flock_launch_s_hat_v(const void* z, size_t n, const void* t_lo, const void* t_hi, int lo_bits, void* partials,
                          int grid, cudaStream_t st) {
   s_hat_v_kernel<<<grid, SH_THREADS, 0, st>>>((const gf128*)z, n, (const gf128*)t_lo, (const gf128*)t_hi, lo_bits,
-                                              (gf128*)partials);
+                                              (gf128*)partials); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 int flock_s_hat_v_warps(int grid) { return grid * (SH_THREADS / 32); }
@@ -113,6 +113,6 @@ int flock_launch_combined_basis(size_t n, const void* t0_lo, const void* t0_hi, 
   if (grid > 152 * 2) grid = 152 * 2;
   combined_basis_kernel<<<(unsigned)grid, CB_THREADS, smem, st>>>(
       n, (const gf128*)t0_lo, (const gf128*)t0_hi, (const gf128*)t1_lo, (const gf128*)t1_hi, lo_bits,
-      (const gf128*)tables, (gf128*)b);
+      (const gf128*)tables, (gf128*)b); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }

@@ -377,8 +377,25 @@ void flock_prover_destroy(ProverState* S) {
 }
 
 const FlockPhaseTimes& flock_prover_times(const ProverState* S) { return S->times; }
+cudaStream_t flock_prover_stream(const ProverState* S) { return S->st; }
 
-int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, int n_log, std::vector<uint8_t>& out) {
+int flock_prover_prove_seed(ProverState* S, int log2, uint64_t seed, std::vector<uint8_t>& out) {
+  try {
+    CK(cudaSetDevice(S->device));
+    size_t n = (size_t)1 << log2;
+    uint64_t l = (uint64_t)log2;
+    uint64_t state0 = seed ^ ((l << 29) | (l >> 35));
+    void* d_in = S->in.get(n * sizeof(flock_compression));
+    FK(flock_launch_gen_inputs(state0, n, d_in, S->st));
+    int n_log = log2 < 3 ? 3 : log2;
+    return flock_prover_prove(S, (const flock_compression*)d_in, n, n_log, out, true);
+  } catch (const Fail& f) {
+    return f.code;
+  }
+}
+
+int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, int n_log, std::vector<uint8_t>& out,
+                       bool input_on_device) {
   try {
     CK(cudaSetDevice(S->device));
     const int m = 14 + n_log;
@@ -413,8 +430,12 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
 
     // ---- witness + commit ----
     const size_t nbits = (size_t)1 << m, nbytes = nbits / 8, n128 = nbits / 128;
-    void* d_in = S->in.get(std::max<size_t>(n, 1) * sizeof(flock_compression));
-    if (n) h2d(d_in, h_in, n * sizeof(flock_compression), st);
+    const void* d_in = h_in;
+    if (!input_on_device) {
+      void* buf = S->in.get(std::max<size_t>(n, 1) * sizeof(flock_compression));
+      if (n) h2d(buf, h_in, n * sizeof(flock_compression), st);
+      d_in = buf;
+    }
     void *dz = S->z.get(nbytes), *da = S->a.get(nbytes), *db = S->b.get(nbytes), *ds = S->stripe.get(nbytes);
     FK(flock_launch_witness((const flock_compression*)d_in, n, n_log, dz, da, db, ds, st));
     const int lbs = 6, rate0 = 1;

@@ -3,6 +3,8 @@
 #include <cstdint>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "../../include/flock_gpu.h"
 
 struct ProverState;
@@ -16,5 +18,9 @@ struct FlockPhaseTimes {
 ProverState* flock_prover_create(int device);
 void flock_prover_destroy(ProverState* s);
 // Proves n host compressions in 2^n_log slots; `out` receives the wire bytes.
-int flock_prover_prove(ProverState* s, const flock_compression* h_in, size_t n, int n_log, std::vector<uint8_t>& out);
+int flock_prover_prove(ProverState* s, const flock_compression* in, size_t n, int n_log, std::vector<uint8_t>& out,
+                       bool input_on_device = false);
+cudaStream_t flock_prover_stream(const ProverState* s);
+// Generates the 2^log2 benchmark inputs of `seed` on the device, then proves them.
+int flock_prover_prove_seed(ProverState* s, int log2, uint64_t seed, std::vector<uint8_t>& out);
 const FlockPhaseTimes& flock_prover_times(const ProverState* s);

@@ -241,6 +241,6 @@ int flock_launch_witness(const flock_compression* d_in, size_t n_in, int n_block
     attr = true;
   }
   witness_kernel<<<(unsigned)blocks, threads, smem, stream>>>(d_in, n_in, n_total, (uint64_t*)d_z,
-                                                              (uint64_t*)d_a, (uint64_t*)d_b, (uint8_t*)d_stripe);
+                                                              (uint64_t*)d_a, (uint64_t*)d_b, (uint8_t*)d_stripe); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }

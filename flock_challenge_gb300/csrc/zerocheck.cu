@@ -339,13 +339,13 @@ int flock_launch_zc_round1(const void* a, const void* b, const void* c, size_t n
     attr = true;
   }
   zc_round1_kernel<<<grid, R1_THREADS, smem, st>>>((const uint64_t*)a, (const uint64_t*)b, (const uint64_t*)c,
-                                                   n_outer, (const gf128*)eq_out, d_tables, (gf128*)partials);
+                                                   n_outer, (const gf128*)eq_out, d_tables, (gf128*)partials); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 int flock_zc_round1_warps(int grid) { return grid * (R1_THREADS / 32); }
 
 int flock_launch_reduce_rows(const void* in, size_t count, int width, void* out, cudaStream_t st) {
-  reduce_rows_kernel<<<(width + 127) / 128, 128, 0, st>>>((const gf128*)in, count, width, (gf128*)out);
+  reduce_rows_kernel<<<(width + 127) / 128, 128, 0, st>>>((const gf128*)in, count, width, (gf128*)out); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
@@ -354,7 +354,7 @@ int flock_launch_fold_skip(const void* a, const void* b, size_t rows, const void
   size_t grid = (rows + 255) / 256;
   if (grid > 152 * 16) grid = 152 * 16;
   fold_skip_kernel<<<(unsigned)grid, 256, 0, st>>>((const uint64_t*)a, (const uint64_t*)b, rows, (const gf128*)lag,
-                                                   (gf128*)out_a, (gf128*)out_b);
+                                                   (gf128*)out_a, (gf128*)out_b); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
@@ -362,7 +362,7 @@ int flock_launch_eq_split(const void* r, int lo_bits, int hi_bits, void* lo, voi
   size_t n = ((size_t)1 << lo_bits) + ((size_t)1 << hi_bits);
   size_t grid = (n + 255) / 256;
   if (grid > 4096) grid = 4096;
-  eq_split_kernel<<<(unsigned)grid, 256, 0, st>>>((const gf128*)r, lo_bits, hi_bits, (gf128*)lo, (gf128*)hi);
+  eq_split_kernel<<<(unsigned)grid, 256, 0, st>>>((const gf128*)r, lo_bits, hi_bits, (gf128*)lo, (gf128*)hi); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
@@ -373,7 +373,7 @@ int flock_launch_zc_round(const void* A, const void* B, size_t n_pairs, int bind
   r.w[0] = (uint32_t)rho[0]; r.w[1] = (uint32_t)(rho[0] >> 32); r.w[2] = (uint32_t)rho[1]; r.w[3] = (uint32_t)(rho[1] >> 32);
   zc_round_kernel<<<grid, RND_THREADS, 0, st>>>((const gf128*)A, (const gf128*)B, n_pairs, bind, r, (gf128*)Aout,
                                                 (gf128*)Bout, (const gf128*)eq_lo, (const gf128*)eq_hi, lo_bits,
-                                                (gf128*)partials);
+                                                (gf128*)partials); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
@@ -384,6 +384,6 @@ int flock_launch_bind_pairs(const void* A, const void* B, size_t n, const uint64
   size_t grid = (n + 255) / 256;
   if (grid > 152 * 8) grid = 152 * 8;
   bind_pairs_kernel<<<(unsigned)grid, 256, 0, st>>>((const gf128*)A, (const gf128*)B, n, r, (gf128*)Aout,
-                                                    (gf128*)Bout);
+                                                    (gf128*)Bout); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }

@@ -47,6 +47,10 @@ typedef struct flock_ctx flock_ctx;
 /* Library version string. */
 const char* flock_version(void);
 
+/* Number of CUDA kernels this library has launched in the process (all
+ * contexts). No reference counterpart; used to count launches per proof. */
+uint64_t flock_kernel_launches(void);
+
 /* Create / destroy a device context bound to `device`. `hbm_budget` bounds the
  * device memory the context may hold (0 = no limit).
  * Replaces the process-level setup of the reference worker
@@ -104,6 +108,26 @@ int flock_setup(flock_ctx* ctx, size_t n_blocks);
  * (blake3.rs:3405-3480, proof_io.rs:161). Transcript domain "flock-bench-v0",
  * BLAKE3 Merkle/Fiat-Shamir, Fast profile, rate 1/2, 64 lanes. */
 int flock_prove(flock_ctx* ctx, const flock_compression* in, size_t n, uint8_t* out, size_t cap, size_t* len);
+
+/* Benchmark inputs: the 2^log2_size compressions the reference derives from
+ * `seed` (generate_compressions, benchmark-tools/common/src/lib.rs:20-33),
+ * generated on the device into d_out (2^log2_size records). */
+int flock_generate_inputs(uint32_t log2_size, uint64_t seed, void* d_out, void* stream);
+
+/* Seed to proof bytes: generates the inputs of `seed` on the device and
+ * proves them (the reference worker's timed path, benchmark-tools/worker/src/
+ * main.rs:66-79: generate_compressions + prove_fast + to_bytes).
+ * 8 <= log2_size <= 21. */
+int flock_prove_seed(flock_ctx* ctx, uint32_t log2_size, uint64_t seed, uint8_t* out, size_t cap, size_t* len);
+
+/* As flock_prove, with the n input records already in device memory (d_in).
+ * No reference counterpart (the reference's inputs live in host memory). */
+int flock_prove_device(flock_ctx* ctx, const flock_compression* d_in, size_t n, uint8_t* out, size_t cap,
+                       size_t* len);
+
+/* The CUDA stream (cudaStream_t) the context's prover launches on, for
+ * event timing by the caller. No reference counterpart. */
+void* flock_stream(flock_ctx* ctx);
 
 /* Host wall time (ms) of the phases of the last proof: setup, commit,
  * zerocheck round 1, zerocheck rounds, lincheck, ring switch, Ligerito,

@@ -44,10 +44,13 @@ void NttF128::forward_interleaved(F128* data, size_t n_total, size_t num_ntts, i
   for (int layer = start_layer; layer < ld; layer++) {
     size_t num_blocks = (size_t)1 << layer;
     size_t half = (size_t)1 << (ld - layer - 1);
-    for (size_t blk = 0; blk < num_blocks; blk++) {
+    // one work item per (block, row) pair; all pairs of a layer are independent
+#pragma omp parallel for schedule(static) if (num_blocks * half >= 4096)
+    for (int64_t item = 0; item < (int64_t)(num_blocks * half); item++) {
+      size_t blk = (size_t)item / half, row = (size_t)item % half;
       F128 t = twiddle(layer, blk);
       size_t base = blk * 2 * half * num_ntts;
-      for (size_t row = 0; row < half; row++) {
+      {
         F128* top = data + base + row * num_ntts;
         F128* bot = top + half * num_ntts;
         for (size_t lane = 0; lane < num_ntts; lane++) {
@@ -82,11 +85,13 @@ Hash32 parent_cv(const Hash32& l, const Hash32& r) {
 std::vector<Hash32> merkle_tree(const uint8_t* data, size_t len, size_t n_leaves) {
   size_t leaf = len / n_leaves;
   std::vector<Hash32> tree(2 * n_leaves - 1);
-  for (size_t i = 0; i < n_leaves; i++) tree[i] = leaf_cv(data + i * leaf, leaf);
+#pragma omp parallel for schedule(static) if (n_leaves >= 256)
+  for (int64_t i = 0; i < (int64_t)n_leaves; i++) tree[i] = leaf_cv(data + i * leaf, leaf);
   size_t rs = 0, rl = n_leaves;
   while (rl > 1) {
     size_t nl = rl / 2;
-    for (size_t i = 0; i < nl; i++) tree[rs + rl + i] = parent_cv(tree[rs + 2 * i], tree[rs + 2 * i + 1]);
+#pragma omp parallel for schedule(static) if (nl >= 1024)
+    for (int64_t i = 0; i < (int64_t)nl; i++) tree[rs + rl + i] = parent_cv(tree[rs + 2 * i], tree[rs + 2 * i + 1]);
     rs += rl;
     rl = nl;
   }

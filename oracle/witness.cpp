@@ -106,10 +106,15 @@ struct BlockBits {
 };
 
 // One compression's witness rows; blake3.rs:965-1076 semantics.
-static void build_block(const Compression& c, BlockBits& w) {
+static const int (*schedule())[8][2] {
   static int sched[7][8][2];
   static bool init = (msg_schedule(sched), true);
   (void)init;
+  return sched;
+}
+
+static void build_block(const Compression& c, BlockBits& w) {
+  const int (*sched)[8][2] = schedule();
   memset(&w, 0, sizeof(w));
   w.put(w.z, Z_CONST_POS, 1, 1);
   w.put(w.a, Z_CONST_POS, 1, 1);
@@ -163,8 +168,10 @@ Witness build_witness(const std::vector<Compression>& blocks, int n_blocks_log, 
   out.b.resize(n_total * per);
   Compression pad;
   memset(&pad, 0, sizeof(pad));
-  BlockBits w;
-  for (size_t j = 0; j < n_total; j++) {
+#pragma omp parallel for schedule(static)
+  for (int64_t jj = 0; jj < (int64_t)n_total; jj++) {
+    size_t j = (size_t)jj;
+    BlockBits w;
     const Compression& c = j < blocks.size() ? blocks[j] : pad;
     build_block(c, w);
     for (size_t i = 0; i < per; i++) {
@@ -177,7 +184,9 @@ Witness build_witness(const std::vector<Compression>& blocks, int n_blocks_log, 
     // Byte (byte_idx*K + i_inner), bit r = bit i_inner of compression
     // 8*byte_idx + r (crates/flock-core/src/lincheck.rs:88-110).
     out.stripe.assign(n_total * K / 8, 0);
-    for (size_t j = 0; j < n_total; j++) {
+#pragma omp parallel for schedule(static)
+    for (int64_t g = 0; g < (int64_t)(n_total / 8); g++)
+    for (size_t j = (size_t)g * 8; j < (size_t)g * 8 + 8; j++) {
       const uint64_t* zb = (const uint64_t*)&out.z[j * per];
       size_t byte_idx = j >> 3;
       int r = (int)(j & 7);

@@ -45,3 +45,15 @@ def test_ranked_canary_byte_identical(cuda_device):
     p = setup.prove_fast(blocks)
     assert len(p) == gold["reference_expected_proof_bytes"]
     assert O.b3_hash(p).hex() == gold["oracle_proof_blake3"]
+
+
+def test_device_input_generator_matches_reference_generator(cuda_device):
+    # benchmark-tools/common/src/lib.rs:20-33
+    for log2, seed in [(8, 0), (12, 0x00C0FFEEBEEFD15C), (10, 2**64 - 1)]:
+        d = F.generate_inputs(log2, seed)
+        assert np.array_equal(d.cpu().numpy(), O.compressions(log2, seed).view(np.uint8))
+
+
+def test_prove_seed_equals_prove_of_generated_inputs(cuda_device):
+    setup = F.Blake3Setup(1 << 9)
+    assert setup.prove_seed(77) == setup.prove_fast(O.compressions(9, 77))
