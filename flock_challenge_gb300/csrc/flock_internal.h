@@ -26,7 +26,6 @@ int flock_launch_merkle(const void* d_data, size_t n_leaves, size_t leaf_bytes, 
 struct ZcRound1Tables;
 int flock_launch_zc_round1(const void* a, const void* b, const void* c, size_t n_outer, const void* eq_out,
                            const ZcRound1Tables* d_tables, void* partials, int grid, cudaStream_t st);
-int flock_zc_round1_warps(int grid);
 int flock_launch_reduce_rows(const void* in, size_t count, int width, void* out, cudaStream_t st);
 int flock_launch_fold_skip(const void* a, const void* b, size_t rows, const void* lag, void* out_a, void* out_b,
                            cudaStream_t st);
@@ -49,6 +48,7 @@ int flock_launch_lc_round(void* c, void* z, size_t n, int bind, const uint64_t r
 int flock_launch_s_hat_v(const void* z, size_t n, const void* t_lo, const void* t_hi, int lo_bits, void* partials,
                          int grid, cudaStream_t st);
 int flock_s_hat_v_warps(int grid);
+int flock_launch_shv_from_zvec(const void* zvec, const void* eq_tail, void* out, cudaStream_t st);
 int flock_launch_combined_basis(size_t n, const void* t0_lo, const void* t0_hi, const void* t1_lo,
                                 const void* t1_hi, int lo_bits, const void* tables, void* b, cudaStream_t st);
 

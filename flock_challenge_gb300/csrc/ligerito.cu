@@ -40,7 +40,7 @@ __device__ __forceinline__ void block_reduce_write(gf256 a, gf256 b, gf256 c, gf
 
 // If fold: in has 2 * n_out elements, bound at r into out (n_out elements);
 // message over the n_out-element state. Partials: (u0, u2, 0) per block.
-__global__ void __launch_bounds__(LG_THREADS)
+__global__ void __launch_bounds__(LG_THREADS, 2)
 lig_fold_msg_kernel(const gf128* __restrict__ f, const gf128* __restrict__ b, size_t n_out, int fold, gf128 r,
                     gf128* __restrict__ fo, gf128* __restrict__ bo, gf128* __restrict__ partials) {
   gf256 u0 = {{0, 0, 0, 0}}, u2 = u0, zz = u0;
@@ -66,7 +66,7 @@ lig_fold_msg_kernel(const gf128* __restrict__ f, const gf128* __restrict__ b, si
 }
 
 // Message of (f, eq(z)) and h = sum f * eq(z); eq(z)[j] = lo[j & mask] * hi[j >> lo_bits].
-__global__ void __launch_bounds__(LG_THREADS)
+__global__ void __launch_bounds__(LG_THREADS, 2)
 lig_intro_eq_kernel(const gf128* __restrict__ f, size_t n, const gf128* __restrict__ lo,
                     const gf128* __restrict__ hi, int lo_bits, gf128* __restrict__ partials) {
   gf256 u0 = {{0, 0, 0, 0}}, u2 = u0, h = u0;

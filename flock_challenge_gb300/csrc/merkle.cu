@@ -62,8 +62,12 @@ __device__ __forceinline__ void chunk_cv(const uint8_t* __restrict__ warp_base, 
   }
 }
 
+// Leaves, then `fuse` parent levels inside each warp (32 consecutive leaves:
+// up to 5 levels) by shuffling the right child's chaining value to the left.
+template <bool MULTI>
 __global__ void __launch_bounds__(LEAF_THREADS)
-leaf_kernel(const uint8_t* __restrict__ data, size_t n_leaves, uint32_t leaf_bytes, uint32_t* __restrict__ out) {
+leaf_kernel(const uint8_t* __restrict__ data, size_t n_leaves, uint32_t leaf_bytes, int fuse,
+            uint32_t* __restrict__ out) {
   // 32 leaves x (4 + 0.5 padding) granules of 16 B per warp.
   __shared__ uint4 stage_all[(LEAF_THREADS / 32) * (32 * 4 + 16)];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -73,7 +77,7 @@ leaf_kernel(const uint8_t* __restrict__ data, size_t n_leaves, uint32_t leaf_byt
   uint32_t* stage = reinterpret_cast<uint32_t*>(stage_all + warp * (32 * 4 + 16));
   const uint8_t* base = data + leaf0 * leaf_bytes;
   uint32_t cv[8];
-  if (leaf_bytes <= 1024) {
+  if (!MULTI) {
     chunk_cv(base, leaf_bytes, lane, nlanes, leaf_bytes, 0, stage, cv);
   } else {
     // Whole chunks; merge with the BLAKE3 chaining-value stack.
@@ -118,6 +122,31 @@ leaf_kernel(const uint8_t* __restrict__ data, size_t n_leaves, uint32_t leaf_byt
     uint4* o = reinterpret_cast<uint4*>(out + (leaf0 + lane) * 8);
     o[0] = make_uint4(cv[0], cv[1], cv[2], cv[3]);
     o[1] = make_uint4(cv[4], cv[5], cv[6], cv[7]);
+  }
+  // fused parent levels (only when the warp holds 32 whole leaves)
+  size_t lvl_off = 0, lvl_len = n_leaves, idx = leaf0 + lane;
+  for (int l = 1; l <= fuse; l++) {
+    const int step = 1 << (l - 1);
+    uint32_t rc[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) rc[i] = __shfl_down_sync(0xffffffffu, cv[i], step);
+    bool left = (lane & (2 * step - 1)) == 0;
+    if (left) {
+      uint32_t m[16];
+#pragma unroll
+      for (int i = 0; i < 8; i++) { m[i] = cv[i]; m[8 + i] = rc[i]; }
+#pragma unroll
+      for (int i = 0; i < 8; i++) cv[i] = b3::IV(i);
+      b3::compress_cv(cv, m, 64, b3::PARENT);
+    }
+    lvl_off += lvl_len;
+    lvl_len >>= 1;
+    idx >>= 1;
+    if (left) {
+      uint4* o = reinterpret_cast<uint4*>(out + (lvl_off + idx) * 8);
+      o[0] = make_uint4(cv[0], cv[1], cv[2], cv[3]);
+      o[1] = make_uint4(cv[4], cv[5], cv[6], cv[7]);
+    }
   }
 }
 
@@ -177,10 +206,22 @@ int flock_launch_merkle(const void* d_data, size_t n_leaves, size_t leaf_bytes, 
       (leaf_bytes > 1024 && (leaf_bytes % 1024 || leaf_bytes > 4096)))
     return FLOCK_ERR_SHAPE;
   size_t blocks = (n_leaves + LEAF_THREADS - 1) / LEAF_THREADS;
-  leaf_kernel<<<(unsigned)blocks, LEAF_THREADS, 0, st>>>((const uint8_t*)d_data, n_leaves, (uint32_t)leaf_bytes,
-                                                         (uint32_t*)d_tree); flock_count_launch();
+  int fuse = 0;
+  while (fuse < 5 && ((size_t)2 << fuse) <= n_leaves) fuse++;  // levels inside a warp of 32 leaves
+  if (n_leaves < 32) fuse = 0;
+  if (leaf_bytes <= 1024)
+    leaf_kernel<false><<<(unsigned)blocks, LEAF_THREADS, 0, st>>>((const uint8_t*)d_data, n_leaves,
+                                                                  (uint32_t)leaf_bytes, fuse, (uint32_t*)d_tree);
+  else
+    leaf_kernel<true><<<(unsigned)blocks, LEAF_THREADS, 0, st>>>((const uint8_t*)d_data, n_leaves,
+                                                                 (uint32_t)leaf_bytes, fuse, (uint32_t*)d_tree);
+  flock_count_launch();
   if (cudaGetLastError() != cudaSuccess) return FLOCK_ERR_CUDA;
   size_t off = 0, len = n_leaves;
+  for (int i = 0; i < fuse; i++) {
+    off += len;
+    len >>= 1;
+  }
   while (len > 1) {
     int lv = 0;
     size_t per = 2 * PARENT_THREADS;

@@ -91,7 +91,24 @@ combined_basis_kernel(size_t n, const gf128* __restrict__ t0_lo, const gf128* __
   }
 }
 
+// s_hat_v of the ab claim from lincheck's pre-sumcheck z_vec (ring_switch.rs:1275-1325):
+// packed word pos = outer * 128 + (i >> 7), bit b = i & 127, so
+// s_hat_v[b] = sum_{h < 128} eq_tail[h] * z_vec[h * 128 + b].
+__global__ void shv_from_zvec_kernel(const gf128* __restrict__ zvec, const gf128* __restrict__ eq_tail,
+                                     gf128* __restrict__ out) {
+  int b = threadIdx.x;
+  gf256 acc = {{0, 0, 0, 0}};
+  for (int h = 0; h < 128; h++) gf256_acc(acc, gf_mul_wide(eq_tail[h], zvec[h * 128 + b]));
+  out[b] = gf256_reduce(acc);
+}
+
 }  // namespace
+
+int flock_launch_shv_from_zvec(const void* zvec, const void* eq_tail, void* out, cudaStream_t st) {
+  shv_from_zvec_kernel<<<1, 128, 0, st>>>((const gf128*)zvec, (const gf128*)eq_tail, (gf128*)out);
+  flock_count_launch();
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
 
 int flock_launch_s_hat_v(const void* z, size_t n, const void* t_lo, const void* t_hi, int lo_bits, void* partials,
                          int grid, cudaStream_t st) {

@@ -274,7 +274,7 @@ struct ProverState {
   cudaStream_t st = nullptr;
   ZcRound1Tables* d_r1t = nullptr;
   DBuf in, z, a, b, stripe, cw, tree, A0, B0, A1, B1, eqlo, eqhi, eqout, rdev, part, red, lag, small, eqin, comb,
-      zvec, lcmsg, tlo0, thi0, tlo1, thi1, tables, bc, f1, b1, W, LO, HI, basis, qbuf, abuf, rows, nidx, nodes,
+      zvec, zvec0, lcmsg, tlo0, thi0, tlo1, thi1, tables, bc, f1, b1, W, LO, HI, basis, qbuf, abuf, rows, nidx, nodes,
       grind, lvl_cw[2], lvl_tree[2];
   DBuf csc_ap, csc_ai, csc_bp, csc_bi;
   bool csc_ready = false;
@@ -480,7 +480,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       }
       for (int i = 13; i < m; i++) r[i] = ro[i - 13];
     }
-    std::vector<F> p_ab(64), p_c(64);
+    std::vector<F> p_ab(64), p_c(64), shv_c;
     {
       const size_t rows = nbits / 64, n_outer = rows / 128;
       std::vector<F> rout(r.begin() + 13, r.end());
@@ -490,14 +490,16 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       void* deq = S->eqout.get(n_outer * 16);
       FK(flock_launch_eq_split(dr, nv, 0, deq, S->eqhi.get(16), st));
       const int grid = 152;
-      int nw = flock_zc_round1_warps(grid);
-      void* dpart = S->part.get((size_t)nw * 128 * 16);
+      void* dpart = S->part.get((size_t)grid * 192 * 16);
       FK(flock_launch_zc_round1(da, db, dz, n_outer, deq, S->d_r1t, dpart, grid, st));
-      auto sums = reduce_partials(*S, dpart, nw, 128);
+      auto sums = reduce_partials(*S, dpart, grid, 192);
       F dinv = zc::medium_dinv();
       const std::vector<F>& PM = phi_ext_matrix();
+      // S[64t + s] (ring-switch statistic of the c claim) and C_s = (1 + r6) S[s] + r6 S[64 + s]
+      shv_c.resize(128);
+      for (int b2 = 0; b2 < 128; b2++) shv_c[b2] = dinv * sums[64 + b2];
       std::vector<F> cs(64);
-      for (int s = 0; s < 64; s++) cs[s] = dinv * sums[64 + s];
+      for (int s = 0; s < 64; s++) cs[s] = (F::one() + r[6]) * shv_c[s] + r[6] * shv_c[64 + s];
       for (int i = 0; i < 64; i++) {
         p_ab[i] = dinv * sums[i];
         p_c[i] = dot(&PM[i * 64], cs.data(), 64);
@@ -591,6 +593,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       FK(flock_launch_lc_partial_fold(ds, n_stripes, S->eqlo.p, S->eqhi.p, lob, dpart, grid, st));
       void* dzv = S->zvec.get(FLOCK_K * 16);
       FK(flock_launch_reduce_rows(dpart, grid, FLOCK_K, dzv, st));
+      CK(cudaMemcpyAsync(S->zvec0.get(FLOCK_K * 16), dzv, FLOCK_K * 16, cudaMemcpyDeviceToDevice, st));
       void* dmsg = S->lcmsg.get(32);
       size_t len = FLOCK_K;
       for (int t = 0; t < inner_rest; t++) {
@@ -635,15 +638,22 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     F claims[2];
     const int L = m - 7;
     const int rs_lo = std::min(13, L - 1);
+    {
+      // ab claim: from the pre-sumcheck z_vec; c claim: from zerocheck round 1.
+      std::vector<F> tail(r_inner_rest.begin() + 1, r_inner_rest.end());
+      auto eq_tail = eq_table(tail);
+      void* det = S->small.get(128 * 16);
+      h2d(det, eq_tail.data(), 128 * 16, st);
+      void* dsh = S->red.get(128 * 16);
+      FK(flock_launch_shv_from_zvec(S->zvec0.p, det, dsh, st));
+      s_hat[0].resize(128);
+      d2h(s_hat[0].data(), dsh, 128 * 16, st);
+      s_hat[1] = shv_c;
+    }
     for (int k = 0; k < 2; k++) {
       tr.label("flock-ring-switch-v0");
       std::vector<F> suffix(xs[k]->begin() + 1, xs[k]->end());
       eq_split_dev(*S, suffix, rs_lo, *tlo[k], *thi[k]);
-      int grid = 512;
-      int nwp = flock_s_hat_v_warps(grid);
-      void* dpart = S->part.get((size_t)nwp * 128 * 16);
-      FK(flock_launch_s_hat_v(dz, n128, tlo[k]->p, thi[k]->p, rs_lo, dpart, grid, st));
-      s_hat[k] = reduce_partials(*S, dpart, nwp, 128);
       tr.observe_slice(s_hat[k].data(), 128);
       auto rpp = tr.sample_vec(7);
       eqr[k] = eq_table(rpp);

@@ -13,6 +13,7 @@ struct ZcRound1Tables {
   uint64_t phi8[256][2];  // phi8 embedding GF(2^8) -> GF(2^128), [lo, hi]
   uint8_t e8[8];          // GF(2^8) eq weight of the three fixed small challenges
   uint8_t e8_mat[8][8];   // multiply-by-e8[xs] as plane masks: out_j = xor_k [bit k] y_k
+  uint8_t e8c[4];         // GF(2^8) eq weight of the fixed challenges r7, r8 (c statistic)
 };
 
 namespace zc {
@@ -50,7 +51,15 @@ inline uint8_t e8(int xs) {
   return e;
 }
 
+// eq weight of r7, r8 only (variables 1, 2 of xs), for the c statistic.
+inline uint8_t e8c(int x2) {
+  uint8_t e = 1;
+  for (int v = 1; v < 3; v++) e = hf::f8_mul(e, ((x2 >> (v - 1)) & 1) ? SMALL_CHAL[v] : (uint8_t)(1 ^ SMALL_CHAL[v]));
+  return e;
+}
+
 inline void build_round1_tables(ZcRound1Tables& T) {
+  for (int x2 = 0; x2 < 4; x2++) T.e8c[x2] = e8c(x2);
   auto M = ext_matrix();
   for (int c = 0; c < 8; c++)
     for (int v = 0; v < 256; v++) {

@@ -16,15 +16,18 @@
 // which is a 143-bit shifted XOR of table values, reduced once and multiplied
 // by eq_out(xo). The F8 values y_i = a^_i b^_i are computed bit-sliced over the
 // 64 lambda points (eight 64-bit planes), so one product handles all points.
-// P^C uses linearity: C_s = sum_x eq(x) c_s(x) for the 64 skip positions s,
-// mapped to Lambda on the host.
+// P^C uses linearity: it needs only the 128 sums
+//   S[64t + s] = sum_{x : x&1 = t} eq(r[7..m], x >> 1) c_s(x)
+// (C_s = (1 + r6) S[s] + r6 S[64 + s], mapped to Lambda on the host), and S is
+// exactly the ring-switch statistic s_hat_v of the c-claim (bit 64t + s of
+// packed word x >> 1), so the opening reuses it.
 #include "flock_internal.h"
 #include "gf128.cuh"
 #include "zc_tables.h"
 
 namespace {
 
-constexpr int R1_THREADS = 512;
+constexpr int R1_THREADS = 384;
 
 // 143-bit accumulator (five 32-bit words) for shifted table values.
 struct Acc5 {
@@ -91,26 +94,30 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
   extern __shared__ uint4 sm[];
   uint64_t* ext = reinterpret_cast<uint64_t*>(sm);                  // [8][256][8]
   uint4* phi = sm + (8 * 256 * 8 * 8) / 16;                         // [256]
-  uint64_t* xch = reinterpret_cast<uint64_t*>(phi + 256);           // per warp [2][16][16]
+  uint64_t* xch = reinterpret_cast<uint64_t*>(phi + 256);           // per warp [2][16][24]
   const uint64_t* ext_src = &T->ext[0][0][0];
   for (int i = threadIdx.x; i < 8 * 256 * 8; i += R1_THREADS) ext[i] = ext_src[i];
   for (int i = threadIdx.x; i < 256; i += R1_THREADS) phi[i] = reinterpret_cast<const uint4*>(T->phi8)[i];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int xm = lane & 15, half = lane >> 4;
-  uint64_t* my_x = xch + warp * (2 * 16 * 16);
-  gf128 sum_ab[4], sum_c[4];
+  uint64_t* my_x = xch + warp * (2 * 16 * 24);
+  gf128 sum_ab[4], sum_c[8];
 #pragma unroll
-  for (int q = 0; q < 4; q++) { sum_ab[q] = gf_zero(); sum_c[q] = gf_zero(); }
+  for (int q = 0; q < 4; q++) sum_ab[q] = gf_zero();
+#pragma unroll
+  for (int q = 0; q < 8; q++) sum_c[q] = gf_zero();
 
   const size_t total_warps = (size_t)gridDim.x * (R1_THREADS / 32);
   const size_t gwarp = (size_t)blockIdx.x * (R1_THREADS / 32) + warp;
   for (size_t pair = gwarp; 2 * pair < n_outer; pair += total_warps) {
     const size_t xo = 2 * pair + half;
     const bool live = xo < n_outer;
-    uint64_t w[8], t[8];
+    uint64_t w[8], t[16];
 #pragma unroll
-    for (int j = 0; j < 8; j++) { w[j] = 0; t[j] = 0; }
+    for (int j = 0; j < 8; j++) w[j] = 0;
+#pragma unroll
+    for (int j = 0; j < 16; j++) t[j] = 0;
     if (live) {
       const size_t row0 = xo * 128 + (size_t)xm * 8;
 #pragma unroll 1
@@ -135,9 +142,11 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
         uint64_t y[8];
         f8_mul_planes(ea, eb, y);
         // w += e8[xs] * y (constant multiply as an 8x8 plane matrix);
-        // t += e8[xs] * c_s (c_s in {0,1}: plane j takes c where bit j of e8 is set).
+        // t[xs & 1] += e8c[xs >> 1] * c_s (c_s in {0,1}: plane j takes c where
+        // bit j of the constant is set).
         const uint8_t* mm = T->e8_mat[xs];
-        const uint8_t e8 = T->e8[xs];
+        const uint8_t e8c = T->e8c[xs >> 1];
+        uint64_t* tt = t + 8 * (xs & 1);
 #pragma unroll
         for (int j = 0; j < 8; j++) {
           uint64_t acc = 0;
@@ -145,69 +154,94 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
           for (int k = 0; k < 8; k++)
             if ((mm[j] >> k) & 1) acc ^= y[k];
           w[j] ^= acc;
-          if ((e8 >> j) & 1) t[j] ^= rc;
+          if ((e8c >> j) & 1) tt[j] ^= rc;
         }
       }
     }
     // Exchange the w / t planes of the 16 xm lanes of each half.
     __syncwarp();
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
-      my_x[(half * 16 + xm) * 16 + j] = w[j];
-      my_x[(half * 16 + xm) * 16 + 8 + j] = t[j];
-    }
+    for (int j = 0; j < 8; j++) my_x[(half * 16 + xm) * 24 + j] = w[j];
+#pragma unroll
+    for (int j = 0; j < 16; j++) my_x[(half * 16 + xm) * 24 + 8 + j] = t[j];
     __syncwarp();
     if (live) {
       // this lane handles points / skip positions 4*xm .. 4*xm+3 of its half
-      Acc5 va[4], vc[4];
+      // (and both parities t of the c statistic)
+      Acc5 va[4], vc[8];
 #pragma unroll
       for (int q = 0; q < 4; q++)
 #pragma unroll
-        for (int k = 0; k < 5; k++) { va[q].w[k] = 0; vc[q].w[k] = 0; }
-#pragma unroll 4
+        for (int k = 0; k < 5; k++) va[q].w[k] = 0;
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+#pragma unroll
+        for (int k = 0; k < 5; k++) vc[q].w[k] = 0;
+#pragma unroll 2
       for (int mm2 = 0; mm2 < 16; mm2++) {
-        const uint64_t* pw = my_x + (half * 16 + mm2) * 16;
+        const uint64_t* pw = my_x + (half * 16 + mm2) * 24;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
           int i = 4 * xm + q;
           acc_shift_xor(va[q], phi[byte_from_planes(pw, i)], mm2);
           acc_shift_xor(vc[q], phi[byte_from_planes(pw + 8, i)], mm2);
+          acc_shift_xor(vc[4 + q], phi[byte_from_planes(pw + 16, i)], mm2);
         }
       }
       gf128 e = gf_load(&eq_out[xo]);
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        sum_ab[q] = gf_add(sum_ab[q], gf_mul(acc_reduce(va[q]), e));
-        sum_c[q] = gf_add(sum_c[q], gf_mul(acc_reduce(vc[q]), e));
-      }
+      for (int q = 0; q < 4; q++) sum_ab[q] = gf_add(sum_ab[q], gf_mul(acc_reduce(va[q]), e));
+#pragma unroll
+      for (int q = 0; q < 8; q++) sum_c[q] = gf_add(sum_c[q], gf_mul(acc_reduce(vc[q]), e));
     }
     __syncwarp();
   }
-  // lanes l and l + 16 hold the same points: combine, then write this warp's partials.
+  // lanes l and l + 16 hold the same points: combine; then reduce the warps
+  // of the block in shared memory (reusing the exchange area) and write one
+  // row of 192 partial sums per block: 64 P^AB values, then S[0..128).
 #pragma unroll
   for (int q = 0; q < 4; q++)
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      sum_ab[q].w[k] ^= __shfl_xor_sync(0xffffffffu, sum_ab[q].w[k], 16);
-      sum_c[q].w[k] ^= __shfl_xor_sync(0xffffffffu, sum_c[q].w[k], 16);
-    }
+    for (int k = 0; k < 4; k++) sum_ab[q].w[k] ^= __shfl_xor_sync(0xffffffffu, sum_ab[q].w[k], 16);
+#pragma unroll
+  for (int q = 0; q < 8; q++)
+#pragma unroll
+    for (int k = 0; k < 4; k++) sum_c[q].w[k] ^= __shfl_xor_sync(0xffffffffu, sum_c[q].w[k], 16);
+  __syncthreads();
+  gf128* red = reinterpret_cast<gf128*>(xch);  // [warps][192]
   if (half == 0) {
-    gf128* out = partials + gwarp * 128;
+    gf128* o = red + warp * 192;
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-      out[4 * xm + q] = sum_ab[q];
-      out[64 + 4 * xm + q] = sum_c[q];
+      o[4 * xm + q] = sum_ab[q];
+      o[64 + 4 * xm + q] = sum_c[q];
+      o[128 + 4 * xm + q] = sum_c[4 + q];
     }
+  }
+  __syncthreads();
+  for (int col = threadIdx.x; col < 192; col += R1_THREADS) {
+    gf128 acc = gf_zero();
+    for (int w2 = 0; w2 < R1_THREADS / 32; w2++) acc = gf_add(acc, red[w2 * 192 + col]);
+    partials[(size_t)blockIdx.x * 192 + col] = acc;
   }
 }
 
-// XOR-reduce `count` rows of `width` F128 into out (one thread per column).
-__global__ void reduce_rows_kernel(const gf128* __restrict__ in, size_t count, int width, gf128* __restrict__ out) {
-  int col = blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= width) return;
+// XOR-reduce `count` rows of `width` F128 into out: each block owns 8 columns
+// and 32 row lanes, then folds the row lanes in shared memory.
+__global__ void __launch_bounds__(256)
+reduce_rows_kernel(const gf128* __restrict__ in, size_t count, int width, gf128* __restrict__ out) {
+  __shared__ gf128 red[32][8];
+  const int cl = threadIdx.x & 7, rl = threadIdx.x >> 3;
+  const int col = blockIdx.x * 8 + cl;
   gf128 acc = gf_zero();
-  for (size_t r = 0; r < count; r++) acc = gf_add(acc, in[r * width + col]);
-  out[col] = acc;
+  if (col < width)
+    for (size_t r = rl; r < count; r += 32) acc = gf_add(acc, in[r * width + col]);
+  red[rl][cl] = acc;
+  __syncthreads();
+  if (rl == 0 && col < width) {
+    for (int k = 1; k < 32; k++) acc = gf_add(acc, red[k][cl]);
+    out[col] = acc;
+  }
 }
 
 // Skip fold at z: out[x] = sum_s bit_s(W[x]) L_s(z), with 8 byte tables of the
@@ -332,7 +366,7 @@ __global__ void bind_pairs_kernel(const gf128* __restrict__ A, const gf128* __re
 
 int flock_launch_zc_round1(const void* a, const void* b, const void* c, size_t n_outer, const void* eq_out,
                            const ZcRound1Tables* d_tables, void* partials, int grid, cudaStream_t st) {
-  size_t smem = 8 * 256 * 8 * 8 + 256 * 16 + (R1_THREADS / 32) * 2 * 16 * 16 * 8;
+  size_t smem = 8 * 256 * 8 * 8 + 256 * 16 + (R1_THREADS / 32) * 2 * 16 * 24 * 8;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(zc_round1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -342,10 +376,10 @@ int flock_launch_zc_round1(const void* a, const void* b, const void* c, size_t n
                                                    n_outer, (const gf128*)eq_out, d_tables, (gf128*)partials); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
-int flock_zc_round1_warps(int grid) { return grid * (R1_THREADS / 32); }
+
 
 int flock_launch_reduce_rows(const void* in, size_t count, int width, void* out, cudaStream_t st) {
-  reduce_rows_kernel<<<(width + 127) / 128, 128, 0, st>>>((const gf128*)in, count, width, (gf128*)out); flock_count_launch();
+  reduce_rows_kernel<<<(width + 7) / 8, 256, 0, st>>>((const gf128*)in, count, width, (gf128*)out); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
