@@ -2,8 +2,7 @@
 //
 // Follows the reference compression at
 // crates/flock-prover/src/r1cs_hashes/blake3.rs:271-310 (IV, message
-// permutation, column/diagonal G order, finalization XORs). The message
-// schedule is unrolled at compile time, so permutations cost no instructions.
+// permutation, column/diagonal G order, finalization XORs).
 #pragma once
 #include <cstdint>
 
@@ -15,12 +14,16 @@ __host__ __device__ constexpr uint32_t IV(int i) {
 }
 enum : uint32_t { CHUNK_START = 1, CHUNK_END = 2, PARENT = 4, ROOT = 8 };
 
-// Message word used by round r at schedule slot s: PERM applied r times.
-__host__ __device__ constexpr int perm1(int i) {
-  return i == 0 ? 2 : i == 1 ? 6 : i == 2 ? 3 : i == 3 ? 10 : i == 4 ? 7 : i == 5 ? 0 : i == 6 ? 4 : i == 7 ? 13
-       : i == 8 ? 1 : i == 9 ? 11 : i == 10 ? 12 : i == 11 ? 5 : i == 12 ? 9 : i == 13 ? 14 : i == 14 ? 15 : 8;
+// Message words of the next round: m'[i] = m[PERM[i]] with the BLAKE3
+// message permutation (2, 6, 3, 10, 7, 0, 4, 13, 1, 11, 12, 5, 9, 14, 15, 8).
+// Every index is a constant, so once the rounds are unrolled the permutation
+// is register renaming and costs no instructions.
+__device__ __forceinline__ void permute(uint32_t m[16]) {
+  uint32_t t[16] = {m[2], m[6], m[3], m[10], m[7], m[0], m[4], m[13],
+                    m[1], m[11], m[12], m[5], m[9], m[14], m[15], m[8]};
+#pragma unroll
+  for (int i = 0; i < 16; i++) m[i] = t[i];
 }
-__host__ __device__ constexpr int sched(int r, int s) { return r == 0 ? s : sched(r - 1, perm1(s)); }
 
 __device__ __forceinline__ uint32_t rotr(uint32_t x, int n) { return __funnelshift_r(x, x, n); }
 
@@ -40,16 +43,20 @@ __device__ __forceinline__ void compress(const uint32_t cv[8], const uint32_t m[
                                          uint32_t block_len, uint32_t flags, uint32_t out[16]) {
   uint32_t v[16] = {cv[0], cv[1], cv[2], cv[3], cv[4], cv[5], cv[6], cv[7],
                     IV(0), IV(1), IV(2), IV(3), (uint32_t)counter, (uint32_t)(counter >> 32), block_len, flags};
+  uint32_t w[16];
+#pragma unroll
+  for (int i = 0; i < 16; i++) w[i] = m[i];
 #pragma unroll
   for (int r = 0; r < 7; r++) {
-    B3_G(0, 4, 8, 12, m[sched(r, 0)], m[sched(r, 1)]);
-    B3_G(1, 5, 9, 13, m[sched(r, 2)], m[sched(r, 3)]);
-    B3_G(2, 6, 10, 14, m[sched(r, 4)], m[sched(r, 5)]);
-    B3_G(3, 7, 11, 15, m[sched(r, 6)], m[sched(r, 7)]);
-    B3_G(0, 5, 10, 15, m[sched(r, 8)], m[sched(r, 9)]);
-    B3_G(1, 6, 11, 12, m[sched(r, 10)], m[sched(r, 11)]);
-    B3_G(2, 7, 8, 13, m[sched(r, 12)], m[sched(r, 13)]);
-    B3_G(3, 4, 9, 14, m[sched(r, 14)], m[sched(r, 15)]);
+    B3_G(0, 4, 8, 12, w[0], w[1]);
+    B3_G(1, 5, 9, 13, w[2], w[3]);
+    B3_G(2, 6, 10, 14, w[4], w[5]);
+    B3_G(3, 7, 11, 15, w[6], w[7]);
+    B3_G(0, 5, 10, 15, w[8], w[9]);
+    B3_G(1, 6, 11, 12, w[10], w[11]);
+    B3_G(2, 7, 8, 13, w[12], w[13]);
+    B3_G(3, 4, 9, 14, w[14], w[15]);
+    if (r < 6) permute(w);
   }
 #pragma unroll
   for (int i = 0; i < 8; i++) {
@@ -63,16 +70,20 @@ __device__ __forceinline__ void compress_cv(uint32_t cv[8], const uint32_t m[16]
                                             uint32_t flags) {
   uint32_t v[16] = {cv[0], cv[1], cv[2], cv[3], cv[4], cv[5], cv[6], cv[7],
                     IV(0), IV(1), IV(2), IV(3), 0u, 0u, block_len, flags};
+  uint32_t w[16];
+#pragma unroll
+  for (int i = 0; i < 16; i++) w[i] = m[i];
 #pragma unroll
   for (int r = 0; r < 7; r++) {
-    B3_G(0, 4, 8, 12, m[sched(r, 0)], m[sched(r, 1)]);
-    B3_G(1, 5, 9, 13, m[sched(r, 2)], m[sched(r, 3)]);
-    B3_G(2, 6, 10, 14, m[sched(r, 4)], m[sched(r, 5)]);
-    B3_G(3, 7, 11, 15, m[sched(r, 6)], m[sched(r, 7)]);
-    B3_G(0, 5, 10, 15, m[sched(r, 8)], m[sched(r, 9)]);
-    B3_G(1, 6, 11, 12, m[sched(r, 10)], m[sched(r, 11)]);
-    B3_G(2, 7, 8, 13, m[sched(r, 12)], m[sched(r, 13)]);
-    B3_G(3, 4, 9, 14, m[sched(r, 14)], m[sched(r, 15)]);
+    B3_G(0, 4, 8, 12, w[0], w[1]);
+    B3_G(1, 5, 9, 13, w[2], w[3]);
+    B3_G(2, 6, 10, 14, w[4], w[5]);
+    B3_G(3, 7, 11, 15, w[6], w[7]);
+    B3_G(0, 5, 10, 15, w[8], w[9]);
+    B3_G(1, 6, 11, 12, w[10], w[11]);
+    B3_G(2, 7, 8, 13, w[12], w[13]);
+    B3_G(3, 4, 9, 14, w[14], w[15]);
+    if (r < 6) permute(w);
   }
 #pragma unroll
   for (int i = 0; i < 8; i++) cv[i] = v[i] ^ v[i + 8];

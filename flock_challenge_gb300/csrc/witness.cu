@@ -136,7 +136,7 @@ struct Sink {
 #define WG(LA, LB, LC, LD, R, S)                                        \
   {                                                                     \
     uint32_t a_ = s[LA], b_ = s[LB], c_ = s[LC], d_ = s[LD];            \
-    uint32_t mx = m[b3::sched(R, S)], my = m[b3::sched(R, S + 1)];      \
+    uint32_t mx = mp[S], my = mp[S + 1];                                \
     uint32_t t0 = k.add(c, a_, b_);                                     \
     uint32_t a1 = k.add(c, t0, mx);                                     \
     uint32_t d1 = b3::rotr(d_ ^ a1, 16);                                \
@@ -207,6 +207,9 @@ witness_kernel(const flock_compression* __restrict__ in, size_t n_in, size_t n_t
   k.lin(c, flg);
   uint32_t s[16] = {cv[0], cv[1], cv[2], cv[3], cv[4], cv[5], cv[6], cv[7],
                     b3::IV(0), b3::IV(1), b3::IV(2), b3::IV(3), tlo, thi, blen, flg};
+  uint32_t mp[16];  // this round's message order
+#pragma unroll
+  for (int i = 0; i < 16; i++) mp[i] = m[i];
 #pragma unroll
   for (int r = 0; r < 7; r++) {
     WG(0, 4, 8, 12, r, 0);
@@ -217,6 +220,7 @@ witness_kernel(const flock_compression* __restrict__ in, size_t n_in, size_t n_t
     WG(1, 6, 11, 12, r, 10);
     WG(2, 7, 8, 13, r, 12);
     WG(3, 4, 9, 14, r, 14);
+    if (r < 6) b3::permute(mp);
   }
 #pragma unroll
   for (int i = 0; i < 8; i++) k.lin(c, s[i + 8] ^ cv[i]);  // out_hi
