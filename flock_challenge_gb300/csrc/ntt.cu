@@ -186,3 +186,121 @@ int flock_launch_ntt(void* d_data, const void* d_src, int log_d, int log_lanes, 
   }
   return FLOCK_OK;
 }
+
+// ---- NTT without device allocation -----------------------------------------
+//
+// Some callers cannot allocate device memory: a host framework that owns all
+// of the GPU's memory through its own pool, or code running where cudaMalloc
+// is not allowed (inside an allocator callback, or while a stream is being
+// captured). flock_launch_ntt allocates a twiddle table per (device, log_d) on
+// first use; flock_ntt_noalloc instead writes the table of each call into the
+// fixed array below, which the module holds on every GPU that loads this
+// library until the process exits.
+//
+// Every call shares the array and leaves its own table there. Each call
+// rewrites all entries it reads before its passes read them, so nothing has to
+// start at zero; but two calls whose work overlaps on the GPU (different
+// streams, no ordering between them) overwrite each other's table and race.
+
+namespace {
+
+constexpr int kNoAllocMaxLogD = FLOCK_NTT_NOALLOC_MAX_LOG_D;
+constexpr int kMaxDevices = 64;
+
+// Twiddle table of one transform of up to 2^16 positions: 2^16 - 1 entries
+// of 16 bytes (1 MiB, the last entry unused).
+__device__ __align__(256) gf128 g_noalloc_twiddles[(size_t)1 << kNoAllocMaxLogD];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kMaxDevices];  // device address of g_noalloc_twiddles per device
+
+// Entry (layer, bit) of the breadth-first table's generators: for layer l the
+// table holds the 2^l subset sums of {row_l[bit] : bit < l}, at
+// v[l(l-1)/2 + bit]. 120 entries cover log_d = 16.
+struct TwiddleGenerators {
+  gf128 v[kNoAllocMaxLogD * (kNoAllocMaxLogD - 1) / 2];
+};
+
+__global__ void expand_twiddles_kernel(const __grid_constant__ TwiddleGenerators gen, int log_d,
+                                       gf128* __restrict__ tw) {
+  uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t total = (1u << log_d) - 1;
+  if (idx >= total) return;
+  int layer = 31 - __clz(idx + 1);
+  uint32_t j = idx + 1 - (1u << layer);
+  const gf128* row = gen.v + layer * (layer - 1) / 2;
+  gf128 acc = gf_zero();
+  for (int bit = 0; bit < layer; bit++)
+    if ((j >> bit) & 1) acc = gf_add(acc, row[bit]);
+  tw[idx] = acc;
+}
+
+// The same normalized subspace-polynomial rows as host_twiddles, in fixed
+// arrays: gen row of layer l is ev[d - l - 1][1 .. l].
+void twiddle_generators(int d, TwiddleGenerators* gen) {
+  hf::F ev[kNoAllocMaxLogD][kNoAllocMaxLogD];
+  for (int i = 0; i < d; i++) ev[0][i] = i < 64 ? hf::F(1ULL << i, 0) : hf::F(0, 1ULL << (i - 64));
+  for (int i = 1; i < d; i++)
+    for (int k = 1; k < d - i + 1; k++) ev[i][k - 1] = ev[i - 1][k] * (ev[i - 1][k] + ev[i - 1][0]);
+  for (int i = 0; i < d; i++) {
+    hf::F iv = hf::inv(ev[i][0]);
+    for (int k = 0; k < d - i; k++) ev[i][k] = ev[i][k] * iv;
+  }
+  for (int layer = 1; layer < d; layer++) {
+    const hf::F* row = ev[d - layer - 1];
+    for (int bit = 0; bit < layer; bit++) {
+      gf128& g = gen->v[layer * (layer - 1) / 2 + bit];
+      g.w[0] = (uint32_t)row[bit + 1].lo;
+      g.w[1] = (uint32_t)(row[bit + 1].lo >> 32);
+      g.w[2] = (uint32_t)row[bit + 1].hi;
+      g.w[3] = (uint32_t)(row[bit + 1].hi >> 32);
+    }
+  }
+}
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the first call on each device; later calls read the cache).
+int noalloc_scratch(gf128** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return FLOCK_ERR_CUDA;
+  if (dev < 0 || dev >= kMaxDevices) return FLOCK_ERR_ARG;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_twiddles) != cudaSuccess || !p) return FLOCK_ERR_CUDA;
+    g_noalloc_addr[dev] = p;
+  }
+  *out = (gf128*)g_noalloc_addr[dev];
+  return FLOCK_OK;
+}
+
+}  // namespace
+
+extern "C" int flock_ntt_noalloc(void* d_data, int log_d, int log_num_ntts, int start_layer, void* stream) {
+  if (!d_data) return FLOCK_ERR_ARG;
+  if (log_d > kNoAllocMaxLogD) return FLOCK_ERR_LIMIT;
+  if (log_num_ntts < 3 || log_num_ntts > 10 || log_d < 1 || start_layer < 0 || start_layer > log_d)
+    return FLOCK_ERR_SHAPE;
+  gf128* tw = nullptr;
+  int rc = noalloc_scratch(&tw);
+  if (rc != FLOCK_OK) return rc;
+  if (start_layer == log_d) return FLOCK_OK;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  TwiddleGenerators gen = {};
+  twiddle_generators(log_d, &gen);
+  uint32_t total = (1u << log_d) - 1;
+  expand_twiddles_kernel<<<(total + 255) / 256, 256, 0, st>>>(gen, log_d, tw);
+  flock_count_launch();
+  if (cudaGetLastError() != cudaSuccess) return FLOCK_ERR_CUDA;
+  gf128* data = (gf128*)d_data;
+  int remaining = log_d - start_layer;
+  int passes = (remaining + 5) / 6;
+  int l = start_layer;
+  for (int q = 0; q < passes; q++) {
+    int f = (remaining - (l - start_layer) + (passes - q) - 1) / (passes - q);
+    rc = run_pass(f, data, data, ~(size_t)0, tw, log_d, log_num_ntts, l, st);
+    if (rc != FLOCK_OK) return rc;
+    l += f;
+  }
+  return FLOCK_OK;
+}

@@ -27,7 +27,8 @@ enum {
   FLOCK_ERR_ARG = -4,     /* null or inconsistent argument */
   FLOCK_ERR_CAPACITY = -5,/* output buffer too small */
   FLOCK_ERR_TIMEOUT = -6, /* a bounded device wait expired */
-  FLOCK_ERR_VERIFY = -7   /* an internal consistency check failed */
+  FLOCK_ERR_VERIFY = -7,  /* an internal consistency check failed */
+  FLOCK_ERR_LIMIT = -8    /* size above the fixed limit of an entry point that allocates nothing */
 };
 
 /* One BLAKE3 compression input (112 bytes). Mirrors the reference tuple
@@ -76,6 +77,21 @@ int flock_witness(const flock_compression* d_in, size_t n, int n_blocks_log, voi
  * start_layer. Replaces AdditiveNttF128::forward_transform_interleaved_from_layer
  * (crates/flock-core/src/ntt/additive_ntt_f128.rs:599-622). */
 int flock_ntt(flock_ctx* ctx, void* d_data, int log_d, int log_num_ntts, int start_layer, void* stream);
+
+/* Largest log_d flock_ntt_noalloc accepts (2^16 positions per transform). */
+#define FLOCK_NTT_NOALLOC_MAX_LOG_D 16
+
+/* flock_ntt for callers that cannot allocate device memory (a host framework
+ * that owns the GPU's memory through its own pool, or code running where
+ * cudaMalloc is not allowed). No counterpart in the reference: it exists for
+ * those callers only. Same transform, arguments and output as flock_ntt on
+ * the current device, without a context. The twiddle table lives in a fixed
+ * 1 MiB device array of the library (held on every GPU that loads it until
+ * exit); log_d above FLOCK_NTT_NOALLOC_MAX_LOG_D returns FLOCK_ERR_LIMIT. The
+ * first call on a device looks up that array's address, so make it before any
+ * stream capture. Calls share the array: calls whose work overlaps on the GPU
+ * race. Calls no cudaMalloc, cudaFree or other allocating routine. */
+int flock_ntt_noalloc(void* d_data, int log_d, int log_num_ntts, int start_layer, void* stream);
 
 /* Flat BLAKE3 Merkle tree (leaves first, root last; 2*n_leaves-1 nodes of 32
  * bytes) over n_leaves equal leaves of leaf_bytes (a multiple of 64, at most
