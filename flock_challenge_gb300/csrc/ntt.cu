@@ -6,15 +6,19 @@
 // 2^(log_d-l-1) positions and block b = pos >> (log_d - l) uses twiddle
 // t(l, b) = table[2^l - 1 + b]; butterfly u += v*t, v += u.
 //
-// GB300 mapping: a pass applies F consecutive layers to a tile of 2^F
-// positions x 16 lanes (8 when the code has 8 lanes) held in shared memory. The tile's positions differ only
-// in the F pair bits of those layers, so every butterfly of the pass stays in
-// the tile and the pass costs one HBM read and one write of the codeword.
-// Each tile row (16 lanes x 16 B) is a contiguous 256-byte run, read and
-// written with 16-byte vector accesses. A pass may read its input from a
-// separate source with a position mask: the first pass of a rate-1/2^r code
-// reads the message directly, position p taking row p mod 2^(log_d - r), which
-// is the replicated state after the r copy layers (pcs/commit.rs:451-473).
+// GB300 mapping: a pass applies F <= 8 consecutive layers to a tile of 2^F
+// positions x 16 lanes (8 when the code has 8 lanes). The tile's positions
+// differ only in the F pair bits of those layers, so every butterfly of the
+// pass stays in the tile and the pass costs one HBM read and one write of the
+// codeword. Each thread holds one lane of 16 positions in registers and
+// applies up to four layers there (eight independent GF(2^128) products per
+// layer keep the integer pipes busy), then the tile is exchanged once through
+// shared memory for the remaining layers. Each tile row (16 lanes x 16 B) is a
+// contiguous 256-byte run, read and written with 16-byte vector accesses. A
+// pass may read its input from a separate source with a position mask: the
+// first pass of a rate-1/2^r code reads the message directly, position p
+// taking row p mod 2^(log_d - r), which is the replicated state after the r
+// copy layers (pcs/commit.rs:451-473).
 #include <cstdio>
 #include <map>
 #include <mutex>
@@ -26,50 +30,119 @@
 
 namespace {
 
-constexpr int NTT_THREADS = 256;
 
-template <int F, int TILE_LANES>
-__global__ void __launch_bounds__(NTT_THREADS)
+// One pass of F layers (l0 .. l0+F-1) over tiles of 2^F positions x TL lanes.
+// A thread keeps one lane of 2^E positions (E = min(F, 4)) in registers, so a
+// layer gives it 2^(E-1) independent butterflies; the pass runs as two stages
+// of at most four layers (the top k1 pair bits, then the low k2 bits) with one
+// shared-memory exchange between them. Loads and stores go straight between
+// HBM and registers: the TL lanes of a position are a contiguous TL*16-byte run.
+// Positions per thread (log2) and the resident threads per SM the register
+// budget is sized for; measured on the L0 commit (2^20 x 64 lanes) and the
+// 8-lane Ligerito codes, 8 positions per thread at 512 threads per SM is best.
+#ifndef NTT_POS_LOG
+#define NTT_POS_LOG 3
+#endif
+#ifndef NTT_SM_THREADS
+#define NTT_SM_THREADS 512
+#endif
+template <int F, int TL>
+struct PassShape {
+  static constexpr int E = F < NTT_POS_LOG ? F : NTT_POS_LOG;  // positions per thread (log2)
+  static constexpr int K1 = F <= E ? F : (F + 1) / 2 < E ? (F + 1) / 2 : E;  // stage 1 layers
+  static constexpr int K2 = F - K1;
+  static_assert(K2 <= E, "a pass covers at most 2 * NTT_POS_LOG layers");
+  static constexpr int PT = 1 << (F - E);            // threads per lane
+  static constexpr int THREADS = TL * PT;
+  static constexpr int SMEM = K2 > 0 ? (1 << F) * TL * 16 : 16;
+  static constexpr int MIN_BLOCKS =
+      NTT_SM_THREADS / THREADS < 1 ? 1 : NTT_SM_THREADS / THREADS > 32 ? 32 : NTT_SM_THREADS / THREADS;
+};
+
+// Tile position of the element with label j in stage 1 / stage 2. Labels are
+// ordered so that the pair bits of the stage's layers are the label's top bits
+// in layer order (stage 1: tile bits F-1 .. F-K1; stage 2: tile bits K2-1 .. 0);
+// the other label bits and the thread index pt fill the remaining tile bits.
+template <int F, int E, int K1>
+__device__ __forceinline__ int pos_stage1(int pt, int j) {
+  return ((j >> (E - K1)) << (F - K1)) | (pt << (E - K1)) | (j & ((1 << (E - K1)) - 1));
+}
+template <int F, int E, int K2>
+__device__ __forceinline__ int pos_stage2(int pt, int j) {
+  return ((j & ((1 << (E - K2)) - 1)) << (F - (E - K2))) | (pt << K2) | (j >> (E - K2));
+}
+template <int E>
+__host__ __device__ constexpr int rotr_bits(int j, int r) {
+  return r == 0 ? j : ((j >> r) | (j << (E - r))) & ((1 << E) - 1);
+}
+
+template <int F, int TL>
+__global__ void __launch_bounds__(PassShape<F, TL>::THREADS, PassShape<F, TL>::MIN_BLOCKS)
 ntt_pass_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t src_pos_mask,
                 const gf128* __restrict__ tw, int log_d, int log_lanes, int l0) {
-  __shared__ gf128 tile[(1 << F) * TILE_LANES];
-  const int lane_groups = (1 << log_lanes) / TILE_LANES;
+  using S = PassShape<F, TL>;
+  constexpr int E = S::E, K1 = S::K1, K2 = S::K2, NE = 1 << E, H = NE / 2;
+  extern __shared__ gf128 tile[];
+  const int lane_groups = (1 << log_lanes) / TL;
   const size_t tile_id = blockIdx.x / lane_groups;
   const int lg = blockIdx.x % lane_groups;
   const int lo_bits = log_d - l0 - F;
   const size_t lo = tile_id & (((size_t)1 << lo_bits) - 1);
   const size_t hi = tile_id >> lo_bits;
   const size_t nl = (size_t)1 << log_lanes;
+  const int ln = threadIdx.x % TL, pt = threadIdx.x / TL;
+  const size_t col = (size_t)lg * TL + ln;
+  auto gpos = [&](int i) { return (hi << (log_d - l0)) | ((size_t)i << lo_bits) | lo; };
 
-  // Load 2^F rows of 16 lanes.
-  for (int e = threadIdx.x; e < (1 << F) * TILE_LANES; e += NTT_THREADS) {
-    int i = e / TILE_LANES, ln = e % TILE_LANES;
-    size_t p = (hi << (log_d - l0)) | ((size_t)i << lo_bits) | lo;
-    size_t sp = p & src_pos_mask;
-    tile[e] = gf_load(&src[sp * nl + (size_t)lg * TILE_LANES + ln]);
-  }
-  __syncthreads();
+  gf128 y[NE];
 #pragma unroll
-  for (int s = 0; s < F; s++) {
-    const int pb = F - 1 - s;  // pair bit inside the tile index
-    for (int e = threadIdx.x; e < (1 << (F - 1)) * TILE_LANES; e += NTT_THREADS) {
-      int pair = e / TILE_LANES, ln = e % TILE_LANES;
-      int i0 = ((pair >> pb) << (pb + 1)) | (pair & ((1 << pb) - 1));
-      int i1 = i0 | (1 << pb);
-      size_t blk = (hi << s) | ((size_t)i0 >> (F - s));
-      gf128 t = gf_load(&tw[(((size_t)1) << (l0 + s)) - 1 + blk]);
-      gf128 u = tile[i0 * TILE_LANES + ln], v = tile[i1 * TILE_LANES + ln];
-      u = gf_add(u, gf_mul(v, t));
-      v = gf_add(v, u);
-      tile[i0 * TILE_LANES + ln] = u;
-      tile[i1 * TILE_LANES + ln] = v;
+  for (int j = 0; j < NE; j++) y[j] = gf_load(&src[(gpos(pos_stage1<F, E, K1>(pt, j)) & src_pos_mask) * nl + col]);
+
+  // One layer per iteration, always pairing labels j and j + H (the top label
+  // bit); the labels are then rotated left by one bit so the next layer's pair
+  // bit is on top. The body stays small (H products), which keeps the hot loop
+  // inside the instruction cache.
+#pragma unroll 1
+  for (int t = 0; t < F; t++) {
+    if (K2 > 0 && t == K1) {
+      // stage 1 done: labels are rotated by K1; exchange into stage-2 labels
+      __syncwarp();
+#pragma unroll
+      for (int j = 0; j < NE; j++) tile[pos_stage1<F, E, K1>(pt, rotr_bits<E>(j, K1 % E)) * TL + ln] = y[j];
+      __syncthreads();
+#pragma unroll
+      for (int j = 0; j < NE; j++) y[j] = tile[pos_stage2<F, E, K2>(pt, j) * TL + ln];
     }
-    __syncthreads();
+    const bool st2 = t >= K1;
+    const int r = st2 ? t - K1 : t;
+    const gf128* twl = tw + ((((size_t)1) << (l0 + t)) - 1 + (hi << t));
+    gf128 tv[H];
+#pragma unroll
+    for (int j = 0; j < H; j++) {
+      const int jo = ((j >> r) | (j << (E - r))) & (NE - 1);
+      const int i0 = st2 ? pos_stage2<F, E, K2>(pt, jo) : pos_stage1<F, E, K1>(pt, jo);
+      tv[j] = gf_load(&twl[i0 >> (F - t)]);
+    }
+#pragma unroll
+    for (int j = 0; j < H; j++) {
+      y[j] = gf_add(y[j], gf_mul(y[j + H], tv[j]));
+      y[j + H] = gf_add(y[j + H], y[j]);
+    }
+    // rotate labels left by one: new[k] = old[rotr(k, 1)]
+    gf128 z[NE];
+#pragma unroll
+    for (int k = 0; k < NE; k++) z[k] = y[rotr_bits<E>(k, 1 % E)];
+#pragma unroll
+    for (int k = 0; k < NE; k++) y[k] = z[k];
   }
-  for (int e = threadIdx.x; e < (1 << F) * TILE_LANES; e += NTT_THREADS) {
-    int i = e / TILE_LANES, ln = e % TILE_LANES;
-    size_t p = (hi << (log_d - l0)) | ((size_t)i << lo_bits) | lo;
-    gf_store(&dst[p * nl + (size_t)lg * TILE_LANES + ln], tile[e]);
+  if (K2 > 0) {
+#pragma unroll
+    for (int j = 0; j < NE; j++)
+      gf_store(&dst[gpos(pos_stage2<F, E, K2>(pt, rotr_bits<E>(j, K2 % E))) * nl + col], y[j]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < NE; j++)
+      gf_store(&dst[gpos(pos_stage1<F, E, K1>(pt, rotr_bits<E>(j, K1 % E))) * nl + col], y[j]);
   }
 }
 
@@ -102,22 +175,43 @@ std::vector<hf::F> host_twiddles(int d) {
 std::mutex g_tw_mu;
 std::map<std::pair<int, int>, void*> g_tw;  // (device, log_d) -> device table
 
+constexpr int kMaxPassLayers = 2 * NTT_POS_LOG < 8 ? 2 * NTT_POS_LOG : 8;
+
 template <int F>
 int launch_pass(gf128* dst, const gf128* src, size_t mask, const gf128* tw, int log_d, int log_lanes, int l0,
                 cudaStream_t st) {
-  size_t tiles = (size_t)1 << (log_d - F);
-  if (log_lanes >= 4) {
-    size_t blocks = tiles * ((1 << log_lanes) / 16);
-    ntt_pass_kernel<F, 16><<<(unsigned)blocks, NTT_THREADS, 0, st>>>(dst, src, mask, tw, log_d, log_lanes, l0); flock_count_launch();
+  if constexpr (F > kMaxPassLayers) {
+    return FLOCK_ERR_SHAPE;
   } else {
-    size_t blocks = tiles * ((1 << log_lanes) / 8);
-    ntt_pass_kernel<F, 8><<<(unsigned)blocks, NTT_THREADS, 0, st>>>(dst, src, mask, tw, log_d, log_lanes, l0); flock_count_launch();
+    size_t tiles = (size_t)1 << (log_d - F);
+    if (log_lanes >= 4) {
+      using S = PassShape<F, 16>;
+      size_t blocks = tiles * ((1 << log_lanes) / 16);
+      ntt_pass_kernel<F, 16><<<(unsigned)blocks, S::THREADS, S::SMEM, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
+    } else {
+      using S = PassShape<F, 8>;
+      size_t blocks = tiles * ((1 << log_lanes) / 8);
+      ntt_pass_kernel<F, 8><<<(unsigned)blocks, S::THREADS, S::SMEM, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
+    }
+    flock_count_launch();
+    return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
   }
-  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+// Raises the dynamic shared-memory limit of the passes that need more than
+// the default 48 KB (F = 8 with 16 lanes: 64 KB), once per process.
+void ntt_set_smem_attrs() {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    if constexpr (kMaxPassLayers >= 8)
+      cudaFuncSetAttribute(ntt_pass_kernel<kMaxPassLayers, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           PassShape<kMaxPassLayers, 16>::SMEM);
+  });
 }
 
 int run_pass(int f, gf128* dst, const gf128* src, size_t mask, const gf128* tw, int log_d, int log_lanes, int l0,
              cudaStream_t st) {
+  ntt_set_smem_attrs();
   switch (f) {
     case 1: return launch_pass<1>(dst, src, mask, tw, log_d, log_lanes, l0, st);
     case 2: return launch_pass<2>(dst, src, mask, tw, log_d, log_lanes, l0, st);
@@ -125,6 +219,8 @@ int run_pass(int f, gf128* dst, const gf128* src, size_t mask, const gf128* tw, 
     case 4: return launch_pass<4>(dst, src, mask, tw, log_d, log_lanes, l0, st);
     case 5: return launch_pass<5>(dst, src, mask, tw, log_d, log_lanes, l0, st);
     case 6: return launch_pass<6>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 7: return launch_pass<7>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 8: return launch_pass<8>(dst, src, mask, tw, log_d, log_lanes, l0, st);
     default: return FLOCK_ERR_SHAPE;
   }
 }
@@ -149,7 +245,7 @@ const void* flock_ntt_twiddles(int log_d) {
   return d;
 }
 
-// Applies layers [start_layer, log_d) in passes of up to 6 layers. d_src (may
+// Applies layers [start_layer, log_d) in passes of up to 8 layers. d_src (may
 // equal d_data) holds the input rows addressed with position mask
 // 2^(log_d - start_layer) - 1, so a distinct d_src supplies the replicated
 // message of a rate-1/2^start_layer code.
@@ -174,7 +270,7 @@ int flock_launch_ntt(void* d_data, const void* d_src, int log_d, int log_lanes, 
     return FLOCK_OK;
   }
   int remaining = log_d - start_layer;
-  int passes = (remaining + 5) / 6;
+  int passes = (remaining + kMaxPassLayers - 1) / kMaxPassLayers;
   int l = start_layer;
   for (int q = 0; q < passes; q++) {
     int f = (remaining - (l - start_layer) + (passes - q) - 1) / (passes - q);
@@ -294,7 +390,7 @@ extern "C" int flock_ntt_noalloc(void* d_data, int log_d, int log_num_ntts, int 
   if (cudaGetLastError() != cudaSuccess) return FLOCK_ERR_CUDA;
   gf128* data = (gf128*)d_data;
   int remaining = log_d - start_layer;
-  int passes = (remaining + 5) / 6;
+  int passes = (remaining + kMaxPassLayers - 1) / kMaxPassLayers;
   int l = start_layer;
   for (int q = 0; q < passes; q++) {
     int f = (remaining - (l - start_layer) + (passes - q) - 1) / (passes - q);

@@ -34,19 +34,6 @@ struct Acc5 {
   uint32_t w[5];
 };
 
-__device__ __forceinline__ void acc_shift_xor(Acc5& a, const uint4 v, int sh) {
-  // a ^= v << sh, 0 <= sh < 16
-  if (sh == 0) {
-    a.w[0] ^= v.x; a.w[1] ^= v.y; a.w[2] ^= v.z; a.w[3] ^= v.w;
-  } else {
-    a.w[0] ^= v.x << sh;
-    a.w[1] ^= __funnelshift_l(v.x, v.y, sh);
-    a.w[2] ^= __funnelshift_l(v.y, v.z, sh);
-    a.w[3] ^= __funnelshift_l(v.z, v.w, sh);
-    a.w[4] ^= v.w >> (32 - sh);
-  }
-}
-
 __device__ __forceinline__ gf128 acc_reduce(const Acc5& a) {
   // bits 128..143 live in w[4] (< 2^15): fold with x^128 = x^7 + x^2 + x + 1
   uint32_t ov = a.w[4];
@@ -79,12 +66,60 @@ __device__ __forceinline__ void f8_mul_planes(const uint64_t* a, const uint64_t*
   for (int k = 0; k < 8; k++) out[k] = p[k];
 }
 
-__device__ __forceinline__ uint32_t byte_from_planes(const uint64_t* pl, int i) {
-  uint32_t v = 0;
-#pragma unroll
-  for (int j = 0; j < 8; j++) v |= (uint32_t)((pl[j] >> i) & 1) << j;
-  return v;
+// 8x8 bit-matrix transpose: bit 8r + c <-> bit 8c + r.
+__device__ __forceinline__ uint64_t transpose8x8(uint64_t x) {
+  uint64_t t;
+  t = (x ^ (x >> 7)) & 0x00AA00AA00AA00AAull; x = x ^ t ^ (t << 7);
+  t = (x ^ (x >> 14)) & 0x0000CCCC0000CCCCull; x = x ^ t ^ (t << 14);
+  t = (x ^ (x >> 28)) & 0x00000000F0F0F0F0ull; x = x ^ t ^ (t << 28);
+  return x;
 }
+
+// Eight 64-bit planes -> 64 bytes (byte i = sum_j bit i of p[j] << j), as 16
+// words in dst (word k holds bytes 4k .. 4k+3), written with 16-byte stores.
+__device__ __forceinline__ void planes_to_bytes(const uint64_t p[8], uint32_t* dst) {
+  uint32_t o[16];
+#pragma unroll
+  for (int g = 0; g < 8; g++) {
+    const int hw = g >> 2, b = g & 3;
+    uint32_t q[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) q[j] = hw ? (uint32_t)(p[j] >> 32) : (uint32_t)p[j];
+    // byte j of x = byte g of p[j]
+    const uint32_t sel = (uint32_t)b | ((uint32_t)(b + 4) << 4);
+    const uint32_t lo = __byte_perm(__byte_perm(q[0], q[1], sel), __byte_perm(q[2], q[3], sel), 0x5410);
+    const uint32_t hi = __byte_perm(__byte_perm(q[4], q[5], sel), __byte_perm(q[6], q[7], sel), 0x5410);
+    const uint64_t y = transpose8x8(((uint64_t)hi << 32) | lo);
+    o[2 * g] = (uint32_t)y;
+    o[2 * g + 1] = (uint32_t)(y >> 32);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+    reinterpret_cast<uint4*>(dst)[k] = make_uint4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
+}
+
+// a ^= v << sh for 0 <= sh < 16, branch-free.
+__device__ __forceinline__ void acc_shift_xor_v(Acc5& a, const uint4 v, uint32_t sh) {
+  a.w[0] ^= v.x << sh;
+  a.w[1] ^= __funnelshift_l(v.x, v.y, sh);
+  a.w[2] ^= __funnelshift_l(v.y, v.z, sh);
+  a.w[3] ^= __funnelshift_l(v.z, v.w, sh);
+  a.w[4] ^= __funnelshift_l(v.w, 0u, sh);
+}
+
+// Shared memory of the round-1 kernel (32-bit words):
+//   ext  [8 byte positions c][4 quarters q][256 values] of 16 B (a value's
+//        eight 64-bit planes, quarter q = planes 2q, 2q+1): consecutive values
+//        of one quarter are consecutive 16-byte slots, so random lookups spread
+//        over all bank groups;
+//   phi  [256] of 16 B;
+//   xch  per warp, per half: [3 sets][16 xm] rows of 20 words (64 bytes used;
+//        the odd 80-byte row pitch makes the 16-byte stores conflict-free),
+//        halves 976 words apart (16 mod 32 banks) so both halves' reads of
+//        one row index hit disjoint banks.
+constexpr int R1_ROW = 20;
+constexpr int R1_HALF = 3 * 16 * R1_ROW + 16;
+constexpr size_t R1_SMEM = (size_t)8 * 4 * 256 * 16 + 256 * 16 + (size_t)(R1_THREADS / 32) * 2 * R1_HALF * 4;
 
 // grid: each warp walks pairs of outer blocks; lane: xm = lane & 15, xo half = lane >> 4.
 __global__ void __launch_bounds__(R1_THREADS, 1)
@@ -92,16 +127,20 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
                  size_t n_outer, const gf128* __restrict__ eq_out, const ZcRound1Tables* __restrict__ T,
                  gf128* __restrict__ partials) {
   extern __shared__ uint4 sm[];
-  uint64_t* ext = reinterpret_cast<uint64_t*>(sm);                  // [8][256][8]
-  uint4* phi = sm + (8 * 256 * 8 * 8) / 16;                         // [256]
-  uint64_t* xch = reinterpret_cast<uint64_t*>(phi + 256);           // per warp [2][16][24]
+  uint4* ext = sm;                                                   // [8][4][256]
+  uint4* phi = sm + 8 * 4 * 256;                                     // [256]
+  uint32_t* xch = reinterpret_cast<uint32_t*>(phi + 256);            // per warp [2][R1_HALF]
   const uint64_t* ext_src = &T->ext[0][0][0];
-  for (int i = threadIdx.x; i < 8 * 256 * 8; i += R1_THREADS) ext[i] = ext_src[i];
+  for (int i = threadIdx.x; i < 8 * 4 * 256; i += R1_THREADS) {
+    const int c = i >> 10, q = (i >> 8) & 3, v = i & 255;
+    const uint64_t* e = ext_src + ((size_t)(c * 256 + v) << 3) + 2 * q;
+    ext[i] = make_uint4((uint32_t)e[0], (uint32_t)(e[0] >> 32), (uint32_t)e[1], (uint32_t)(e[1] >> 32));
+  }
   for (int i = threadIdx.x; i < 256; i += R1_THREADS) phi[i] = reinterpret_cast<const uint4*>(T->phi8)[i];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int xm = lane & 15, half = lane >> 4;
-  uint64_t* my_x = xch + warp * (2 * 16 * 24);
+  uint32_t* my_x = xch + warp * (2 * R1_HALF) + half * R1_HALF;
   gf128 sum_ab[4], sum_c[8];
 #pragma unroll
   for (int q = 0; q < 4; q++) sum_ab[q] = gf_zero();
@@ -121,18 +160,21 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
     if (live) {
       const size_t row0 = xo * 128 + (size_t)xm * 8;
 #pragma unroll 1
-      for (int xs = 0; xs < 8; xs++) {
+      for (int xs2 = 0; xs2 < 4; xs2++)
+#pragma unroll
+      for (int par = 0; par < 2; par++) {
+        const int xs = 2 * xs2 + par;
         uint64_t ra = A[row0 + xs], rb = B[row0 + xs], rc = C[row0 + xs];
         uint64_t ea[8], eb[8];
 #pragma unroll
         for (int j = 0; j < 8; j++) { ea[j] = 0; eb[j] = 0; }
 #pragma unroll
         for (int c = 0; c < 8; c++) {
-          const uint4* pa = reinterpret_cast<const uint4*>(ext + ((c * 256 + ((ra >> (8 * c)) & 255)) << 3));
-          const uint4* pb = reinterpret_cast<const uint4*>(ext + ((c * 256 + ((rb >> (8 * c)) & 255)) << 3));
+          const uint4* pa = ext + c * 1024 + ((ra >> (8 * c)) & 255);
+          const uint4* pb = ext + c * 1024 + ((rb >> (8 * c)) & 255);
 #pragma unroll
           for (int q = 0; q < 4; q++) {
-            uint4 va = pa[q], vb = pb[q];
+            uint4 va = pa[q * 256], vb = pb[q * 256];
             ea[2 * q] ^= ((uint64_t)va.y << 32) | va.x;
             ea[2 * q + 1] ^= ((uint64_t)va.w << 32) | va.z;
             eb[2 * q] ^= ((uint64_t)vb.y << 32) | vb.x;
@@ -146,7 +188,7 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
         // bit j of the constant is set).
         const uint8_t* mm = T->e8_mat[xs];
         const uint8_t e8c = T->e8c[xs >> 1];
-        uint64_t* tt = t + 8 * (xs & 1);
+        uint64_t* tt = t + 8 * par;
 #pragma unroll
         for (int j = 0; j < 8; j++) {
           uint64_t acc = 0;
@@ -158,41 +200,40 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
         }
       }
     }
-    // Exchange the w / t planes of the 16 xm lanes of each half.
+    // Hand the three plane sets to the lanes of this half as bytes: the lane
+    // of point quad xm reads word xm of every (set, producer) row.
     __syncwarp();
-#pragma unroll
-    for (int j = 0; j < 8; j++) my_x[(half * 16 + xm) * 24 + j] = w[j];
-#pragma unroll
-    for (int j = 0; j < 16; j++) my_x[(half * 16 + xm) * 24 + 8 + j] = t[j];
+    planes_to_bytes(w, my_x + (0 * 16 + xm) * R1_ROW);
+    planes_to_bytes(t, my_x + (1 * 16 + xm) * R1_ROW);
+    planes_to_bytes(t + 8, my_x + (2 * 16 + xm) * R1_ROW);
     __syncwarp();
     if (live) {
       // this lane handles points / skip positions 4*xm .. 4*xm+3 of its half
-      // (and both parities t of the c statistic)
-      Acc5 va[4], vc[8];
+      // (and both parities t of the c statistic), one plane set at a time
+      const gf128 e = gf_load(&eq_out[xo]);
+      // one plane set per iteration (not unrolled: the body holds four GF
+      // products, which keeps the loop inside the instruction cache)
+#pragma unroll 1
+      for (int set = 0; set < 3; set++) {
+        Acc5 v[4];
 #pragma unroll
-      for (int q = 0; q < 4; q++)
+        for (int q = 0; q < 4; q++)
 #pragma unroll
-        for (int k = 0; k < 5; k++) va[q].w[k] = 0;
+          for (int k = 0; k < 5; k++) v[q].w[k] = 0;
+#pragma unroll 4
+        for (int mm2 = 0; mm2 < 16; mm2++) {
+          const uint32_t bw = my_x[(set * 16 + mm2) * R1_ROW + xm];
 #pragma unroll
-      for (int q = 0; q < 8; q++)
-#pragma unroll
-        for (int k = 0; k < 5; k++) vc[q].w[k] = 0;
-#pragma unroll 2
-      for (int mm2 = 0; mm2 < 16; mm2++) {
-        const uint64_t* pw = my_x + (half * 16 + mm2) * 24;
+          for (int q = 0; q < 4; q++) acc_shift_xor_v(v[q], phi[(bw >> (8 * q)) & 255], (uint32_t)mm2);
+        }
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-          int i = 4 * xm + q;
-          acc_shift_xor(va[q], phi[byte_from_planes(pw, i)], mm2);
-          acc_shift_xor(vc[q], phi[byte_from_planes(pw + 8, i)], mm2);
-          acc_shift_xor(vc[4 + q], phi[byte_from_planes(pw + 16, i)], mm2);
+          const gf128 p = gf_mul(acc_reduce(v[q]), e);
+          if (set == 0) sum_ab[q] = gf_add(sum_ab[q], p);
+          else if (set == 1) sum_c[q] = gf_add(sum_c[q], p);
+          else sum_c[4 + q] = gf_add(sum_c[4 + q], p);
         }
       }
-      gf128 e = gf_load(&eq_out[xo]);
-#pragma unroll
-      for (int q = 0; q < 4; q++) sum_ab[q] = gf_add(sum_ab[q], gf_mul(acc_reduce(va[q]), e));
-#pragma unroll
-      for (int q = 0; q < 8; q++) sum_c[q] = gf_add(sum_c[q], gf_mul(acc_reduce(vc[q]), e));
     }
     __syncwarp();
   }
@@ -366,7 +407,7 @@ __global__ void bind_pairs_kernel(const gf128* __restrict__ A, const gf128* __re
 
 int flock_launch_zc_round1(const void* a, const void* b, const void* c, size_t n_outer, const void* eq_out,
                            const ZcRound1Tables* d_tables, void* partials, int grid, cudaStream_t st) {
-  size_t smem = 8 * 256 * 8 * 8 + 256 * 16 + (R1_THREADS / 32) * 2 * 16 * 24 * 8;
+  const size_t smem = R1_SMEM;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(zc_round1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
