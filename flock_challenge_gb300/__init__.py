@@ -22,8 +22,9 @@ COMPRESSION_DTYPE = np.dtype([("cv", "<u4", 8), ("m", "<u4", 16), ("counter", "<
 assert COMPRESSION_DTYPE.itemsize == 112
 
 FLOCK_OK = 0
+FLOCK_PENDING = 1
 _ERRORS = {-1: "shape", -2: "cuda", -3: "out of memory", -4: "argument", -5: "capacity",
-           -6: "timeout", -7: "verify"}
+           -6: "timeout", -7: "verify", -8: "limit"}
 
 
 class FlockError(RuntimeError):
@@ -151,6 +152,21 @@ def _proto_lib():
         L.flock_kernel_launches.restype = ctypes.c_uint64
         L.flock_stream.argtypes = [P]
         L.flock_stream.restype = P
+        u64p, szp = ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_size_t)
+        L.flock_footprint_bytes.argtypes = [ctypes.c_uint32]
+        L.flock_footprint_bytes.restype = ctypes.c_size_t
+        L.flock_server_create.argtypes = [ctypes.c_int, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(P)]
+        L.flock_server_destroy.argtypes = [P]
+        L.flock_server_submit_seed.argtypes = [P, ctypes.c_uint32, ctypes.c_uint64, u64p]
+        L.flock_server_submit.argtypes = [P, P, ctypes.c_size_t, u64p]
+        L.flock_server_poll.argtypes = [P, ctypes.c_uint64, P, ctypes.c_size_t, szp]
+        L.flock_server_wait.argtypes = [P, ctypes.c_uint64, P, ctypes.c_size_t, szp]
+        L.flock_server_request_times.argtypes = [P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double),
+                                                 ctypes.POINTER(ctypes.c_double)]
+        L.flock_server_reserved_bytes.argtypes = [P]
+        L.flock_server_reserved_bytes.restype = ctypes.c_size_t
+        L.flock_prove_batch.argtypes = [P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_uint32), u64p, P,
+                                        ctypes.c_size_t, szp]
         L._proto_ready = True
     return L
 
@@ -236,3 +252,100 @@ def generate_inputs(log2_size, seed, device="cuda"):
     out = torch.empty((1 << log2_size) * 112, dtype=torch.uint8, device=device)
     check(_proto_lib().flock_generate_inputs(log2_size, seed, _dptr(out), None), "flock_generate_inputs")
     return out
+
+
+def footprint_bytes(log2_size):
+    """Device bytes one prover holds for a proof of 2^log2_size compressions."""
+    return int(_proto_lib().flock_footprint_bytes(log2_size))
+
+
+class Server:
+    """Proof server with continuous batching (flock_server_*).
+
+    ``Server(device, hbm_budget, workers)``; ``submit_seed(log2, seed)`` or
+    ``submit(blocks)`` return a request id; ``wait(id)`` / ``poll(id)`` return
+    the proof bytes (poll returns None while the request runs). Requests are
+    admitted while the workers' device memory fits ``hbm_budget`` (0 = no
+    limit) and run concurrently on the workers' streams.
+    """
+
+    def __init__(self, device=0, hbm_budget=0, workers=2):
+        self._h = ctypes.c_void_p()
+        check(_proto_lib().flock_server_create(device, hbm_budget, workers, ctypes.byref(self._h)),
+              "flock_server_create")
+        self._buf = np.zeros(1 << 20, np.uint8)
+
+    def close(self):
+        if self._h:
+            _proto_lib().flock_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def submit_seed(self, log2_size, seed):
+        rid = ctypes.c_uint64()
+        check(_proto_lib().flock_server_submit_seed(self._h, log2_size, seed, ctypes.byref(rid)),
+              "flock_server_submit_seed")
+        return rid.value
+
+    def submit(self, blocks):
+        blocks = np.ascontiguousarray(blocks, dtype=COMPRESSION_DTYPE)
+        rid = ctypes.c_uint64()
+        check(_proto_lib().flock_server_submit(self._h, blocks.ctypes.data_as(ctypes.c_void_p), len(blocks),
+                                               ctypes.byref(rid)), "flock_server_submit")
+        return rid.value
+
+    def _collect(self, fn, rid):
+        ln = ctypes.c_size_t()
+        rc = fn(self._h, rid, self._buf.ctypes.data_as(ctypes.c_void_p), self._buf.size, ctypes.byref(ln))
+        if rc == -5:
+            self._buf = np.zeros(ln.value, np.uint8)
+            rc = fn(self._h, rid, self._buf.ctypes.data_as(ctypes.c_void_p), self._buf.size, ctypes.byref(ln))
+        if rc == FLOCK_PENDING:
+            return None
+        check(rc, fn.__name__)
+        return self._buf[:ln.value].tobytes()
+
+    def poll(self, rid):
+        return self._collect(_proto_lib().flock_server_poll, rid)
+
+    def wait(self, rid):
+        return self._collect(_proto_lib().flock_server_wait, rid)
+
+    def times(self, rid):
+        """(queue_ms, run_ms) of a finished request, before it is collected."""
+        q, r = ctypes.c_double(), ctypes.c_double()
+        rc = _proto_lib().flock_server_request_times(self._h, rid, ctypes.byref(q), ctypes.byref(r))
+        if rc == FLOCK_PENDING:
+            return None
+        check(rc, "flock_server_request_times")
+        return q.value, r.value
+
+    def reserved_bytes(self):
+        return int(_proto_lib().flock_server_reserved_bytes(self._h))
+
+    def prove_batch(self, log2_sizes, seeds):
+        """Batched form: one proof per (log2_size, seed), as flock_prove_seed would make it."""
+        n = len(log2_sizes)
+        sizes = (ctypes.c_uint32 * n)(*log2_sizes)
+        sds = (ctypes.c_uint64 * n)(*seeds)
+        lens = (ctypes.c_size_t * n)()
+        cap = n * 600000
+        out = np.zeros(cap, np.uint8)
+        check(_proto_lib().flock_prove_batch(self._h, n, sizes, sds, out.ctypes.data_as(ctypes.c_void_p), cap, lens),
+              "flock_prove_batch")
+        proofs, off = [], 0
+        for i in range(n):
+            proofs.append(out[off:off + lens[i]].tobytes())
+            off += lens[i]
+        return proofs

@@ -8,9 +8,21 @@
 #include "r1cs_setup.h"
 
 #include <atomic>
+#include <mutex>
+#include <set>
 
 static std::atomic<unsigned long long> g_launches{0};
 void flock_count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+void flock_once_per_device(const void* key, void (*fn)()) {
+  static std::mutex mu;
+  static std::set<std::pair<int, const void*>> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  // run under the lock: no thread launches the kernel before the work is done
+  if (done.insert({dev, key}).second) fn();
+}
 
 struct flock_ctx {
   int device = 0;
@@ -105,6 +117,7 @@ static int prove_impl(flock_ctx* ctx, const flock_compression* in, size_t n, uin
   size_t nn = n < 8 ? 8 : n;
   int n_log = 0;
   while (((size_t)1 << n_log) < nn) n_log++;
+  if (ctx->hbm_budget && flock_footprint_bytes((uint32_t)n_log) > ctx->hbm_budget) return FLOCK_ERR_OOM;
   if (!ctx->prover) {
     ctx->prover = flock_prover_create(ctx->device);
     if (!ctx->prover) return FLOCK_ERR_CUDA;
@@ -134,6 +147,7 @@ int flock_generate_inputs(uint32_t log2_size, uint64_t seed, void* d_out, void* 
 
 int flock_prove_seed(flock_ctx* ctx, uint32_t log2_size, uint64_t seed, uint8_t* out, size_t cap, size_t* len) {
   if (!ctx || !len || log2_size < 8 || log2_size > 21) return FLOCK_ERR_ARG;
+  if (ctx->hbm_budget && flock_footprint_bytes(log2_size) > ctx->hbm_budget) return FLOCK_ERR_OOM;
   if (!ctx->prover) {
     ctx->prover = flock_prover_create(ctx->device);
     if (!ctx->prover) return FLOCK_ERR_CUDA;

@@ -69,6 +69,10 @@ int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, cudaSt
 
 // Launch counter of this library's kernels (read through flock_kernel_launches).
 void flock_count_launch();
+// Runs fn once per (current device, key), under a lock, so no thread passes
+// before the first caller's fn has finished: per-device one-time work such as
+// raising a kernel's shared-memory limit.
+void flock_once_per_device(const void* key, void (*fn)());
 
 // Benchmark inputs (inputs.cu): n records from SplitMix64 state `state0`.
 int flock_launch_gen_inputs(uint64_t state0, size_t n, void* d_out, cudaStream_t st);

@@ -199,14 +199,14 @@ int launch_pass(gf128* dst, const gf128* src, size_t mask, const gf128* tw, int 
 }
 
 // Raises the dynamic shared-memory limit of the passes that need more than
-// the default 48 KB (F = 8 with 16 lanes: 64 KB), once per process.
+// the default 48 KB (8 layers with 16 lanes: 64 KB), once per device.
 void ntt_set_smem_attrs() {
-  static std::once_flag once;
-  std::call_once(once, [] {
-    if constexpr (kMaxPassLayers >= 8)
+  if constexpr (kMaxPassLayers >= 8) {
+    flock_once_per_device((const void*)ntt_pass_kernel<kMaxPassLayers, 16>, [] {
       cudaFuncSetAttribute(ntt_pass_kernel<kMaxPassLayers, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            PassShape<kMaxPassLayers, 16>::SMEM);
-  });
+    });
+  }
 }
 
 int run_pass(int f, gf128* dst, const gf128* src, size_t mask, const gf128* tw, int log_d, int log_lanes, int l0,

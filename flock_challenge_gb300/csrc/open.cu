@@ -121,11 +121,9 @@ int flock_s_hat_v_warps(int grid) { return grid * (SH_THREADS / 32); }
 int flock_launch_combined_basis(size_t n, const void* t0_lo, const void* t0_hi, const void* t1_lo, const void* t1_hi,
                                 int lo_bits, const void* tables, void* b, cudaStream_t st) {
   size_t smem = 2 * 16 * 256 * 16;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(combined_basis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
-  }
+  flock_once_per_device((const void*)combined_basis_kernel, [] {
+    cudaFuncSetAttribute(combined_basis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(2 * 16 * 256 * 16));
+  });
   size_t grid = (n + CB_THREADS - 1) / CB_THREADS;
   if (grid > 152 * 2) grid = 152 * 2;
   combined_basis_kernel<<<(unsigned)grid, CB_THREADS, smem, st>>>(

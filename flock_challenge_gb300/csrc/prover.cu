@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <mutex>
 #include <set>
 #include <stdexcept>
 #include <string>
@@ -76,8 +77,11 @@ struct DBuf {
   size_t bytes = 0;
   DBuf() = default;
   DBuf(const DBuf&) = delete;
-  ~DBuf() {
+  ~DBuf() { release(); }
+  void release() {
     if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
   }
   void* get(size_t b) {
     if (b > bytes) {
@@ -184,6 +188,8 @@ struct Sks {
 const Sks& sks_for(int n) {
   static std::vector<Sks> cache(64);
   static std::vector<bool> have(64, false);
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lk(mu);
   if (!have[n]) {
     Sks r;
     r.s.assign(n + 1, F());
@@ -279,14 +285,51 @@ struct ProverState {
   DBuf csc_ap, csc_ai, csc_bp, csc_bi;
   bool csc_ready = false;
   FlockPhaseTimes times;
+  // Pinned host staging: small host->device copies are bump-allocated in
+  // [0, kPinH2D) for the duration of one proof (pinned sources keep the
+  // copies asynchronous); device->host reads go through the last kPinD2H bytes.
+  uint8_t* pin = nullptr;
+  size_t pin_off = 0;
+
+  std::vector<DBuf*> bufs() {
+    return {&in, &z, &a, &b, &stripe, &cw, &tree, &A0, &B0, &A1, &B1, &eqlo, &eqhi, &eqout, &rdev, &part, &red,
+            &lag, &small, &eqin, &comb, &zvec, &zvec0, &lcmsg, &tlo0, &thi0, &tlo1, &thi1, &tables, &bc, &f1, &b1,
+            &W, &LO, &HI, &basis, &qbuf, &abuf, &rows, &nidx, &nodes, &grind, &lvl_cw[0], &lvl_cw[1],
+            &lvl_tree[0], &lvl_tree[1], &csc_ap, &csc_ai, &csc_bp, &csc_bi};
+  }
+  std::vector<const DBuf*> bufs() const {
+    auto v = const_cast<ProverState*>(this)->bufs();
+    return std::vector<const DBuf*>(v.begin(), v.end());
+  }
 };
 
 namespace {
 
-void h2d(void* d, const void* h, size_t n, cudaStream_t st) { CK(cudaMemcpyAsync(d, h, n, cudaMemcpyHostToDevice, st)); }
-void d2h(void* h, const void* d, size_t n, cudaStream_t st) {
-  CK(cudaMemcpyAsync(h, d, n, cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
+constexpr size_t kPinH2D = (size_t)4 << 20, kPinD2H = (size_t)1 << 20;
+
+void h2d(ProverState& S, void* d, const void* h, size_t n) {
+  if (n == 0) return;
+  const size_t need = (n + 255) & ~(size_t)255;
+  if (S.pin && S.pin_off + need <= kPinH2D) {
+    uint8_t* p = S.pin + S.pin_off;
+    S.pin_off += need;
+    std::memcpy(p, h, n);
+    CK(cudaMemcpyAsync(d, p, n, cudaMemcpyHostToDevice, S.st));
+  } else {
+    CK(cudaMemcpyAsync(d, h, n, cudaMemcpyHostToDevice, S.st));
+  }
+}
+void d2h(ProverState& S, void* h, const void* d, size_t n) {
+  if (n == 0) return;
+  if (S.pin && n <= kPinD2H) {
+    uint8_t* p = S.pin + kPinH2D;
+    CK(cudaMemcpyAsync(p, d, n, cudaMemcpyDeviceToHost, S.st));
+    CK(cudaStreamSynchronize(S.st));
+    std::memcpy(h, p, n);
+  } else {
+    CK(cudaMemcpyAsync(h, d, n, cudaMemcpyDeviceToHost, S.st));
+    CK(cudaStreamSynchronize(S.st));
+  }
 }
 void u2(const F& x, uint64_t out[2]) { out[0] = x.lo; out[1] = x.hi; }
 
@@ -307,7 +350,7 @@ void ligero_commit(ProverState& S, const void* poly, int lmc, int lni, int rate,
   FK(flock_launch_ntt(cw, poly, log_d, lni, rate, S.st));
   size_t leaves = (size_t)1 << log_d;
   FK(flock_launch_merkle(cw, leaves, (size_t)16 << lni, tree, S.st));
-  d2h(root, (const uint8_t*)tree + (2 * leaves - 2) * 32, 32, S.st);
+  d2h(S, root, (const uint8_t*)tree + (2 * leaves - 2) * 32, 32);
 }
 
 Open open_rows(ProverState& S, const void* cw, const void* tree, size_t block_len, int width,
@@ -315,19 +358,19 @@ Open open_rows(ProverState& S, const void* cw, const void* tree, size_t block_le
   Open o;
   o.width = width;
   uint32_t* dq = (uint32_t*)S.qbuf.get(q.size() * 4);
-  h2d(dq, q.data(), q.size() * 4, S.st);
+  h2d(S, dq, q.data(), q.size() * 4);
   void* dr = S.rows.get(q.size() * width * 16);
   FK(flock_launch_gather_rows(cw, dq, (int)q.size(), width, dr, S.st));
   o.rows.resize(q.size() * width);
-  d2h(o.rows.data(), dr, o.rows.size() * 16, S.st);
+  d2h(S, o.rows.data(), dr, o.rows.size() * 16);
   auto idx = multiproof_nodes(block_len, q);
   o.nodes.resize(idx.size() * 32);
   if (!idx.empty()) {
     uint32_t* di = (uint32_t*)S.nidx.get(idx.size() * 4);
-    h2d(di, idx.data(), idx.size() * 4, S.st);
+    h2d(S, di, idx.data(), idx.size() * 4);
     void* dn = S.nodes.get(idx.size() * 32);
     FK(flock_launch_gather_nodes(tree, di, (int)idx.size(), dn, S.st));
-    d2h(o.nodes.data(), dn, o.nodes.size(), S.st);
+    d2h(S, o.nodes.data(), dn, o.nodes.size());
   }
   return o;
 }
@@ -345,14 +388,14 @@ std::vector<F> reduce_partials(ProverState& S, const void* part, size_t count, i
   void* r = S.red.get((size_t)width * 16);
   FK(flock_launch_reduce_rows(part, count, width, r, S.st));
   std::vector<F> out(width);
-  d2h(out.data(), r, (size_t)width * 16, S.st);
+  d2h(S, out.data(), r, (size_t)width * 16);
   return out;
 }
 
 void eq_split_dev(ProverState& S, const std::vector<F>& r, int lo_bits, DBuf& lo, DBuf& hi) {
   int hi_bits = (int)r.size() - lo_bits;
   void* dr = S.rdev.get(r.size() * 16 + 16);
-  h2d(dr, r.data(), r.size() * 16, S.st);
+  h2d(S, dr, r.data(), r.size() * 16);
   FK(flock_launch_eq_split(dr, lo_bits, hi_bits, lo.get((size_t)16 << lo_bits), hi.get((size_t)16 << hi_bits), S.st));
 }
 
@@ -365,6 +408,10 @@ ProverState* flock_prover_create(int device) {
     delete S;
     return nullptr;
   }
+  // Without pinned staging the copies still work, through the driver's own.
+  void* pin = nullptr;
+  if (cudaMallocHost(&pin, kPinH2D + kPinD2H) == cudaSuccess) S->pin = (uint8_t*)pin;
+  else cudaGetLastError();
   return S;
 }
 
@@ -373,7 +420,21 @@ void flock_prover_destroy(ProverState* S) {
   cudaSetDevice(S->device);
   if (S->d_r1t) cudaFree(S->d_r1t);
   if (S->st) cudaStreamDestroy(S->st);
+  if (S->pin) cudaFreeHost(S->pin);
   delete S;
+}
+
+size_t flock_prover_reserved_bytes(const ProverState* S) {
+  size_t t = S->d_r1t ? sizeof(ZcRound1Tables) : 0;
+  for (const DBuf* b : S->bufs()) t += b->bytes;
+  return t;
+}
+
+void flock_prover_trim(ProverState* S) {
+  cudaSetDevice(S->device);
+  cudaStreamSynchronize(S->st);
+  for (DBuf* b : S->bufs()) b->release();
+  S->csc_ready = false;
 }
 
 const FlockPhaseTimes& flock_prover_times(const ProverState* S) { return S->times; }
@@ -398,6 +459,8 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
                        bool input_on_device) {
   try {
     CK(cudaSetDevice(S->device));
+    CK(cudaStreamSynchronize(S->st));  // the staging area of the previous proof is free again
+    S->pin_off = 0;
     const int m = 14 + n_log;
     LigCfg cfg;
     if (!lig_config(m, 0, cfg)) return FLOCK_ERR_SHAPE;
@@ -418,10 +481,10 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     }
     if (!S->csc_ready) {
       const HostCsc& c = flock_host_csc();
-      h2d(S->csc_ap.get(c.a_ptr.size() * 4), c.a_ptr.data(), c.a_ptr.size() * 4, st);
-      h2d(S->csc_ai.get(c.a_idx.size() * 4), c.a_idx.data(), c.a_idx.size() * 4, st);
-      h2d(S->csc_bp.get(c.b_ptr.size() * 4), c.b_ptr.data(), c.b_ptr.size() * 4, st);
-      h2d(S->csc_bi.get(c.b_idx.size() * 4), c.b_idx.data(), c.b_idx.size() * 4, st);
+      h2d(*S, S->csc_ap.get(c.a_ptr.size() * 4), c.a_ptr.data(), c.a_ptr.size() * 4);
+      h2d(*S, S->csc_ai.get(c.a_idx.size() * 4), c.a_idx.data(), c.a_idx.size() * 4);
+      h2d(*S, S->csc_bp.get(c.b_ptr.size() * 4), c.b_ptr.data(), c.b_ptr.size() * 4);
+      h2d(*S, S->csc_bi.get(c.b_idx.size() * 4), c.b_idx.data(), c.b_idx.size() * 4);
       CK(cudaStreamSynchronize(st));
       S->csc_ready = true;
     }
@@ -433,7 +496,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     const void* d_in = h_in;
     if (!input_on_device) {
       void* buf = S->in.get(std::max<size_t>(n, 1) * sizeof(flock_compression));
-      if (n) h2d(buf, h_in, n * sizeof(flock_compression), st);
+      if (n) h2d(*S, buf, h_in, n * sizeof(flock_compression));
       d_in = buf;
     }
     void *dz = S->z.get(nbytes), *da = S->a.get(nbytes), *db = S->b.get(nbytes), *ds = S->stripe.get(nbytes);
@@ -446,7 +509,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     FK(flock_launch_ntt(dcw, dz, log_d0, lbs, rate0, st));
     FK(flock_launch_merkle(dcw, block0, (size_t)16 << lbs, dtree, st));
     uint8_t root0[32];
-    d2h(root0, (const uint8_t*)dtree + (2 * block0 - 2) * 32, 32, st);
+    d2h(*S, root0, (const uint8_t*)dtree + (2 * block0 - 2) * 32, 32);
     T.commit_ms = clk.lap();
 
     Wire w;
@@ -486,7 +549,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       std::vector<F> rout(r.begin() + 13, r.end());
       int nv = (int)rout.size();
       void* dr = S->rdev.get(rout.size() * 16 + 16);
-      h2d(dr, rout.data(), rout.size() * 16, st);
+      h2d(*S, dr, rout.data(), rout.size() * 16);
       void* deq = S->eqout.get(n_outer * 16);
       FK(flock_launch_eq_split(dr, nv, 0, deq, S->eqhi.get(16), st));
       const int grid = 152;
@@ -519,7 +582,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     void *dA0 = S->A0.get(rows0 * 16), *dB0 = S->B0.get(rows0 * 16);
     void *dA1 = S->A1.get(rows0 / 2 * 16), *dB1 = S->B1.get(rows0 / 2 * 16);
     void* dlag = S->lag.get(64 * 16);
-    h2d(dlag, lag_z.data(), 64 * 16, st);
+    h2d(*S, dlag, lag_z.data(), 64 * 16);
     FK(flock_launch_fold_skip(da, db, rows0, dlag, dA0, dB0, st));
     const int n_mlv = m - 6;
     std::vector<std::pair<F, F>> zc_rounds;
@@ -552,8 +615,8 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       uint64_t rp[2];
       u2(rho.back(), rp);
       FK(flock_launch_bind_pairs(curA, curB, 1, rp, nxtA, nxtB, st));
-      d2h(&fa, nxtA, 16, st);
-      d2h(&fb, nxtB, 16, st);
+      d2h(*S, &fa, nxtA, 16);
+      d2h(*S, &fb, nxtB, 16);
     }
     tr.observe(fa);
     tr.observe(fb);
@@ -576,7 +639,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     std::vector<F> z_partial(64);
     {
       void* dxr = S->small.get(inner_rest * 16);
-      h2d(dxr, x_in.data(), inner_rest * 16, st);
+      h2d(*S, dxr, x_in.data(), inner_rest * 16);
       void* deqin = S->eqin.get(FLOCK_K * 16);
       FK(flock_launch_lc_quirky_eq(dlag, dxr, inner_rest, deqin, st));
       void* dcomb = S->comb.get(FLOCK_K * 16);
@@ -602,7 +665,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
         if (t > 0) len /= 2;
         FK(flock_launch_lc_round(dcomb, dzv, len, t > 0, rp, 1, dmsg, st));
         F msg[2];
-        d2h(msg, dmsg, 32, st);
+        d2h(*S, msg, dmsg, 32);
         tr.observe(msg[0]);
         tr.observe(msg[1]);
         lc_rounds.push_back({msg[0], msg[1]});
@@ -611,7 +674,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       uint64_t rp[2];
       u2(lc_rr.back(), rp);
       FK(flock_launch_lc_round(dcomb, dzv, len / 2, 1, rp, 0, dmsg, st));
-      d2h(z_partial.data(), dzv, 64 * 16, st);
+      d2h(*S, z_partial.data(), dzv, 64 * 16);
     }
     tr.observe_slice(z_partial.data(), 64);
     F r_inner_skip = tr.sample();
@@ -643,11 +706,11 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       std::vector<F> tail(r_inner_rest.begin() + 1, r_inner_rest.end());
       auto eq_tail = eq_table(tail);
       void* det = S->small.get(128 * 16);
-      h2d(det, eq_tail.data(), 128 * 16, st);
+      h2d(*S, det, eq_tail.data(), 128 * 16);
       void* dsh = S->red.get(128 * 16);
       FK(flock_launch_shv_from_zvec(S->zvec0.p, det, dsh, st));
       s_hat[0].resize(128);
-      d2h(s_hat[0].data(), dsh, 128 * 16, st);
+      d2h(*S, s_hat[0].data(), dsh, 128 * 16);
       s_hat[1] = shv_c;
     }
     for (int k = 0; k < 2; k++) {
@@ -676,7 +739,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
         }
       }
       void* dt = S->tables.get(tabs.size() * 16);
-      h2d(dt, tabs.data(), tabs.size() * 16, st);
+      h2d(*S, dt, tabs.data(), tabs.size() * 16);
       FK(flock_launch_combined_basis(n128, S->tlo0.p, S->thi0.p, S->tlo1.p, S->thi1.p, rs_lo, dt, dbc, st));
     }
     T.ring_switch_ms = clk.lap();
@@ -768,12 +831,12 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       auto aw = eq_table(alpha_v);
       aw.resize(q.size());
       void* dsk = S->small.get((size_t)(2 * (nvars + 1)) * 16);
-      h2d(dsk, sk.s.data(), (nvars + 1) * 16, st);
-      h2d((char*)dsk + (nvars + 1) * 16, sk.inv.data(), (nvars + 1) * 16, st);
+      h2d(*S, dsk, sk.s.data(), (nvars + 1) * 16);
+      h2d(*S, (char*)dsk + (nvars + 1) * 16, sk.inv.data(), (nvars + 1) * 16);
       uint32_t* dq = (uint32_t*)S->qbuf.get(q.size() * 4);
-      h2d(dq, q.data(), q.size() * 4, st);
+      h2d(*S, dq, q.data(), q.size() * 4);
       void* dal = S->abuf.get(q.size() * 16);
-      h2d(dal, aw.data(), q.size() * 16, st);
+      h2d(*S, dal, aw.data(), q.size() * 16);
       int lo_bits = (nvars + 1) / 2, hi_bits = nvars - lo_bits;
       void* dW = S->W.get(q.size() * nvars * 16);
       void* dLO = S->LO.get((q.size() << lo_bits) * 16);
@@ -826,7 +889,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       }
       if (i == cfg.steps - 1) {
         yr.resize(len);
-        d2h(yr.data(), fcur, len * 16, st);
+        d2h(*S, yr.data(), fcur, len * 16);
         for (auto& v : yr) tr.observe(v);
         grind_nonces.push_back(grind((uint32_t)cfg.grind_bits[i + 1]));
         auto ql = sample_queries(tr, prev_block, cfg.queries[i + 1]);

@@ -24,3 +24,8 @@ cudaStream_t flock_prover_stream(const ProverState* s);
 // Generates the 2^log2 benchmark inputs of `seed` on the device, then proves them.
 int flock_prover_prove_seed(ProverState* s, int log2, uint64_t seed, std::vector<uint8_t>& out);
 const FlockPhaseTimes& flock_prover_times(const ProverState* s);
+// Device bytes the state holds (its buffers grow to the largest proof seen).
+size_t flock_prover_reserved_bytes(const ProverState* s);
+// Frees the state's device buffers (after its stream is idle); the next proof
+// allocates them again.
+void flock_prover_trim(ProverState* s);

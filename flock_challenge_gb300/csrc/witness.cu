@@ -239,11 +239,9 @@ int flock_launch_witness(const flock_compression* d_in, size_t n_in, int n_block
   const int threads = 32 * WARPS_PER_BLOCK;
   size_t blocks = (n_total + threads - 1) / threads;
   size_t smem = (size_t)WARPS_PER_BLOCK * 3 * 32 * STAGE_STRIDE * sizeof(uint64_t);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(witness_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
-  }
+  flock_once_per_device((const void*)witness_kernel, [] {
+    cudaFuncSetAttribute(witness_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(WARPS_PER_BLOCK * 3 * 32 * STAGE_STRIDE * sizeof(uint64_t)));
+  });
   witness_kernel<<<(unsigned)blocks, threads, smem, stream>>>(d_in, n_in, n_total, (uint64_t*)d_z,
                                                               (uint64_t*)d_a, (uint64_t*)d_b, (uint8_t*)d_stripe); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;

@@ -408,11 +408,9 @@ __global__ void bind_pairs_kernel(const gf128* __restrict__ A, const gf128* __re
 int flock_launch_zc_round1(const void* a, const void* b, const void* c, size_t n_outer, const void* eq_out,
                            const ZcRound1Tables* d_tables, void* partials, int grid, cudaStream_t st) {
   const size_t smem = R1_SMEM;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(zc_round1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
-  }
+  flock_once_per_device((const void*)zc_round1_kernel, [] {
+    cudaFuncSetAttribute(zc_round1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)R1_SMEM);
+  });
   zc_round1_kernel<<<grid, R1_THREADS, smem, st>>>((const uint64_t*)a, (const uint64_t*)b, (const uint64_t*)c,
                                                    n_outer, (const gf128*)eq_out, d_tables, (gf128*)partials); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;

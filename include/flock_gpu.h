@@ -20,6 +20,7 @@ extern "C" {
 #endif
 
 enum {
+  FLOCK_PENDING = 1,      /* a served request is not finished yet (not an error) */
   FLOCK_OK = 0,
   FLOCK_ERR_SHAPE = -1,   /* size / shape outside the supported range */
   FLOCK_ERR_CUDA = -2,    /* a CUDA call failed */
@@ -53,7 +54,8 @@ const char* flock_version(void);
 uint64_t flock_kernel_launches(void);
 
 /* Create / destroy a device context bound to `device`. `hbm_budget` bounds the
- * device memory the context may hold (0 = no limit).
+ * device memory the context may hold (0 = no limit): a proof whose
+ * flock_footprint_bytes exceeds it returns FLOCK_ERR_OOM.
  * Replaces the process-level setup of the reference worker
  * (benchmark-tools/worker/src/main.rs:45-57) and the Metal context of
  * crates/flock-core/src/gpu_commit.rs:1454-1478. */
@@ -150,6 +152,50 @@ void* flock_stream(flock_ctx* ctx);
  * serialization (first n entries). No reference counterpart (the reference's
  * FLOCK_PHASE_TIMING prints, crates/flock-prover/src/prover.rs:958-1216). */
 int flock_last_phase_times(const flock_ctx* ctx, double* ms, int n);
+
+/* ---- Batched and served proving ---------------------------------------- */
+
+/* Device bytes one prover holds for a proof of 2^log2_size compressions (the
+ * admission estimate of the server and of hbm_budget). No reference
+ * counterpart. */
+size_t flock_footprint_bytes(uint32_t log2_size);
+
+typedef struct flock_server flock_server;
+
+/* A proof server on `device` with n_workers concurrent provers (each its own
+ * CUDA stream and resident buffers). Requests are admitted, in arrival order
+ * where they fit, while the workers' device memory stays within hbm_budget
+ * (0 = no limit); requests that arrive while others run start as soon as a
+ * worker and memory are free, so their kernels overlap on the device.
+ * Replaces the reference's worker-per-proof serving loop
+ * (benchmark-tools/worker/src/main.rs:45-90) with continuous batching on one
+ * GPU. */
+int flock_server_create(int device, size_t hbm_budget, int n_workers, flock_server** out);
+/* Finishes the queued requests, then stops the workers and frees the device. */
+void flock_server_destroy(flock_server* s);
+/* Queue a proof of the 2^log2_size benchmark inputs of `seed` (8..21), as
+ * flock_prove_seed; *id identifies the request. FLOCK_ERR_OOM when the proof
+ * alone exceeds the budget. */
+int flock_server_submit_seed(flock_server* s, uint32_t log2_size, uint64_t seed, uint64_t* id);
+/* Queue a proof of n host compressions (copied), as flock_prove. */
+int flock_server_submit(flock_server* s, const flock_compression* in, size_t n, uint64_t* id);
+/* FLOCK_PENDING while running; else the request's status, with the proof
+ * copied to out (FLOCK_ERR_CAPACITY, *len set, keeps the proof for a retry).
+ * A collected request is forgotten. */
+int flock_server_poll(flock_server* s, uint64_t id, uint8_t* out, size_t cap, size_t* len);
+/* As flock_server_poll, blocking until the request is finished. */
+int flock_server_wait(flock_server* s, uint64_t id, uint8_t* out, size_t cap, size_t* len);
+/* Queue and run times (ms) of a finished, not yet collected request. */
+int flock_server_request_times(flock_server* s, uint64_t id, double* queue_ms, double* run_ms);
+/* Device bytes the server's workers hold or have reserved. */
+size_t flock_server_reserved_bytes(flock_server* s);
+/* Batched form: proofs of count (size, seed) pairs through the server's
+ * workers (largest first), written to out back to back in input order with
+ * lens[i] their sizes. Each proof equals flock_prove_seed's for that pair.
+ * No single reference counterpart (the reference proves one bundle per
+ * worker run). */
+int flock_prove_batch(flock_server* s, size_t count, const uint32_t* log2_sizes, const uint64_t* seeds, uint8_t* out,
+                      size_t cap, size_t* lens);
 
 #ifdef __cplusplus
 }

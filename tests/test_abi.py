@@ -38,3 +38,9 @@ def test_create_without_gpu_reports_error():
         return
     h = ctypes.c_void_p()
     assert F.lib().flock_create(0, 0, ctypes.byref(h)) != 0
+
+
+def test_footprint_estimate_is_monotone():
+    fp = [F.footprint_bytes(l) for l in range(8, 22)]
+    assert all(b > a for a, b in zip(fp, fp[1:]))
+    assert 7 << 30 < F.footprint_bytes(18) < 9 << 30
