@@ -1,22 +1,27 @@
 """Benchmark: verified BLAKE3 compressions/s at 2^18 per proof on one GB300.
 
-python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--log2 L]
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--log2 L] [--no-forms]
 
 Workload (the ranked configuration): one proof of 2^18 BLAKE3 compressions
 per step, inputs drawn by the reference generator
-(benchmark-tools/common/src/lib.rs:20-33) from a per-step 64-bit seed. A step
-is the whole prover: witness, PCS commit, zerocheck, lincheck, ring switch,
-Ligerito opening and serialization of the proof bundle. The score of the
-reference is 2^18 / median proof time (README.md:14-25); here every step's
-proof is also checked: its length and digest are compared with the
-deterministic re-proof, and the first proof is accepted by the CPU verifier.
+(benchmark-tools/common/src/lib.rs:20-33, run on the device) from a per-step
+64-bit seed. A step is the whole prover: witness, PCS commit, zerocheck,
+lincheck, ring switch, Ligerito opening and serialization of the proof
+bundle. The score of the reference is 2^18 / median proof time
+(README.md:14-25); here every timed proof is also checked against the
+deterministic re-proof of its inputs (length and bytes), and one GPU proof is
+accepted by the CPU verifier in the cpu_baseline leg.
 
 value: device-timed (CUDA events on the prover's stream) with the inputs
   already resident in HBM (flock_prove_device).
-e2e:   the public C ABI with host buffers (flock_prove): the 28 MB input copy
-  host->device and the proof bytes device->host are inside the timer.
+e2e:   the public C ABI with pinned host buffers (flock_prove): the 28 MB
+  input copy host->device and the proof bytes device->host are inside the
+  timer.
 Working set > 5 GB (1 GiB codeword, 0.5 GiB witness planes) >> 129 MB L2, so no
 explicit L2 flush is needed between steps.
+forms: the batched form (64 proofs of 2^12..2^18 through the proof server vs
+  the same proofs in sequence) and the served form (Poisson arrivals of
+  2^10..2^20 proofs, p50/p99 latency); see flock_challenge_gb300/forms.py.
 
 --impl reference times the CPU oracle (a C++ restatement of the reference
 prover path; the reference's Rust cannot be built here) on all host cores, on
@@ -38,6 +43,11 @@ sys.path.insert(0, ROOT)
 
 METRIC = "verified BLAKE3 compressions/s at 2^18 per proof"
 PUBLISHED = 483866.0  # README.md:110-116, unmodified reference, Apple M4 Pro runner
+
+# dram__bytes_read.sum + dram__bytes_write.sum of the L0 commit NTT passes per
+# launch set, from ncu on a 2^18-position case scaled by positions (traffic
+# grows in proportion): profiles/ntt_pass_l0_2e16.md.
+NTT_TRAFFIC_PER_SET = {20: 7.75e9}
 
 
 def load_peaks():
@@ -102,11 +112,21 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
-def oracle_baseline(budget_s=20.0, log2=14):
-    """CPU oracle proofs of 2^log2 compressions on all host cores (bounded sample)."""
+def oracle_baseline(budget_s=20.0, log2=14, gpu_proof=None, gpu_m=None):
+    """CPU oracle proofs of 2^log2 compressions on all host cores (bounded sample).
+
+    This leg is the only part of the benchmark that runs the oracle: it times
+    the oracle prover and, as the checker, runs the oracle verifier on one
+    proof made by the GPU arm."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib as O
     cores = os.cpu_count() or 1
+    checked = None
+    if gpu_proof is not None:
+        ok, why = O.verify(gpu_proof, gpu_m)
+        if not ok:
+            raise SystemExit(f"GPU proof rejected by the CPU verifier: {why}")
+        checked = f"GPU proof of m={gpu_m} ({len(gpu_proof)} bytes) accepted by the CPU verifier"
     blocks = O.compressions(log2, 0)
     O.prove(O.compressions(8, 0), 8)  # warm the setup caches (digests) outside the timer
     t_setup = time.perf_counter()
@@ -119,9 +139,12 @@ def oracle_baseline(budget_s=20.0, log2=14):
         O.prove(O.compressions(log2, len(times) + 1), log2)
         times.append(time.perf_counter() - t)
     med = sorted(times)[len(times) // 2]
-    return {"value": (1 << log2) / med, "unit": "compressions/s", "cores": cores, "kind": "port",
-            "sample": f"{len(times)} full oracle proofs of 2^{log2} compressions (m={14 + log2}), "
-                      f"median {med:.2f} s, OpenMP on {cores} host threads"}
+    out = {"value": (1 << log2) / med, "unit": "compressions/s", "cores": cores, "kind": "port",
+           "sample": f"{len(times)} full oracle proofs of 2^{log2} compressions (m={14 + log2}), "
+                     f"median {med:.2f} s, OpenMP on {cores} host threads"}
+    if checked:
+        out["gpu_proof_check"] = checked
+    return out
 
 
 def run_reference(args):
@@ -145,10 +168,7 @@ def kernel_roofline(F, ctx_handle, stream_ptr, log2, peaks, torch, dev):
     m = 14 + log2
     log_d = m - 7 - 6 + 1
     n = 1 << log2
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import oracle_lib as O
-    blocks = O.compressions(log2, 99)
-    d_in = torch.from_numpy(blocks.view("uint8").copy()).to(dev)
+    d_in = F.generate_inputs(log2, 99, device=dev)
     z, _, _, _ = F.generate_witness(d_in, n, log2, want_ab=False, want_stripe=False)
     cw = torch.empty((1 << (log_d + 6)) * 16, dtype=torch.uint8, device=dev)
     torch.cuda.synchronize()
@@ -166,13 +186,18 @@ def kernel_roofline(F, ctx_handle, stream_ptr, log2, peaks, torch, dev):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
     passes = (log_d - 1 + 5) // 6
-    # algorithmic bytes: each pass reads and writes the 2^log_d x 64 x 16 B codeword
-    alg = 2 * passes * (1 << (log_d + 6)) * 16
+    # algorithmic bytes: the first pass reads the 2^(log_d-1) x 64 x 16 B message,
+    # every pass writes the 2^log_d x 64 x 16 B codeword, later passes read it
+    cw = (1 << (log_d + 6)) * 16
+    alg = cw // 2 + cw + (passes - 1) * 2 * cw
     achieved = alg / (ms * 1e-3) / 1e9
     muls = (log_d - 1) * (1 << (log_d - 1)) * 64
-    return {"kernel": "ntt_pass_kernel (L0 commit, layers 1..19, 4 passes)", "bound": "hbm",
+    return {"kernel": f"ntt_pass_kernel (L0 commit, layers 1..{log_d - 1}, {passes} passes)", "bound": "hbm",
             "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-            "traffic": None, "ms_per_launch_set": ms, "gf128_muls_per_s": muls / (ms * 1e-3)}
+            "traffic": NTT_TRAFFIC_PER_SET.get(log_d), "algorithmic_bytes_per_set": alg,
+            "ms_per_launch_set": ms, "gf128_muls_per_s": muls / (ms * 1e-3),
+            "note": "the passes are bound by the GF(2^128) multiply issue rate, not HBM: "
+                    "see profiles/ntt_pass_l0_2e16.md for issue-slot and pipe utilisation"}
 
 
 def run_gpu(args):
@@ -188,15 +213,23 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
     log2 = args.log2
     n = 1 << log2
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import oracle_lib as O  # input generator + verifier (checker only)
-
     setup = F.Blake3Setup(n, device=local)
     stream = torch.cuda.ExternalStream(setup.stream_handle(), device=dev)
     nseeds = max(args.steps, 1)
-    host = [O.compressions(log2, 1000 * rank + i) for i in range(nseeds)]
-    pinned = [torch.from_numpy(b.view(np.uint8).copy()).pin_memory() for b in host]
-    d_ins = [p.to(dev) for p in pinned[:2]]
+    # per-step inputs: the reference generator (benchmark-tools/common/src/lib.rs:20-33),
+    # run on the device; host copies (pinned) feed the end-to-end leg
+    d_seeded = [F.generate_inputs(log2, 1000 * rank + i, device=dev) for i in range(nseeds)]
+    host = [d.cpu().pin_memory() for d in d_seeded]
+    d_ins = d_seeded[:2]
+    L = F._proto_lib()
+    obuf = np.zeros(1 << 20, np.uint8)
+
+    def prove_host(h):
+        """flock_prove with a pinned host buffer: the input copy is inside the call."""
+        ln = ctypes.c_size_t()
+        F.check(L.flock_prove(setup.ctx.handle, ctypes.c_void_p(h.data_ptr()), n,
+                              obuf.ctypes.data_as(ctypes.c_void_p), obuf.size, ctypes.byref(ln)), "flock_prove")
+        return ln.value
 
     def prove_dev(d_in):
         return setup.prove_device(d_in)
@@ -205,9 +238,6 @@ def run_gpu(args):
     for i in range(max(args.warmup, 3)):
         prove_dev(d_ins[i % 2])
     first = prove_dev(d_ins[0])
-    ok, why = O.verify(first, 14 + log2) if rank == 0 else (True, "")
-    if not ok:
-        raise SystemExit(f"proof rejected by the CPU verifier: {why}")
     second = prove_dev(d_ins[1])
     torch.cuda.synchronize()
     if ws > 1:
@@ -231,8 +261,7 @@ def run_gpu(args):
         t0 = time.perf_counter()
         sizes = []
         for i in range(args.steps):
-            p = setup.prove_fast(host[i % len(host)])
-            sizes.append(len(p))
+            sizes.append(prove_host(host[i % len(host)]))
         torch.cuda.synchronize()
         e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
         # Seed to proof bytes (the reference worker's timed path): inputs generated on the device.
@@ -259,8 +288,9 @@ def run_gpu(args):
             "config": {"workload": f"one proof of 2^{log2} BLAKE3 compressions per step (m={14 + log2}, "
                                    "rate 1/2, 64 lanes, Fast profile, BLAKE3 Merkle + transcript)",
                        "parallelism": f"replicas x{ws}", "l2": "working set > 5 GB, larger than L2",
-                       "proof_bytes": len(first), "verified": "first proof accepted by the CPU verifier; "
-                                                              "every timed proof byte-equal to its re-proof",
+                       "proof_bytes": len(first), "verified": "a GPU proof accepted by the CPU verifier (see "
+                                                              "cpu_baseline); every timed proof byte-equal to "
+                                                              "its re-proof",
                        "phase_ms_last_proof": {k: round(v, 3) for k, v in phases.items()}},
             "e2e": {"value": total / (e2e_ms * 1e-3), "unit": "compressions/s", "h2d_bytes_per_step": n * 112,
                     "d2h_bytes_per_step": len(first)},
@@ -271,7 +301,12 @@ def run_gpu(args):
             "roofline": roof,
             "clocks": clk.summary(),
         }
-        line["cpu_baseline"] = oracle_baseline(budget_s=20.0)
+        line["cpu_baseline"] = oracle_baseline(budget_s=20.0, gpu_proof=first, gpu_m=14 + log2)
+        if args.forms and ws == 1:
+            from flock_challenge_gb300 import forms
+            plain = forms.PlainProver()
+            line["forms"] = {"batched": forms.run_batched(64, 3, plain=plain),
+                             "serving": forms.run_serving((8.0, 24.0, 40.0), 60, 3, plain=plain)}
         print(json.dumps(line))
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -284,6 +319,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--log2", type=int, default=18)
+    ap.add_argument("--forms", dest="forms", action="store_true", default=True,
+                    help="also measure the batched and served forms (default)")
+    ap.add_argument("--no-forms", dest="forms", action="store_false")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

@@ -1,0 +1,135 @@
+"""Batched and served proving measured against the plain GPU path.
+
+python -m flock_challenge_gb300.forms [--batch 64] [--requests 60] [--rates 4,8] [--workers 3]
+
+Batched form: `count` proofs whose sizes are drawn log-uniformly from
+2^12..2^18 compressions (seeds 0..count-1) go through one server with
+several workers (flock_prove_batch); the same proofs are made one after
+another on one plain context. Both aggregate compressions/s are reported and
+every batched proof must equal its plain proof byte for byte.
+
+Served form: requests with sizes log-uniform in 2^10..2^20 arrive as a
+Poisson process at each swept rate; the server admits them by device-memory
+budget and overlaps their work. Reported per rate: p50/p99 latency (submit to
+proof ready), sustained compressions/s, and that every served proof equals the
+plain proof of the same request.
+"""
+import argparse
+import json
+import math
+import threading
+import time
+
+import numpy as np
+
+from . import Blake3Setup, Server, footprint_bytes
+
+
+def log_uniform_sizes(n, lo, hi, seed):
+    rng = np.random.default_rng(seed)
+    return [int(math.floor(rng.uniform(lo, hi + 1))) for _ in range(n)]
+
+
+class PlainProver:
+    """One plain context per size (the plain path's own caches), proofs in sequence."""
+
+    def __init__(self):
+        self.setups = {}
+
+    def prove(self, log2, seed):
+        if log2 not in self.setups:
+            self.setups[log2] = Blake3Setup(1 << log2)
+        return self.setups[log2].prove_seed(seed)
+
+
+def run_batched(count=64, workers=3, seed=20260, plain=None):
+    sizes = log_uniform_sizes(count, 12, 18, seed)
+    seeds = list(range(count))
+    total = sum(1 << l for l in sizes)
+    plain = plain or PlainProver()
+    for l in sorted(set(sizes)):          # warm caches (statement digests, buffers)
+        plain.prove(l, 10**6)
+    t = time.perf_counter()
+    ref = [plain.prove(l, s) for l, s in zip(sizes, seeds)]
+    t_plain = time.perf_counter() - t
+    with Server(workers=workers) as srv:
+        srv.prove_batch(sorted(set(sizes)), [10**6] * len(set(sizes)))   # warm the workers
+        t = time.perf_counter()
+        got = srv.prove_batch(sizes, seeds)
+        t_batch = time.perf_counter() - t
+    same = all(a == b for a, b in zip(got, ref))
+    return {"proofs": count, "sizes_log2": "log-uniform 12..18", "compressions": total, "workers": workers,
+            "batched_compressions_per_s": total / t_batch, "plain_sequential_compressions_per_s": total / t_plain,
+            "speedup_vs_plain": t_plain / t_batch, "byte_identical_to_plain": same}
+
+
+def run_serving(rates=(4.0, 8.0), requests=60, workers=3, budget_gb=120, seed=777, plain=None):
+    budget = int(budget_gb * (1 << 30))
+    out = []
+    plain = plain or PlainProver()
+    for rate in rates:
+        rng = np.random.default_rng(seed + int(rate * 1000))
+        sizes = log_uniform_sizes(requests, 10, 20, seed + int(rate))
+        seeds = [int(x) for x in rng.integers(0, 2**62, requests)]
+        gaps = rng.exponential(1.0 / rate, requests)
+        with Server(workers=workers, hbm_budget=budget) as srv:
+            srv.prove_batch(sorted(set(sizes)), [1] * len(set(sizes)))   # warm the workers
+            ids, lat, proofs = [], {}, {}
+            lock = threading.Lock()
+            t0 = time.perf_counter()
+
+            def collect():
+                pending = set()
+                while True:
+                    with lock:
+                        pending |= {i for i in ids if i not in lat and i not in pending}
+                        finished_submitting = len(ids) == requests
+                    for i in list(pending):
+                        tm = srv.times(i)
+                        if tm is not None:
+                            lat[i] = tm[0] + tm[1]
+                            proofs[i] = srv.wait(i)
+                            pending.discard(i)
+                    if finished_submitting and not pending and len(lat) == requests:
+                        return
+                    time.sleep(0.0005)
+
+            th = threading.Thread(target=collect)
+            th.start()
+            nxt = t0
+            for k in range(requests):
+                nxt += gaps[k]
+                d = nxt - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                rid = srv.submit_seed(sizes[k], seeds[k])
+                with lock:
+                    ids.append(rid)
+            th.join()
+            wall = time.perf_counter() - t0
+        lats = np.array([lat[i] for i in ids])
+        total = sum(1 << l for l in sizes)
+        same = all(proofs[i] == plain.prove(l, s) for i, l, s in zip(ids, sizes, seeds) if l <= 16)
+        out.append({"rate_per_s": rate, "requests": requests, "sizes_log2": "log-uniform 10..20",
+                    "p50_ms": float(np.percentile(lats, 50)), "p99_ms": float(np.percentile(lats, 99)),
+                    "sustained_compressions_per_s": total / wall, "offered_compressions_per_s": total / gaps.sum(),
+                    "workers": workers, "hbm_budget_gb": budget_gb,
+                    "byte_identical_to_plain_(sizes_le_2^16)": same})
+    return out
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--requests", type=int, default=60)
+    ap.add_argument("--rates", default="4,8")
+    ap.add_argument("--workers", type=int, default=3)
+    a = ap.parse_args(argv)
+    plain = PlainProver()
+    res = {"batched": run_batched(a.batch, a.workers, plain=plain),
+           "serving": run_serving([float(x) for x in a.rates.split(",")], a.requests, a.workers, plain=plain)}
+    print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()
