@@ -6,8 +6,9 @@
 //    subset-sum table of t_lo, and multiplies its 128 accumulators by t_hi once
 //    per block. Lane l owns bits 4l..4l+3.
 //  * combined basis b[pos] = sum_k gamma_k sum_b bit_b(t_k(pos)) eq(r''_k)[b]
-//    (ring_switch.rs:1720-1760, pcs.rs:1080-1110): 16 byte tables per claim with
-//    gamma folded in, one F128 multiply per claim per position.
+//    (ring_switch.rs:1720-1760, pcs.rs:1080-1110), t_k = eq tensor of the
+//    claim's suffix: per high index, byte tables of the linear map
+//    lo -> L_k(lo * hi), no F128 multiply per position.
 #include "flock_internal.h"
 #include "gf128.cuh"
 
@@ -67,27 +68,71 @@ s_hat_v_kernel(const gf128* __restrict__ z, size_t n, const gf128* __restrict__ 
 }
 
 constexpr int CB_THREADS = 256;
-// tables: [2][16][256] F128 (gamma-scaled byte tables of eq(r''_k)).
+constexpr size_t CB_SMEM = (size_t)2 * 16 * 256 * 16 + 2 * 128 * 16;
+
+// x^i * h for 0 <= i < 128: shift into 256 bits, then reduce.
+__device__ __forceinline__ gf128 gf_mul_xpow(gf128 h, int i) {
+  uint64_t lo = h.w[0] | ((uint64_t)h.w[1] << 32), hi = h.w[2] | ((uint64_t)h.w[3] << 32);
+  uint64_t r[4] = {0, 0, 0, 0};
+  // (hi:lo) << i over four 64-bit words
+  const int wsh = i >> 6, bsh = i & 63;
+  uint64_t s0 = lo << bsh, s1 = (hi << bsh) | (bsh ? lo >> (64 - bsh) : 0), s2 = bsh ? hi >> (64 - bsh) : 0;
+  if (wsh == 0) { r[0] = s0; r[1] = s1; r[2] = s2; }
+  else { r[1] = s0; r[2] = s1; r[3] = s2; }
+  return gf_reduce(r[0], r[1], r[2], r[3]);
+}
+
+// Combined basis b[p] = sum_k L_k(lo_k[p & lo_mask] * hi_k[p >> lo_bits]) with
+// the GF(2)-linear map L_k(u) = sum_b bit_b(u) w_k[b], w_k = gamma_k eq(r''_k)
+// (ring_switch.rs:1720-1760, pcs.rs:1080-1110). For a fixed high index the
+// map lo -> L_k(lo * h) is again GF(2)-linear, so a CTA builds its sixteen
+// byte tables from the 128 images L_k(x^i h) and then needs no GF(2^128)
+// product per position: 2 x 16 table lookups. Each CTA owns one high index
+// and a slice of the low range.
 __global__ void __launch_bounds__(CB_THREADS)
-combined_basis_kernel(size_t n, const gf128* __restrict__ t0_lo, const gf128* __restrict__ t0_hi,
-                      const gf128* __restrict__ t1_lo, const gf128* __restrict__ t1_hi, int lo_bits,
-                      const gf128* __restrict__ tables, gf128* __restrict__ b) {
-  extern __shared__ gf128 tab[];
-  for (int i = threadIdx.x; i < 2 * 16 * 256; i += CB_THREADS) tab[i] = tables[i];
+combined_basis_kernel(int lo_bits, int slices, const gf128* __restrict__ lo0, const gf128* __restrict__ hi0,
+                      const gf128* __restrict__ lo1, const gf128* __restrict__ hi1, const gf128* __restrict__ w,
+                      gf128* __restrict__ b) {
+  extern __shared__ gf128 cb[];
+  gf128* tab = cb;                  // [2][16][256]
+  gf128* beta = cb + 2 * 16 * 256;  // [2][128]
+  const size_t h = blockIdx.x / slices;
+  const int slice = blockIdx.x % slices;
+  {
+    const int k = threadIdx.x >> 7, i = threadIdx.x & 127;
+    const gf128 y = gf_mul_xpow(k ? hi1[h] : hi0[h], i);
+    const gf128* wk = w + 128 * k;
+    gf128 acc = gf_zero();
+#pragma unroll 4
+    for (int bb = 0; bb < 128; bb++)
+      if ((y.w[bb >> 5] >> (bb & 31)) & 1) acc = gf_add(acc, wk[bb]);
+    beta[k * 128 + i] = acc;
+  }
   __syncthreads();
-  const size_t lo_mask = ((size_t)1 << lo_bits) - 1;
-  for (size_t p = (size_t)blockIdx.x * CB_THREADS + threadIdx.x; p < n; p += (size_t)gridDim.x * CB_THREADS) {
-    gf128 u0 = gf_mul(t0_lo[p & lo_mask], t0_hi[p >> lo_bits]);
-    gf128 u1 = gf_mul(t1_lo[p & lo_mask], t1_hi[p >> lo_bits]);
+  for (int e = threadIdx.x; e < 2 * 16 * 256; e += CB_THREADS) {
+    const int k = e >> 12, q = (e >> 8) & 15, v = e & 255;
+    const gf128* bq = beta + k * 128 + 8 * q;
+    gf128 acc = gf_zero();
+#pragma unroll
+    for (int t = 0; t < 8; t++)
+      if ((v >> t) & 1) acc = gf_add(acc, bq[t]);
+    tab[e] = acc;
+  }
+  __syncthreads();
+  const size_t lo_n = (size_t)1 << lo_bits;
+  const size_t per = lo_n / slices;
+  const size_t j0 = (size_t)slice * per;
+  for (size_t j = j0 + threadIdx.x; j < j0 + per; j += CB_THREADS) {
+    const gf128 u0 = lo0[j], u1 = lo1[j];
     gf128 acc = gf_zero();
 #pragma unroll
     for (int q = 0; q < 16; q++) {
-      uint32_t b0 = (u0.w[q >> 2] >> (8 * (q & 3))) & 255;
-      uint32_t b1 = (u1.w[q >> 2] >> (8 * (q & 3))) & 255;
+      const uint32_t b0 = (u0.w[q >> 2] >> (8 * (q & 3))) & 255;
+      const uint32_t b1 = (u1.w[q >> 2] >> (8 * (q & 3))) & 255;
       acc = gf_add(acc, tab[q * 256 + b0]);
       acc = gf_add(acc, tab[4096 + q * 256 + b1]);
     }
-    b[p] = acc;
+    b[(h << lo_bits) + j] = acc;
   }
 }
 
@@ -119,15 +164,19 @@ int flock_launch_s_hat_v(const void* z, size_t n, const void* t_lo, const void* 
 int flock_s_hat_v_warps(int grid) { return grid * (SH_THREADS / 32); }
 
 int flock_launch_combined_basis(size_t n, const void* t0_lo, const void* t0_hi, const void* t1_lo, const void* t1_hi,
-                                int lo_bits, const void* tables, void* b, cudaStream_t st) {
-  size_t smem = 2 * 16 * 256 * 16;
+                                int lo_bits, const void* w, void* b, cudaStream_t st) {
   flock_once_per_device((const void*)combined_basis_kernel, [] {
-    cudaFuncSetAttribute(combined_basis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(2 * 16 * 256 * 16));
+    cudaFuncSetAttribute(combined_basis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CB_SMEM);
   });
-  size_t grid = (n + CB_THREADS - 1) / CB_THREADS;
-  if (grid > 152 * 2) grid = 152 * 2;
-  combined_basis_kernel<<<(unsigned)grid, CB_THREADS, smem, st>>>(
-      n, (const gf128*)t0_lo, (const gf128*)t0_hi, (const gf128*)t1_lo, (const gf128*)t1_hi, lo_bits,
-      (const gf128*)tables, (gf128*)b); flock_count_launch();
+  const size_t lo_n = (size_t)1 << lo_bits;
+  if (n % lo_n != 0 || lo_n < CB_THREADS) return FLOCK_ERR_SHAPE;
+  const size_t n_hi = n >> lo_bits;
+  // enough CTAs to fill the GPU: split the low range when there are few high indices
+  int slices = 1;
+  while (n_hi * slices < 152 * 2 && lo_n / (2 * slices) >= CB_THREADS) slices *= 2;
+  combined_basis_kernel<<<(unsigned)(n_hi * slices), CB_THREADS, CB_SMEM, st>>>(
+      lo_bits, slices, (const gf128*)t0_lo, (const gf128*)t0_hi, (const gf128*)t1_lo, (const gf128*)t1_hi,
+      (const gf128*)w, (gf128*)b);
+  flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }

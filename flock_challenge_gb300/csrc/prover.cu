@@ -727,19 +727,12 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     F target = gam[0] * claims[0] + gam[1] * claims[1];
     void* dbc = S->bc.get(n128 * 16);
     {
-      std::vector<F> tabs(2 * 16 * 256);
-      for (int k = 0; k < 2; k++) {
-        for (int q = 0; q < 16; q++) {
-          F* t = &tabs[(k * 16 + q) * 256];
-          t[0] = F();
-          for (int v = 1; v < 256; v++) {
-            int low = __builtin_ctz(v);
-            t[v] = t[v & (v - 1)] + gam[k] * eqr[k][8 * q + low];
-          }
-        }
-      }
-      void* dt = S->tables.get(tabs.size() * 16);
-      h2d(*S, dt, tabs.data(), tabs.size() * 16);
+      // w_k[b] = gamma_k eq(r''_k)[b]: the basis is sum_k sum_b bit_b(t_k) w_k[b]
+      std::vector<F> wk(2 * 128);
+      for (int k = 0; k < 2; k++)
+        for (int bb = 0; bb < 128; bb++) wk[k * 128 + bb] = gam[k] * eqr[k][bb];
+      void* dt = S->tables.get(wk.size() * 16);
+      h2d(*S, dt, wk.data(), wk.size() * 16);
       FK(flock_launch_combined_basis(n128, S->tlo0.p, S->thi0.p, S->tlo1.p, S->thi1.p, rs_lo, dt, dbc, st));
     }
     T.ring_switch_ms = clk.lap();

@@ -340,7 +340,10 @@ __global__ void eq_split_kernel(const gf128* __restrict__ r, int lo_bits, int hi
 // eq[j] = eq_lo[j & lo_mask] * eq_hi[j >> lo_bits]: the inner sums run over
 // eq_lo only and are multiplied by eq_hi once per CTA row block.
 constexpr int RND_THREADS = 256;
-__global__ void __launch_bounds__(RND_THREADS)
+#ifndef ZC_RND_MIN_BLOCKS
+#define ZC_RND_MIN_BLOCKS 2  // two resident blocks per SM (128 registers) measured best
+#endif
+__global__ void __launch_bounds__(RND_THREADS, ZC_RND_MIN_BLOCKS)
 zc_round_kernel(const gf128* __restrict__ A, const gf128* __restrict__ B, size_t n_pairs, int bind,
                 gf128 rho, gf128* __restrict__ Aout, gf128* __restrict__ Bout, const gf128* __restrict__ eq_lo,
                 const gf128* __restrict__ eq_hi, int lo_bits, gf128* __restrict__ partials) {
