@@ -73,3 +73,19 @@ def test_commit_matches_oracle(ctx, n_log):
     assert np.array_equal(host(cw).view(np.uint64), ocw)
     assert np.array_equal(host(tree).reshape(-1, 32), otree)
     assert root == oroot
+
+
+@pytest.mark.parametrize("rows_log", [8, 10])
+def test_rate_quarter_256_columns_4k_leaves_matches_oracle(ctx, rows_log):
+    """The kernel-microbench shape: 2^rows x 256 columns of uniform F128, rate 1/4
+    (two replica layers, then the NTT), Merkle leaves of 256 x 16 B = 4 KiB (four
+    BLAKE3 chunks merged, non-root)."""
+    m = 7 + 8 + rows_log
+    rng = np.random.default_rng(rows_log)
+    z = rng.integers(0, 2**63, (1 << (m - 7)) * 2, dtype=np.uint64)
+    z |= rng.integers(0, 2, z.shape, dtype=np.uint64) << np.uint64(63)
+    root, cw, tree = F.commit(ctx, to_dev(z), m, log_inv_rate=2, log_batch_size=8)
+    oroot, ocw, otree = O.commit(z, m, 2, 8, want_codeword=True, want_tree=True)
+    assert np.array_equal(host(cw).view(np.uint64), ocw)
+    assert np.array_equal(host(tree).reshape(-1, 32), otree)
+    assert root == oroot
