@@ -116,3 +116,58 @@ __device__ __forceinline__ gf128 gf_mul_x(gf128 a) {
   r.w[0] = (a.w[0] << 1) ^ (0x87u & (0u - carry));
   return r;
 }
+
+// ---- products by a prepared operand ------------------------------------------
+// When one factor is reused (an NTT twiddle, an eq weight), its nine Karatsuba
+// words (b0, b1, b0^b1, b2, b3, b2^b3, b0^b2, b1^b3, b0^b1^b2^b3), each split
+// into the four every-fourth-bit masks, can be computed once and stored: a
+// product with the prepared form skips that masking (36 logic instructions).
+struct __align__(16) gf128p {
+  uint4 m[9];
+};
+
+__host__ __device__ inline gf128p gf_prepare(gf128 b) {
+  const uint32_t w[9] = {b.w[0], b.w[1], b.w[0] ^ b.w[1], b.w[2], b.w[3], b.w[2] ^ b.w[3],
+                         b.w[0] ^ b.w[2], b.w[1] ^ b.w[3], b.w[0] ^ b.w[1] ^ b.w[2] ^ b.w[3]};
+  gf128p p;
+  for (int i = 0; i < 9; i++)
+    p.m[i] = make_uint4(w[i] & 0x11111111u, w[i] & 0x22222222u, w[i] & 0x44444444u, w[i] & 0x88888888u);
+  return p;
+}
+
+__device__ __forceinline__ uint64_t clmul32_p(uint32_t a, uint4 b) {
+  const uint32_t m0 = 0x11111111u, m1 = 0x22222222u, m2 = 0x44444444u, m3 = 0x88888888u;
+  uint32_t a0 = a & m0, a1 = a & m1, a2 = a & m2, a3 = a & m3;
+  uint64_t r0 = mulw(a0, b.x) ^ mulw(a1, b.w) ^ mulw(a2, b.z) ^ mulw(a3, b.y);
+  uint64_t r1 = mulw(a0, b.y) ^ mulw(a1, b.x) ^ mulw(a2, b.w) ^ mulw(a3, b.z);
+  uint64_t r2 = mulw(a0, b.z) ^ mulw(a1, b.y) ^ mulw(a2, b.x) ^ mulw(a3, b.w);
+  uint64_t r3 = mulw(a0, b.w) ^ mulw(a1, b.z) ^ mulw(a2, b.y) ^ mulw(a3, b.x);
+  return (r0 & 0x1111111111111111ull) | (r1 & 0x2222222222222222ull) | (r2 & 0x4444444444444444ull) |
+         (r3 & 0x8888888888888888ull);
+}
+
+__device__ __forceinline__ gf256 gf_mul_wide_p(gf128 a, const gf128p& p) {
+  const uint32_t a0 = a.w[0], a1 = a.w[1], a2 = a.w[2], a3 = a.w[3];
+  uint64_t ll = clmul32_p(a0, p.m[0]), lh = clmul32_p(a1, p.m[1]), lm = clmul32_p(a0 ^ a1, p.m[2]);
+  lm ^= ll ^ lh;
+  const uint64_t l0 = ll ^ (lm << 32), l1 = lh ^ (lm >> 32);
+  uint64_t hl = clmul32_p(a2, p.m[3]), hh = clmul32_p(a3, p.m[4]), hm = clmul32_p(a2 ^ a3, p.m[5]);
+  hm ^= hl ^ hh;
+  const uint64_t h0 = hl ^ (hm << 32), h1 = hh ^ (hm >> 32);
+  const uint32_t c0 = a0 ^ a2, c1 = a1 ^ a3;
+  uint64_t ml = clmul32_p(c0, p.m[6]), mh = clmul32_p(c1, p.m[7]), mx = clmul32_p(c0 ^ c1, p.m[8]);
+  mx ^= ml ^ mh;
+  uint64_t m0 = ml ^ (mx << 32), m1 = mh ^ (mx >> 32);
+  m0 ^= l0 ^ h0;
+  m1 ^= l1 ^ h1;
+  gf256 o;
+  o.r[0] = l0; o.r[1] = l1 ^ m0; o.r[2] = h0 ^ m1; o.r[3] = h1;
+  return o;
+}
+__device__ __forceinline__ gf128 gf_mul_p(gf128 a, const gf128p& p) { return gf256_reduce(gf_mul_wide_p(a, p)); }
+__device__ __forceinline__ gf128p gf_load_p(const gf128p* q) {
+  gf128p p;
+#pragma unroll
+  for (int i = 0; i < 9; i++) p.m[i] = q->m[i];
+  return p;
+}

@@ -55,8 +55,10 @@ struct PassShape {
   static constexpr int PT = 1 << (F - E);            // threads per lane
   static constexpr int THREADS = TL * PT;
   static constexpr int SMEM = K2 > 0 ? (1 << F) * TL * 16 : 16;
-  static constexpr int MIN_BLOCKS =
-      NTT_SM_THREADS / THREADS < 1 ? 1 : NTT_SM_THREADS / THREADS > 32 ? 32 : NTT_SM_THREADS / THREADS;
+  static constexpr int WARP_THREADS = THREADS < 32 ? 32 : THREADS;  // a block occupies whole warps
+  static constexpr int MIN_BLOCKS = NTT_SM_THREADS / WARP_THREADS < 1   ? 1
+                                    : NTT_SM_THREADS / WARP_THREADS > 32 ? 32
+                                                                         : NTT_SM_THREADS / WARP_THREADS;
 };
 
 // Tile position of the element with label j in stage 1 / stage 2. Labels are
@@ -76,10 +78,12 @@ __host__ __device__ constexpr int rotr_bits(int j, int r) {
   return r == 0 ? j : ((j >> r) | (j << (E - r))) & ((1 << E) - 1);
 }
 
-template <int F, int TL>
+// PREP: the twiddle table holds prepared operands (gf128p) instead of plain
+// elements, so the products skip the twiddle's masking.
+template <int F, int TL, bool PREP>
 __global__ void __launch_bounds__(PassShape<F, TL>::THREADS, PassShape<F, TL>::MIN_BLOCKS)
 ntt_pass_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t src_pos_mask,
-                const gf128* __restrict__ tw, int log_d, int log_lanes, int l0) {
+                const void* __restrict__ tw_any, int log_d, int log_lanes, int l0) {
   using S = PassShape<F, TL>;
   constexpr int E = S::E, K1 = S::K1, K2 = S::K2, NE = 1 << E, H = NE / 2;
   extern __shared__ gf128 tile[];
@@ -115,18 +119,31 @@ ntt_pass_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t s
     }
     const bool st2 = t >= K1;
     const int r = st2 ? t - K1 : t;
-    const gf128* twl = tw + ((((size_t)1) << (l0 + t)) - 1 + (hi << t));
-    gf128 tv[H];
+    const size_t twb = (((size_t)1) << (l0 + t)) - 1 + (hi << t);
+    int ti[H];
 #pragma unroll
     for (int j = 0; j < H; j++) {
       const int jo = ((j >> r) | (j << (E - r))) & (NE - 1);
       const int i0 = st2 ? pos_stage2<F, E, K2>(pt, jo) : pos_stage1<F, E, K1>(pt, jo);
-      tv[j] = gf_load(&twl[i0 >> (F - t)]);
+      ti[j] = i0 >> (F - t);
     }
+    if constexpr (PREP) {
+      const gf128p* twl = reinterpret_cast<const gf128p*>(tw_any) + twb;
 #pragma unroll
-    for (int j = 0; j < H; j++) {
-      y[j] = gf_add(y[j], gf_mul(y[j + H], tv[j]));
-      y[j + H] = gf_add(y[j + H], y[j]);
+      for (int j = 0; j < H; j++) {
+        y[j] = gf_add(y[j], gf_mul_p(y[j + H], gf_load_p(&twl[ti[j]])));
+        y[j + H] = gf_add(y[j + H], y[j]);
+      }
+    } else {
+      const gf128* twl = reinterpret_cast<const gf128*>(tw_any) + twb;
+      gf128 tv[H];
+#pragma unroll
+      for (int j = 0; j < H; j++) tv[j] = gf_load(&twl[ti[j]]);
+#pragma unroll
+      for (int j = 0; j < H; j++) {
+        y[j] = gf_add(y[j], gf_mul(y[j + H], tv[j]));
+        y[j + H] = gf_add(y[j + H], y[j]);
+      }
     }
     // rotate labels left by one: new[k] = old[rotr(k, 1)]
     gf128 z[NE];
@@ -177,8 +194,8 @@ std::map<std::pair<int, int>, void*> g_tw;  // (device, log_d) -> device table
 
 constexpr int kMaxPassLayers = 2 * NTT_POS_LOG < 8 ? 2 * NTT_POS_LOG : 8;
 
-template <int F>
-int launch_pass(gf128* dst, const gf128* src, size_t mask, const gf128* tw, int log_d, int log_lanes, int l0,
+template <int F, bool PREP>
+int launch_pass(gf128* dst, const gf128* src, size_t mask, const void* tw, int log_d, int log_lanes, int l0,
                 cudaStream_t st) {
   if constexpr (F > kMaxPassLayers) {
     return FLOCK_ERR_SHAPE;
@@ -187,11 +204,13 @@ int launch_pass(gf128* dst, const gf128* src, size_t mask, const gf128* tw, int 
     if (log_lanes >= 4) {
       using S = PassShape<F, 16>;
       size_t blocks = tiles * ((1 << log_lanes) / 16);
-      ntt_pass_kernel<F, 16><<<(unsigned)blocks, S::THREADS, S::SMEM, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
+      ntt_pass_kernel<F, 16, PREP>
+          <<<(unsigned)blocks, S::THREADS, S::SMEM, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
     } else {
       using S = PassShape<F, 8>;
       size_t blocks = tiles * ((1 << log_lanes) / 8);
-      ntt_pass_kernel<F, 8><<<(unsigned)blocks, S::THREADS, S::SMEM, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
+      ntt_pass_kernel<F, 8, PREP>
+          <<<(unsigned)blocks, S::THREADS, S::SMEM, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
     }
     flock_count_launch();
     return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
@@ -202,28 +221,43 @@ int launch_pass(gf128* dst, const gf128* src, size_t mask, const gf128* tw, int 
 // the default 48 KB (8 layers with 16 lanes: 64 KB), once per device.
 void ntt_set_smem_attrs() {
   if constexpr (kMaxPassLayers >= 8) {
-    flock_once_per_device((const void*)ntt_pass_kernel<kMaxPassLayers, 16>, [] {
-      cudaFuncSetAttribute(ntt_pass_kernel<kMaxPassLayers, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    flock_once_per_device((const void*)ntt_pass_kernel<kMaxPassLayers, 16, true>, [] {
+      cudaFuncSetAttribute(ntt_pass_kernel<kMaxPassLayers, 16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           PassShape<kMaxPassLayers, 16>::SMEM);
+      cudaFuncSetAttribute(ntt_pass_kernel<kMaxPassLayers, 16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            PassShape<kMaxPassLayers, 16>::SMEM);
     });
   }
 }
 
-int run_pass(int f, gf128* dst, const gf128* src, size_t mask, const gf128* tw, int log_d, int log_lanes, int l0,
-             cudaStream_t st) {
+template <bool PREP>
+int run_pass_t(int f, gf128* dst, const gf128* src, size_t mask, const void* tw, int log_d, int log_lanes, int l0,
+               cudaStream_t st) {
   ntt_set_smem_attrs();
   switch (f) {
-    case 1: return launch_pass<1>(dst, src, mask, tw, log_d, log_lanes, l0, st);
-    case 2: return launch_pass<2>(dst, src, mask, tw, log_d, log_lanes, l0, st);
-    case 3: return launch_pass<3>(dst, src, mask, tw, log_d, log_lanes, l0, st);
-    case 4: return launch_pass<4>(dst, src, mask, tw, log_d, log_lanes, l0, st);
-    case 5: return launch_pass<5>(dst, src, mask, tw, log_d, log_lanes, l0, st);
-    case 6: return launch_pass<6>(dst, src, mask, tw, log_d, log_lanes, l0, st);
-    case 7: return launch_pass<7>(dst, src, mask, tw, log_d, log_lanes, l0, st);
-    case 8: return launch_pass<8>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 1: return launch_pass<1, PREP>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 2: return launch_pass<2, PREP>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 3: return launch_pass<3, PREP>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 4: return launch_pass<4, PREP>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 5: return launch_pass<5, PREP>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 6: return launch_pass<6, PREP>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 7: return launch_pass<7, PREP>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 8: return launch_pass<8, PREP>(dst, src, mask, tw, log_d, log_lanes, l0, st);
     default: return FLOCK_ERR_SHAPE;
   }
 }
+
+int run_pass(int f, gf128* dst, const gf128* src, size_t mask, const gf128* tw, int log_d, int log_lanes, int l0,
+             cudaStream_t st) {
+  return run_pass_t<false>(f, dst, src, mask, tw, log_d, log_lanes, l0, st);
+}
+
+__global__ void prepare_twiddles_kernel(const gf128* __restrict__ tw, size_t n, gf128p* __restrict__ out) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = gf_prepare(tw[i]);
+}
+
+std::map<std::pair<int, int>, void*> g_twp;  // (device, log_d) -> prepared table (under g_tw_mu)
 
 }  // namespace
 
@@ -245,6 +279,30 @@ const void* flock_ntt_twiddles(int log_d) {
   return d;
 }
 
+// Prepared twiddle table (gf128p per entry), built on the device from the
+// plain table once per (device, log_d).
+const void* flock_ntt_twiddles_prepared(int log_d) {
+  const gf128* tw = (const gf128*)flock_ntt_twiddles(log_d);
+  if (!tw) return nullptr;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_tw_mu);
+  auto key = std::make_pair(dev, log_d);
+  auto it = g_twp.find(key);
+  if (it != g_twp.end()) return it->second;
+  const size_t n = ((size_t)1 << log_d) - 1;
+  void* d = nullptr;
+  if (cudaMalloc(&d, (n + 1) * sizeof(gf128p)) != cudaSuccess) return nullptr;
+  prepare_twiddles_kernel<<<(unsigned)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096), 256>>>(tw, n, (gf128p*)d);
+  flock_count_launch();
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    cudaFree(d);
+    return nullptr;
+  }
+  g_twp[key] = d;
+  return d;
+}
+
 // Applies layers [start_layer, log_d) in passes of up to 8 layers. d_src (may
 // equal d_data) holds the input rows addressed with position mask
 // 2^(log_d - start_layer) - 1, so a distinct d_src supplies the replicated
@@ -253,7 +311,7 @@ int flock_launch_ntt(void* d_data, const void* d_src, int log_d, int log_lanes, 
                      cudaStream_t stream) {
   if (log_lanes < 3 || log_lanes > 10 || log_d < 1 || log_d > 30 || start_layer < 0 || start_layer > log_d)
     return FLOCK_ERR_SHAPE;
-  const gf128* tw = (const gf128*)flock_ntt_twiddles(log_d);
+  const void* tw = flock_ntt_twiddles_prepared(log_d);
   if (!tw) return FLOCK_ERR_OOM;
   gf128* data = (gf128*)d_data;
   const gf128* src = d_src ? (const gf128*)d_src : data;
@@ -274,7 +332,7 @@ int flock_launch_ntt(void* d_data, const void* d_src, int log_d, int log_lanes, 
   int l = start_layer;
   for (int q = 0; q < passes; q++) {
     int f = (remaining - (l - start_layer) + (passes - q) - 1) / (passes - q);
-    int rc = run_pass(f, data, src, mask, tw, log_d, log_lanes, l, stream);
+    int rc = run_pass_t<true>(f, data, src, mask, tw, log_d, log_lanes, l, stream);
     if (rc != FLOCK_OK) return rc;
     src = data;
     mask = ~(size_t)0;
