@@ -2,7 +2,8 @@
 //
 //  * partial fold: z_vec[i] = sum_outer z[i, outer] eq(x_outer, outer), read
 //    from the byte stripe (byte (outer/8)*2^14 + i holds 8 outer bits), one
-//    256-entry subset-sum table of eq per stripe (lincheck.rs:655-720);
+//    256-entry subset-sum table of eq per stripe, eight stripes per round
+//    (lincheck.rs:655-720);
 //  * comb: alpha * A0^T eq_inner + B0^T eq_inner (+ beta at the constant
 //    column) gathered column-wise from a CSC copy of the base matrices;
 //  * product sumcheck rounds over (comb, z_vec), binding the top variable
@@ -12,43 +13,64 @@
 
 namespace {
 
-constexpr int PF_THREADS = 1024;
-constexpr int PF_PER_THREAD = FLOCK_K / PF_THREADS;  // 16
+constexpr int PF_THREADS = 256;
+constexpr int PF_PER_THREAD = 16;                                    // bytes (columns) per thread
+constexpr int PF_SLICES = FLOCK_K / (PF_THREADS * PF_PER_THREAD);  // column slices: 4
 
-__global__ void __launch_bounds__(PF_THREADS, 1)
+constexpr int PF_GROUP = 8;  // stripes per table round (64 outer indices)
+
+// CTA (slice, part): columns [slice * 4096, +4096) of the stripe groups
+// part, part + parts, ... Per round: 64 eq weights (one product each, 64
+// threads), PF_GROUP subset-sum tables of 256 entries, then every thread folds
+// its 16 bytes of each stripe. Grouping amortises the barriers and the table
+// build over eight stripes; the four column slices keep 64 accumulator
+// registers per thread affordable.
+__global__ void __launch_bounds__(PF_THREADS, 2)
 lc_partial_fold_kernel(const uint8_t* __restrict__ stripe, size_t n_stripes, const gf128* __restrict__ eq_lo,
                        const gf128* __restrict__ eq_hi, int lo_bits, gf128* __restrict__ partials) {
-  __shared__ gf128 t8[256];
-  __shared__ gf128 e8v[8];
+  __shared__ gf128 t8[PF_GROUP][256];
+  __shared__ gf128 e8v[PF_GROUP * 8];
   gf128 acc[PF_PER_THREAD];
 #pragma unroll
   for (int k = 0; k < PF_PER_THREAD; k++) acc[k] = gf_zero();
+  const int slice = blockIdx.x % PF_SLICES;
+  const size_t part = blockIdx.x / PF_SLICES, parts = gridDim.x / PF_SLICES;
+  const size_t col0 = (size_t)slice * PF_THREADS * PF_PER_THREAD + (size_t)threadIdx.x * PF_PER_THREAD;
   const size_t lo_mask = ((size_t)1 << lo_bits) - 1;
-  for (size_t s = blockIdx.x; s < n_stripes; s += gridDim.x) {
-    if (threadIdx.x < 8) {
-      size_t o = 8 * s + threadIdx.x;
+  const size_t n_groups = n_stripes / PF_GROUP;
+  for (size_t g = part; g < n_groups; g += parts) {
+    const size_t s0 = g * PF_GROUP;
+    if (threadIdx.x < PF_GROUP * 8) {
+      size_t o = 8 * s0 + threadIdx.x;
       e8v[threadIdx.x] = gf_mul(eq_lo[o & lo_mask], eq_hi[o >> lo_bits]);
     }
+    // this thread's bytes of the group's stripes (loads overlap the table build)
+    uint4 bytes[PF_GROUP];
+#pragma unroll
+    for (int q = 0; q < PF_GROUP; q++)
+      bytes[q] = *reinterpret_cast<const uint4*>(stripe + (s0 + q) * FLOCK_K + col0);
     __syncthreads();
-    if (threadIdx.x < 256) {
-      gf128 v = gf_zero();
+    for (int e = threadIdx.x; e < PF_GROUP * 256; e += PF_THREADS) {
+      const int q = e >> 8, v = e & 255;
+      gf128 acc8 = gf_zero();
+#pragma unroll
       for (int r = 0; r < 8; r++)
-        if ((threadIdx.x >> r) & 1) v = gf_add(v, e8v[r]);
-      t8[threadIdx.x] = v;
+        if ((v >> r) & 1) acc8 = gf_add(acc8, e8v[8 * q + r]);
+      t8[q][v] = acc8;
     }
     __syncthreads();
-    const uint8_t* row = stripe + s * FLOCK_K;
-    // each thread: 16 consecutive bytes (one uint4) of the 2^14-byte stripe
-    uint4 bytes = reinterpret_cast<const uint4*>(row)[threadIdx.x];
-    uint32_t wds[4] = {bytes.x, bytes.y, bytes.z, bytes.w};
 #pragma unroll
-    for (int k = 0; k < PF_PER_THREAD; k++) {
-      uint32_t b = (wds[k >> 2] >> (8 * (k & 3))) & 255;
-      if (b) acc[k] = gf_add(acc[k], t8[b]);
+    for (int q = 0; q < PF_GROUP; q++) {
+      const uint32_t wds[4] = {bytes[q].x, bytes[q].y, bytes[q].z, bytes[q].w};
+#pragma unroll
+      for (int k = 0; k < PF_PER_THREAD; k++) {
+        uint32_t b = (wds[k >> 2] >> (8 * (k & 3))) & 255;
+        if (b) acc[k] = gf_add(acc[k], t8[q][b]);
+      }
     }
     __syncthreads();
   }
-  gf128* out = partials + (size_t)blockIdx.x * FLOCK_K + (size_t)threadIdx.x * PF_PER_THREAD;
+  gf128* out = partials + part * FLOCK_K + col0;
 #pragma unroll
   for (int k = 0; k < PF_PER_THREAD; k++) out[k] = acc[k];
 }
@@ -134,10 +156,14 @@ inline gf128 to_gf(const uint64_t v[2]) {
 
 }  // namespace
 
+// grid = number of partial rows (stripe-group partitions); partials: grid x 2^14.
 int flock_launch_lc_partial_fold(const void* stripe, size_t n_stripes, const void* eq_lo, const void* eq_hi,
                                  int lo_bits, void* partials, int grid, cudaStream_t st) {
-  lc_partial_fold_kernel<<<grid, PF_THREADS, 0, st>>>((const uint8_t*)stripe, n_stripes, (const gf128*)eq_lo,
-                                                      (const gf128*)eq_hi, lo_bits, (gf128*)partials); flock_count_launch();
+  if (n_stripes % PF_GROUP != 0) return FLOCK_ERR_SHAPE;
+  lc_partial_fold_kernel<<<grid * PF_SLICES, PF_THREADS, 0, st>>>((const uint8_t*)stripe, n_stripes,
+                                                                  (const gf128*)eq_lo, (const gf128*)eq_hi, lo_bits,
+                                                                  (gf128*)partials);
+  flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 

@@ -651,7 +651,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       int lob = n_outer_log / 2;
       eq_split_dev(*S, x_out, lob, S->eqlo, S->eqhi);
       size_t n_stripes = ((size_t)1 << n_outer_log) / 8;
-      int grid = (int)std::min<size_t>(n_stripes, 152);
+      int grid = (int)std::min<size_t>(n_stripes / 8, 152);  // partial rows (stripe-group partitions)
       void* dpart = S->part.get((size_t)grid * FLOCK_K * 16);
       FK(flock_launch_lc_partial_fold(ds, n_stripes, S->eqlo.p, S->eqhi.p, lob, dpart, grid, st));
       void* dzv = S->zvec.get(FLOCK_K * 16);
