@@ -345,7 +345,7 @@ constexpr int RND_THREADS = 256;
 #endif
 __global__ void __launch_bounds__(RND_THREADS, ZC_RND_MIN_BLOCKS)
 zc_round_kernel(const gf128* __restrict__ A, const gf128* __restrict__ B, size_t n_pairs, int bind,
-                gf128 rho, gf128* __restrict__ Aout, gf128* __restrict__ Bout, const gf128* __restrict__ eq_lo,
+                const __grid_constant__ gf128p rho, gf128* __restrict__ Aout, gf128* __restrict__ Bout, const gf128* __restrict__ eq_lo,
                 const gf128* __restrict__ eq_hi, int lo_bits, gf128* __restrict__ partials) {
   // grid-stride over hi blocks: each CTA handles whole hi indices
   const size_t lo_n = (size_t)1 << lo_bits;
@@ -359,11 +359,11 @@ zc_round_kernel(const gf128* __restrict__ A, const gf128* __restrict__ B, size_t
       gf128 a0, a1, b0, b1;
       if (bind) {
         gf128 p0 = A[4 * j], p1 = A[4 * j + 1], p2 = A[4 * j + 2], p3 = A[4 * j + 3];
-        a0 = gf_add(p0, gf_mul(rho, gf_add(p0, p1)));
-        a1 = gf_add(p2, gf_mul(rho, gf_add(p2, p3)));
+        a0 = gf_add(p0, gf_mul_p(gf_add(p0, p1), rho));
+        a1 = gf_add(p2, gf_mul_p(gf_add(p2, p3), rho));
         gf128 q0 = B[4 * j], q1 = B[4 * j + 1], q2 = B[4 * j + 2], q3 = B[4 * j + 3];
-        b0 = gf_add(q0, gf_mul(rho, gf_add(q0, q1)));
-        b1 = gf_add(q2, gf_mul(rho, gf_add(q2, q3)));
+        b0 = gf_add(q0, gf_mul_p(gf_add(q0, q1), rho));
+        b1 = gf_add(q2, gf_mul_p(gf_add(q2, q3), rho));
         Aout[2 * j] = a0; Aout[2 * j + 1] = a1;
         Bout[2 * j] = b0; Bout[2 * j + 1] = b1;
       } else {
@@ -447,7 +447,8 @@ int flock_launch_zc_round(const void* A, const void* B, size_t n_pairs, int bind
                           int grid, cudaStream_t st) {
   gf128 r;
   r.w[0] = (uint32_t)rho[0]; r.w[1] = (uint32_t)(rho[0] >> 32); r.w[2] = (uint32_t)rho[1]; r.w[3] = (uint32_t)(rho[1] >> 32);
-  zc_round_kernel<<<grid, RND_THREADS, 0, st>>>((const gf128*)A, (const gf128*)B, n_pairs, bind, r, (gf128*)Aout,
+  zc_round_kernel<<<grid, RND_THREADS, 0, st>>>((const gf128*)A, (const gf128*)B, n_pairs, bind, gf_prepare(r),
+                                                (gf128*)Aout,
                                                 (gf128*)Bout, (const gf128*)eq_lo, (const gf128*)eq_hi, lo_bits,
                                                 (gf128*)partials); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
