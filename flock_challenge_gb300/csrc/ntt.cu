@@ -21,7 +21,9 @@
 // copy layers (pcs/commit.rs:451-473).
 #include <cstdio>
 #include <map>
+#include <cstdlib>
 #include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "flock_internal.h"
@@ -37,28 +39,33 @@ namespace {
 // of at most four layers (the top k1 pair bits, then the low k2 bits) with one
 // shared-memory exchange between them. Loads and stores go straight between
 // HBM and registers: the TL lanes of a position are a contiguous TL*16-byte run.
-// Positions per thread (log2) and the resident threads per SM the register
-// budget is sized for; measured on the L0 commit (2^20 x 64 lanes) and the
-// 8-lane Ligerito codes, 8 positions per thread at 512 threads per SM is best.
-#ifndef NTT_POS_LOG
-#define NTT_POS_LOG 3
-#endif
-#ifndef NTT_SM_THREADS
-#define NTT_SM_THREADS 512
-#endif
-template <int F, int TL>
+// Pass shape variants: positions per thread (log2) and the resident threads
+// per SM the register budget is sized for. The autotuner below times them per
+// transform shape on the device and keeps the fastest; variant 1 is the
+// default when tuning is off.
+//   variant 0: 4 positions per thread, 768 threads/SM (passes of <= 4 layers)
+//   variant 1: 8 positions per thread, 512 threads/SM (passes of <= 6 layers)
+//   variant 2: 16 positions per thread, 256 threads/SM (passes of <= 8 layers)
+constexpr int kVariants = 3;
+constexpr int kDefaultVariant = 1;
+__host__ __device__ constexpr int variant_pos_log(int v) { return v == 0 ? 2 : v == 1 ? 3 : 4; }
+__host__ __device__ constexpr int variant_sm_threads(int v) { return v == 0 ? 768 : v == 1 ? 512 : 256; }
+__host__ __device__ constexpr int variant_max_layers(int v) {
+  return 2 * variant_pos_log(v) < 8 ? 2 * variant_pos_log(v) : 8;
+}
+
+template <int F, int TL, int V>
 struct PassShape {
-  static constexpr int E = F < NTT_POS_LOG ? F : NTT_POS_LOG;  // positions per thread (log2)
+  static constexpr int E = F < variant_pos_log(V) ? F : variant_pos_log(V);  // positions per thread (log2)
   static constexpr int K1 = F <= E ? F : (F + 1) / 2 < E ? (F + 1) / 2 : E;  // stage 1 layers
   static constexpr int K2 = F - K1;
-  static_assert(K2 <= E, "a pass covers at most 2 * NTT_POS_LOG layers");
+  static_assert(K2 <= E, "a pass covers at most twice the positions-per-thread bits");
   static constexpr int PT = 1 << (F - E);            // threads per lane
   static constexpr int THREADS = TL * PT;
   static constexpr int SMEM = K2 > 0 ? (1 << F) * TL * 16 : 16;
   static constexpr int WARP_THREADS = THREADS < 32 ? 32 : THREADS;  // a block occupies whole warps
-  static constexpr int MIN_BLOCKS = NTT_SM_THREADS / WARP_THREADS < 1   ? 1
-                                    : NTT_SM_THREADS / WARP_THREADS > 32 ? 32
-                                                                         : NTT_SM_THREADS / WARP_THREADS;
+  static constexpr int BLOCKS_FIT = variant_sm_threads(V) / WARP_THREADS;
+  static constexpr int MIN_BLOCKS = BLOCKS_FIT < 1 ? 1 : BLOCKS_FIT > 32 ? 32 : BLOCKS_FIT;
 };
 
 // Tile position of the element with label j in stage 1 / stage 2. Labels are
@@ -80,11 +87,11 @@ __host__ __device__ constexpr int rotr_bits(int j, int r) {
 
 // PREP: the twiddle table holds prepared operands (gf128p) instead of plain
 // elements, so the products skip the twiddle's masking.
-template <int F, int TL, bool PREP>
-__global__ void __launch_bounds__(PassShape<F, TL>::THREADS, PassShape<F, TL>::MIN_BLOCKS)
+template <int F, int TL, bool PREP, int V>
+__global__ void __launch_bounds__(PassShape<F, TL, V>::THREADS, PassShape<F, TL, V>::MIN_BLOCKS)
 ntt_pass_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t src_pos_mask,
                 const void* __restrict__ tw_any, int log_d, int log_lanes, int l0) {
-  using S = PassShape<F, TL>;
+  using S = PassShape<F, TL, V>;
   constexpr int E = S::E, K1 = S::K1, K2 = S::K2, NE = 1 << E, H = NE / 2;
   extern __shared__ gf128 tile[];
   const int lane_groups = (1 << log_lanes) / TL;
@@ -192,24 +199,28 @@ std::vector<hf::F> host_twiddles(int d) {
 std::mutex g_tw_mu;
 std::map<std::pair<int, int>, void*> g_tw;  // (device, log_d) -> device table
 
-constexpr int kMaxPassLayers = 2 * NTT_POS_LOG < 8 ? 2 * NTT_POS_LOG : 8;
-
-template <int F, bool PREP>
+template <int F, bool PREP, int V>
 int launch_pass(gf128* dst, const gf128* src, size_t mask, const void* tw, int log_d, int log_lanes, int l0,
                 cudaStream_t st) {
-  if constexpr (F > kMaxPassLayers) {
+  if constexpr (F > variant_max_layers(V)) {
     return FLOCK_ERR_SHAPE;
   } else {
     size_t tiles = (size_t)1 << (log_d - F);
     if (log_lanes >= 4) {
-      using S = PassShape<F, 16>;
+      using S = PassShape<F, 16, V>;
       size_t blocks = tiles * ((1 << log_lanes) / 16);
-      ntt_pass_kernel<F, 16, PREP>
+      if constexpr (S::SMEM > 48 * 1024) {
+        flock_once_per_device((const void*)ntt_pass_kernel<F, 16, PREP, V>, [] {
+          cudaFuncSetAttribute(ntt_pass_kernel<F, 16, PREP, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               PassShape<F, 16, V>::SMEM);
+        });
+      }
+      ntt_pass_kernel<F, 16, PREP, V>
           <<<(unsigned)blocks, S::THREADS, S::SMEM, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
     } else {
-      using S = PassShape<F, 8>;
+      using S = PassShape<F, 8, V>;
       size_t blocks = tiles * ((1 << log_lanes) / 8);
-      ntt_pass_kernel<F, 8, PREP>
+      ntt_pass_kernel<F, 8, PREP, V>
           <<<(unsigned)blocks, S::THREADS, S::SMEM, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
     }
     flock_count_launch();
@@ -217,40 +228,51 @@ int launch_pass(gf128* dst, const gf128* src, size_t mask, const void* tw, int l
   }
 }
 
-// Raises the dynamic shared-memory limit of the passes that need more than
-// the default 48 KB (8 layers with 16 lanes: 64 KB), once per device.
-void ntt_set_smem_attrs() {
-  if constexpr (kMaxPassLayers >= 8) {
-    flock_once_per_device((const void*)ntt_pass_kernel<kMaxPassLayers, 16, true>, [] {
-      cudaFuncSetAttribute(ntt_pass_kernel<kMaxPassLayers, 16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           PassShape<kMaxPassLayers, 16>::SMEM);
-      cudaFuncSetAttribute(ntt_pass_kernel<kMaxPassLayers, 16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           PassShape<kMaxPassLayers, 16>::SMEM);
-    });
-  }
-}
-
-template <bool PREP>
-int run_pass_t(int f, gf128* dst, const gf128* src, size_t mask, const void* tw, int log_d, int log_lanes, int l0,
+template <bool PREP, int V>
+int run_pass_v(int f, gf128* dst, const gf128* src, size_t mask, const void* tw, int log_d, int log_lanes, int l0,
                cudaStream_t st) {
-  ntt_set_smem_attrs();
   switch (f) {
-    case 1: return launch_pass<1, PREP>(dst, src, mask, tw, log_d, log_lanes, l0, st);
-    case 2: return launch_pass<2, PREP>(dst, src, mask, tw, log_d, log_lanes, l0, st);
-    case 3: return launch_pass<3, PREP>(dst, src, mask, tw, log_d, log_lanes, l0, st);
-    case 4: return launch_pass<4, PREP>(dst, src, mask, tw, log_d, log_lanes, l0, st);
-    case 5: return launch_pass<5, PREP>(dst, src, mask, tw, log_d, log_lanes, l0, st);
-    case 6: return launch_pass<6, PREP>(dst, src, mask, tw, log_d, log_lanes, l0, st);
-    case 7: return launch_pass<7, PREP>(dst, src, mask, tw, log_d, log_lanes, l0, st);
-    case 8: return launch_pass<8, PREP>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 1: return launch_pass<1, PREP, V>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 2: return launch_pass<2, PREP, V>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 3: return launch_pass<3, PREP, V>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 4: return launch_pass<4, PREP, V>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 5: return launch_pass<5, PREP, V>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 6: return launch_pass<6, PREP, V>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 7: return launch_pass<7, PREP, V>(dst, src, mask, tw, log_d, log_lanes, l0, st);
+    case 8: return launch_pass<8, PREP, V>(dst, src, mask, tw, log_d, log_lanes, l0, st);
     default: return FLOCK_ERR_SHAPE;
   }
 }
 
+// The passes of layers [start_layer, log_d) with variant v: passes of at most
+// variant_max_layers(v) layers, split evenly. The first pass reads src with
+// the position mask; later passes work in place on dst.
+template <bool PREP>
+int run_passes(int v, gf128* dst, const gf128* src, size_t mask, const void* tw, int log_d, int log_lanes,
+               int start_layer, cudaStream_t st) {
+  const int max_f = variant_max_layers(v);
+  const int remaining = log_d - start_layer;
+  const int passes = (remaining + max_f - 1) / max_f;
+  int l = start_layer;
+  for (int q = 0; q < passes; q++) {
+    const int f = (remaining - (l - start_layer) + (passes - q) - 1) / (passes - q);
+    int rc = v == 0 ? run_pass_v<PREP, 0>(f, dst, src, mask, tw, log_d, log_lanes, l, st)
+           : v == 1 ? run_pass_v<PREP, 1>(f, dst, src, mask, tw, log_d, log_lanes, l, st)
+                    : run_pass_v<PREP, 2>(f, dst, src, mask, tw, log_d, log_lanes, l, st);
+    if (rc != FLOCK_OK) return rc;
+    src = dst;
+    mask = ~(size_t)0;
+    l += f;
+  }
+  return FLOCK_OK;
+}
+
+// Plain-twiddle pass of the default shape (the no-allocation entry point).
 int run_pass(int f, gf128* dst, const gf128* src, size_t mask, const gf128* tw, int log_d, int log_lanes, int l0,
              cudaStream_t st) {
-  return run_pass_t<false>(f, dst, src, mask, tw, log_d, log_lanes, l0, st);
+  return run_pass_v<false, kDefaultVariant>(f, dst, src, mask, tw, log_d, log_lanes, l0, st);
 }
+constexpr int kMaxPassLayers = variant_max_layers(kDefaultVariant);
 
 __global__ void prepare_twiddles_kernel(const gf128* __restrict__ tw, size_t n, gf128p* __restrict__ out) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -303,10 +325,91 @@ const void* flock_ntt_twiddles_prepared(int log_d) {
   return d;
 }
 
-// Applies layers [start_layer, log_d) in passes of up to 8 layers. d_src (may
-// equal d_data) holds the input rows addressed with position mask
-// 2^(log_d - start_layer) - 1, so a distinct d_src supplies the replicated
-// message of a rate-1/2^start_layer code.
+// ---- pass-shape autotuner -----------------------------------------------
+//
+// Per (device, log_d, lanes, start layer), the first call times every pass
+// variant on a scratch buffer of the same shape (two runs each, CUDA events
+// on the caller's stream) and keeps the fastest for later calls. The variants
+// compute identical results; only speed differs. FLOCK_NTT_TUNE=0 in the
+// environment turns tuning off (the default variant everywhere).
+namespace {
+
+struct TuneKey {
+  int dev, log_d, log_lanes, start;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(dev, log_d, log_lanes, start) < std::tie(o.dev, o.log_d, o.log_lanes, o.start);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, int> g_tuned;
+
+bool tuning_enabled() {
+  const char* e = std::getenv("FLOCK_NTT_TUNE");
+  return !(e && e[0] == '0');
+}
+
+int tune_variant(const TuneKey& k, const void* tw, cudaStream_t st) {
+  const size_t bytes = ((size_t)16 << k.log_lanes) << k.log_d;
+  void* scratch = nullptr;
+  if (cudaMalloc(&scratch, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return kDefaultVariant;
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int best = kDefaultVariant;
+  float best_ms = 1e30f;
+  gf128* d = (gf128*)scratch;
+  cudaMemsetAsync(scratch, 0, bytes, st);
+  for (int v = 0; v < kVariants; v++) {
+    if (run_passes<true>(v, d, d, ~(size_t)0, tw, k.log_d, k.log_lanes, k.start, st) != FLOCK_OK) continue;
+    cudaEventRecord(e0, st);
+    bool ok = true;
+    for (int rep = 0; rep < 2 && ok; rep++)
+      ok = run_passes<true>(v, d, d, ~(size_t)0, tw, k.log_d, k.log_lanes, k.start, st) == FLOCK_OK;
+    cudaEventRecord(e1, st);
+    float ms = 0;
+    if (ok && cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess &&
+        ms < best_ms) {
+      best_ms = ms;
+      best = v;
+    }
+  }
+  cudaStreamSynchronize(st);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(scratch);
+  return best;
+}
+
+int pick_variant(int log_d, int log_lanes, int start, const void* tw, cudaStream_t st) {
+  if (!tuning_enabled()) return kDefaultVariant;
+  TuneKey k{0, log_d, log_lanes, start};
+  cudaGetDevice(&k.dev);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(k);
+    if (it != g_tuned.end()) return it->second;
+  }
+  const int v = tune_variant(k, tw, st);
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tuned[k] = v;
+  return v;
+}
+
+}  // namespace
+
+extern "C" int flock_ntt_tuned_variant(int device, int log_d, int log_lanes, int start_layer) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tuned.find(TuneKey{device, log_d, log_lanes, start_layer});
+  return it == g_tuned.end() ? -1 : it->second;
+}
+
+// Applies layers [start_layer, log_d) in passes whose shape the autotuner
+// chose. d_src (may equal d_data) holds the input rows addressed with
+// position mask 2^(log_d - start_layer) - 1, so a distinct d_src supplies the
+// replicated message of a rate-1/2^start_layer code.
 int flock_launch_ntt(void* d_data, const void* d_src, int log_d, int log_lanes, int start_layer,
                      cudaStream_t stream) {
   if (log_lanes < 3 || log_lanes > 10 || log_d < 1 || log_d > 30 || start_layer < 0 || start_layer > log_d)
@@ -327,18 +430,8 @@ int flock_launch_ntt(void* d_data, const void* d_src, int log_d, int log_lanes, 
     }
     return FLOCK_OK;
   }
-  int remaining = log_d - start_layer;
-  int passes = (remaining + kMaxPassLayers - 1) / kMaxPassLayers;
-  int l = start_layer;
-  for (int q = 0; q < passes; q++) {
-    int f = (remaining - (l - start_layer) + (passes - q) - 1) / (passes - q);
-    int rc = run_pass_t<true>(f, data, src, mask, tw, log_d, log_lanes, l, stream);
-    if (rc != FLOCK_OK) return rc;
-    src = data;
-    mask = ~(size_t)0;
-    l += f;
-  }
-  return FLOCK_OK;
+  const int v = pick_variant(log_d, log_lanes, start_layer, tw, stream);
+  return run_passes<true>(v, data, src, mask, tw, log_d, log_lanes, start_layer, stream);
 }
 
 // ---- NTT without device allocation -----------------------------------------

@@ -80,6 +80,13 @@ int flock_witness(const flock_compression* d_in, size_t n, int n_blocks_log, voi
  * (crates/flock-core/src/ntt/additive_ntt_f128.rs:599-622). */
 int flock_ntt(flock_ctx* ctx, void* d_data, int log_d, int log_num_ntts, int start_layer, void* stream);
 
+/* Pass shape (0, 1, 2: 4, 8 or 16 positions per thread) the NTT autotuner
+ * chose for a transform shape on `device`, or -1 if that shape has not run
+ * yet. The first flock_ntt / commit / proof of a shape times the shapes on a
+ * scratch buffer and keeps the fastest; FLOCK_NTT_TUNE=0 in the environment
+ * disables tuning. No reference counterpart. */
+int flock_ntt_tuned_variant(int device, int log_d, int log_lanes, int start_layer);
+
 /* Largest log_d flock_ntt_noalloc accepts (2^16 positions per transform). */
 #define FLOCK_NTT_NOALLOC_MAX_LOG_D 16
 

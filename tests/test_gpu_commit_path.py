@@ -89,3 +89,23 @@ def test_rate_quarter_256_columns_4k_leaves_matches_oracle(ctx, rows_log):
     assert np.array_equal(host(cw).view(np.uint64), ocw)
     assert np.array_equal(host(tree).reshape(-1, 32), otree)
     assert root == oroot
+
+
+def test_ntt_autotuner_records_a_shape_and_keeps_results(ctx, monkeypatch):
+    import ctypes
+    L = F.lib()
+    L.flock_ntt_tuned_variant.argtypes = [ctypes.c_int] * 4
+    rng = np.random.default_rng(5)
+    data = rng.integers(0, 2**63, (1 << (15 + 4)) * 2, dtype=np.uint64)
+    ref = O.ntt_interleaved(data, 16, 1)
+    d = to_dev(data)
+    F.ntt(ctx, d, 15, 4, 1)
+    assert L.flock_ntt_tuned_variant(0, 15, 4, 1) in (0, 1, 2)
+    assert np.array_equal(host(d).view(np.uint64), ref)
+    # tuning off: the default shape, same result, nothing recorded
+    monkeypatch.setenv("FLOCK_NTT_TUNE", "0")
+    data2 = rng.integers(0, 2**63, (1 << (14 + 4)) * 2, dtype=np.uint64)
+    d2 = to_dev(data2)
+    F.ntt(ctx, d2, 14, 4, 1)
+    assert L.flock_ntt_tuned_variant(0, 14, 4, 1) == -1
+    assert np.array_equal(host(d2).view(np.uint64), O.ntt_interleaved(data2, 16, 1))
