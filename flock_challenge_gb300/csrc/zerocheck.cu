@@ -340,6 +340,10 @@ __global__ void eq_split_kernel(const gf128* __restrict__ r, int lo_bits, int hi
 // eq[j] = eq_lo[j & lo_mask] * eq_hi[j >> lo_bits]: the inner sums run over
 // eq_lo only and are multiplied by eq_hi once per CTA row block.
 constexpr int RND_THREADS = 256;
+#ifndef ZC_UNROLL
+#define ZC_UNROLL 1
+#endif
+constexpr int kZcUnroll = ZC_UNROLL;
 #ifndef ZC_RND_MIN_BLOCKS
 #define ZC_RND_MIN_BLOCKS 2  // two resident blocks per SM (128 registers) measured best
 #endif
@@ -355,6 +359,7 @@ zc_round_kernel(const gf128* __restrict__ A, const gf128* __restrict__ B, size_t
     gf256 l1 = {{0, 0, 0, 0}}, li = {{0, 0, 0, 0}};
     size_t base = h * lo_n;
     size_t end = base + lo_n < n_pairs ? base + lo_n : n_pairs;
+#pragma unroll kZcUnroll
     for (size_t j = base + threadIdx.x; j < end; j += RND_THREADS) {
       gf128 a0, a1, b0, b1;
       if (bind) {
