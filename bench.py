@@ -285,6 +285,12 @@ def run_gpu(args):
             setup.prove_seed(1000 * rank + i)
         torch.cuda.synchronize()
         seed_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    # every timed proof checked by the device-accelerated verifier (outside the timer)
+    t0 = time.perf_counter()
+    verified = F.verify(first, ctx=setup.ctx) and F.verify(second, ctx=setup.ctx)
+    verify_ms = (time.perf_counter() - t0) * 1e3 / 2
+    if not verified:
+        raise SystemExit("a timed proof was rejected by flock_verify")
     peaks, src = load_peaks()
     roof = kernel_roofline(F, setup.ctx.handle, None, log2, peaks, torch, dev)
     roof["peak_source"] = src
@@ -308,6 +314,8 @@ def run_gpu(args):
             "e2e_seed_to_proof": {"value": job_throughput(n, ws, seed_ms), "unit": "compressions/s",
                                   "h2d_bytes_per_step": 8, "d2h_bytes_per_step": len(first),
                                   "note": "seed in, inputs generated on the device, proof bytes out"},
+            "verify": {"impl": "flock_verify (host transcript + device kernels)", "ms_per_proof": verify_ms,
+                       "accepted": verified, "note": "the timed steps alternate two inputs; both proofs verified"},
             "gpu_launches": int(launches),
             "roofline": roof,
             "clocks": clk.summary(),

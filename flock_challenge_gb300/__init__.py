@@ -167,6 +167,8 @@ def _proto_lib():
         L.flock_server_reserved_bytes.restype = ctypes.c_size_t
         L.flock_prove_batch.argtypes = [P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_uint32), u64p, P,
                                         ctypes.c_size_t, szp]
+        L.flock_verify.argtypes = [P, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_int)]
+        L.flock_verify_batch.argtypes = [P, ctypes.c_size_t, ctypes.POINTER(P), szp, ctypes.POINTER(ctypes.c_int)]
         L._proto_ready = True
     return L
 
@@ -230,6 +232,10 @@ class Blake3Setup:
     def prove_device(self, d_blocks):
         """Proof of n_blocks records already in device memory (uint8 CUDA tensor)."""
         return self._call(_proto_lib().flock_prove_device, ctypes.c_void_p(d_blocks.data_ptr()), self.n_blocks)
+
+    def verify(self, proof):
+        """True when `proof` (bundle bytes) verifies (flock_verify, on this context's GPU)."""
+        return verify(proof, ctx=self.ctx)
 
     def stream_handle(self):
         """cudaStream_t the prover launches on (for event timing)."""
@@ -349,3 +355,37 @@ class Server:
             proofs.append(out[off:off + lens[i]].tobytes())
             off += lens[i]
         return proofs
+
+
+_VERIFY_CTX = {}
+
+
+def verify(proof, ctx=None, device=0):
+    """flock_verify: True when the serialized proof bundle verifies.
+
+    Mirrors verifier::verify_ligerito on R1csProofBundleLigerito::from_bytes
+    (crates/flock-core/src/verifier.rs, crates/flock-prover/src/proof_io.rs)."""
+    if ctx is None:
+        ctx = _VERIFY_CTX.get(device)
+        if ctx is None:
+            ctx = _VERIFY_CTX[device] = Context(device)
+    buf = np.frombuffer(bytes(proof), np.uint8)
+    ok = ctypes.c_int()
+    check(_proto_lib().flock_verify(ctx.handle, buf.ctypes.data_as(ctypes.c_void_p), buf.size, ctypes.byref(ok)),
+          "flock_verify")
+    return bool(ok.value)
+
+
+def verify_batch(proofs, ctx=None, device=0):
+    """flock_verify_batch over a list of proof bundles: a list of booleans."""
+    if ctx is None:
+        ctx = _VERIFY_CTX.get(device)
+        if ctx is None:
+            ctx = _VERIFY_CTX[device] = Context(device)
+    bufs = [np.frombuffer(bytes(p), np.uint8) for p in proofs]
+    n = len(bufs)
+    ptrs = (ctypes.c_void_p * n)(*[b.ctypes.data for b in bufs])
+    lens = (ctypes.c_size_t * n)(*[b.size for b in bufs])
+    acc = (ctypes.c_int * n)()
+    check(_proto_lib().flock_verify_batch(ctx.handle, n, ptrs, lens, acc), "flock_verify_batch")
+    return [bool(a) for a in acc]

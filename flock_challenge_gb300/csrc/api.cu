@@ -160,6 +160,24 @@ int flock_prove_seed(flock_ctx* ctx, uint32_t log2_size, uint64_t seed, uint8_t*
   return FLOCK_OK;
 }
 
+int flock_verify(flock_ctx* ctx, const uint8_t* proof, size_t len, int* accepted) {
+  if (!ctx || (!proof && len) || !accepted) return FLOCK_ERR_ARG;
+  if (!ctx->prover) {
+    ctx->prover = flock_prover_create(ctx->device);
+    if (!ctx->prover) return FLOCK_ERR_CUDA;
+  }
+  return flock_prover_verify(ctx->prover, proof, len, accepted, nullptr);
+}
+
+int flock_verify_batch(flock_ctx* ctx, size_t count, const uint8_t* const* proofs, const size_t* lens, int* accepted) {
+  if (!ctx || (count && (!proofs || !lens || !accepted))) return FLOCK_ERR_ARG;
+  for (size_t i = 0; i < count; i++) {
+    int rc = flock_verify(ctx, proofs[i], lens[i], &accepted[i]);
+    if (rc != FLOCK_OK) return rc;
+  }
+  return FLOCK_OK;
+}
+
 void* flock_stream(flock_ctx* ctx) {
   if (!ctx) return nullptr;
   if (!ctx->prover) ctx->prover = flock_prover_create(ctx->device);

@@ -68,6 +68,7 @@ int flock_launch_gather_nodes(const void* tree, const uint32_t* idx, int n, void
 int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, cudaStream_t st, uint64_t* nonce);
 
 // Launch counter of this library's kernels (read through flock_kernel_launches).
+int flock_launch_fold_lsb(const void* in, size_t n_out, const uint64_t r[2], void* out, cudaStream_t st);
 void flock_count_launch();
 // Runs fn once per (current device, key), under a lock, so no thread passes
 // before the first caller's fn has finished: per-device one-time work such as

@@ -140,6 +140,15 @@ basis_kernel(const gf128* __restrict__ LO, const gf128* __restrict__ HI, int nq,
   }
 }
 
+// out[j] = in[2j] + r (in[2j] + in[2j+1]): one LSB fold (ligerito.rs:1673-1691).
+__global__ void fold_lsb_kernel(const gf128* __restrict__ in, size_t n_out, const __grid_constant__ gf128p r,
+                                gf128* __restrict__ out) {
+  for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < n_out; j += (size_t)gridDim.x * blockDim.x) {
+    const gf128 x0 = in[2 * j], x1 = in[2 * j + 1];
+    out[j] = gf_add(x0, gf_mul_p(gf_add(x0, x1), r));
+  }
+}
+
 __global__ void gather_rows_kernel(const gf128* __restrict__ mat, const uint32_t* __restrict__ rows, int n_rows,
                                    int width, gf128* __restrict__ out) {
   size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -223,5 +232,12 @@ int flock_launch_gather_rows(const void* mat, const uint32_t* rows, int n_rows, 
 int flock_launch_gather_nodes(const void* tree, const uint32_t* idx, int n, void* out, cudaStream_t st) {
   if (n == 0) return FLOCK_OK;
   gather_nodes_kernel<<<(2 * n + 255) / 256, 256, 0, st>>>((const uint4*)tree, idx, n, (uint4*)out); flock_count_launch();
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_launch_fold_lsb(const void* in, size_t n_out, const uint64_t r[2], void* out, cudaStream_t st) {
+  fold_lsb_kernel<<<grid_for(n_out, 256, 152 * 8), 256, 0, st>>>((const gf128*)in, n_out, gf_prepare(to_gf(r)),
+                                                                 (gf128*)out);
+  flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }

@@ -8,6 +8,7 @@
 // kernels of this library; the host keeps the Fiat-Shamir transcript and the
 // O(1)-sized algebra between rounds (Lagrange weights, 64/128-entry vectors).
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cstring>
 #include <mutex>
@@ -935,5 +936,644 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     return f.code;
   } catch (const std::bad_alloc&) {
     return FLOCK_ERR_OOM;
+  }
+}
+
+// ============================================================================
+// Verifier (crates/flock-core/src/verifier.rs verify_ligerito, with
+// R1csProofBundleLigerito::from_bytes, proof_io.rs:161-208): the transcript
+// replay, the sumcheck checks, Merkle openings and proof-of-work checks run on
+// the host; the parts that are linear in the witness size run on the device
+// with the prover's kernels: the lincheck matrix fold A^T eq, B^T eq (lc_comb),
+// the ring-switch combined basis (2^(m-7) positions) and its LSB folds down to
+// the final Ligerito residual.
+// ============================================================================
+namespace {
+
+struct Reader {
+  const uint8_t* p;
+  size_t n, off = 0;
+  bool ok = true;
+  bool take(void* dst, size_t k) {
+    if (!ok || k > n - off) return ok = false;
+    memcpy(dst, p + off, k);
+    off += k;
+    return true;
+  }
+  uint64_t u64() {
+    uint64_t v = 0;
+    take(&v, 8);
+    return v;
+  }
+  uint32_t u32() {
+    uint32_t v = 0;
+    take(&v, 4);
+    return v;
+  }
+  F f() {
+    F v;
+    v.lo = u64();
+    v.hi = u64();
+    return v;
+  }
+  // length-prefixed F128 vector with an upper bound on the length
+  std::vector<F> fv(size_t max_len) {
+    uint64_t k = u64();
+    if (!ok || k > max_len || k * 16 > n - off) {
+      ok = false;
+      return {};
+    }
+    std::vector<F> v(k);
+    take(v.data(), 16 * k);
+    return v;
+  }
+  std::vector<std::pair<F, F>> pv(size_t max_len) {
+    uint64_t k = u64();
+    if (!ok || k > max_len || k * 32 > n - off) {
+      ok = false;
+      return {};
+    }
+    std::vector<std::pair<F, F>> v(k);
+    for (auto& e : v) {
+      e.first = f();
+      e.second = f();
+    }
+    return v;
+  }
+  std::vector<uint64_t> u64v(size_t max_len) {
+    uint64_t k = u64();
+    if (!ok || k > max_len || k * 8 > n - off) {
+      ok = false;
+      return {};
+    }
+    std::vector<uint64_t> v(k);
+    take(v.data(), 8 * k);
+    return v;
+  }
+};
+
+struct VOpen {
+  std::vector<std::vector<F>> rows;
+  std::vector<std::array<uint8_t, 32>> nodes;
+};
+bool read_open(Reader& r, VOpen& o) {
+  uint64_t nq = r.u64();
+  if (!r.ok || nq > (1u << 20)) return r.ok = false;
+  o.rows.resize(nq);
+  for (auto& row : o.rows) row = r.fv(1 << 12);
+  uint64_t nn = r.u64();
+  if (!r.ok || nn > (1u << 24) || nn * 32 > r.n - r.off) return r.ok = false;
+  o.nodes.resize(nn);
+  for (auto& h : o.nodes) r.take(h.data(), 32);
+  return r.ok;
+}
+
+using H32 = std::array<uint8_t, 32>;
+H32 cv_bytes(const uint32_t w[8]) {
+  H32 h;
+  memcpy(h.data(), w, 32);  // little-endian words
+  return h;
+}
+// Non-root chaining value of a single-chunk leaf (<= 1024 bytes): blocks with
+// counter 0, CHUNK_START on the first, CHUNK_END on the last (merkle.rs:200-210).
+H32 leaf_cv(const uint8_t* d, size_t len) {
+  uint32_t cv[8];
+  memcpy(cv, hb3::IV, 32);
+  size_t nb = len == 0 ? 1 : (len + 63) / 64;
+  for (size_t b = 0; b < nb; b++) {
+    size_t off = b * 64, bl = len - off < 64 ? len - off : 64;
+    uint32_t m[16], o[16];
+    hb3::load_words(d + off, bl, m);
+    uint32_t fl = (b == 0 ? hb3::CHUNK_START : 0) | (b + 1 == nb ? hb3::CHUNK_END : 0);
+    hb3::compress(cv, m, 0, (uint32_t)bl, fl, o);
+    memcpy(cv, o, 32);
+  }
+  return cv_bytes(cv);
+}
+H32 parent_cv(const H32& l, const H32& r) {
+  uint32_t m[16], o[16];
+  memcpy(m, l.data(), 32);
+  memcpy(m + 8, r.data(), 32);
+  hb3::compress(hb3::IV, m, 0, 64, hb3::PARENT, o);
+  return cv_bytes(o);
+}
+// Octopus multi-proof check (merkle.rs:937-1004).
+bool merkle_multi_ok(const H32& root, size_t n_leaves, const std::vector<uint32_t>& pos, std::vector<H32> leaves,
+                     const std::vector<H32>& proof) {
+  if (n_leaves == 0 || (n_leaves & (n_leaves - 1)) || pos.size() != leaves.size()) return false;
+  if (pos.empty()) return proof.empty();
+  for (size_t i = 0; i < pos.size(); i++)
+    if (pos[i] >= n_leaves || (i && pos[i - 1] >= pos[i])) return false;
+  if (n_leaves == 1) return proof.empty() && leaves[0] == root;
+  std::vector<std::pair<size_t, H32>> act;
+  for (size_t i = 0; i < pos.size(); i++) act.push_back({pos[i], leaves[i]});
+  size_t pi = 0;
+  for (size_t ll = n_leaves; ll > 1; ll >>= 1) {
+    std::vector<std::pair<size_t, H32>> nxt;
+    for (size_t i = 0; i < act.size();) {
+      size_t p = act[i].first;
+      H32 l, r;
+      if (i + 1 < act.size() && act[i + 1].first == (p ^ 1)) {
+        l = act[i].second;
+        r = act[i + 1].second;
+        i += 2;
+      } else {
+        if (pi >= proof.size()) return false;
+        const H32& sb = proof[pi++];
+        if (p & 1) { l = sb; r = act[i].second; }
+        else { l = act[i].second; r = sb; }
+        i += 1;
+      }
+      nxt.push_back({p >> 1, parent_cv(l, r)});
+    }
+    act.swap(nxt);
+  }
+  return pi == proof.size() && act.size() == 1 && act[0].second == root;
+}
+
+// Proof of work (challenger.rs:1246-1310): BLAKE3(digest || nonce_le || 0^24)
+// as one root block has >= bits leading zero bits, MSB first from byte 0.
+bool pow_ok(fs::Transcript& tr, uint64_t nonce, uint32_t bits) {
+  uint8_t dg[32];
+  tr.digest(dg);
+  uint8_t blk[64] = {0};
+  memcpy(blk, dg, 32);
+  memcpy(blk + 32, &nonce, 8);
+  uint32_t m[16], o[16];
+  hb3::load_words(blk, 64, m);
+  hb3::compress(hb3::IV, m, 0, 64, hb3::CHUNK_START | hb3::CHUNK_END | hb3::ROOT, o);
+  uint8_t h[32];
+  memcpy(h, o, 32);
+  uint32_t left = bits;
+  for (int k = 0; k < 32 && left; k++) {
+    if (left >= 8) {
+      if (h[k]) return false;
+      left -= 8;
+    } else {
+      if (h[k] >> (8 - left)) return false;
+      left = 0;
+    }
+  }
+  tr.absorb_nonce(nonce);
+  return true;
+}
+
+struct Quad {
+  F c, b, a;
+  static Quad from(F u0, F u2, F t) { return {u0, t + u2, u2}; }
+  F eval(F r) const { return c + r * b + r * r * a; }
+  static Quad fold(const Quad& p, const Quad& q, F al) { return {p.c + al * q.c, p.b + al * q.b, p.a + al * q.a}; }
+};
+
+// Lagrange weights at z over all 128 nodes phi8(0..127), for the nodes
+// 64..127 (multilinear.rs:522-548): the interpolant that vanishes on S.
+std::vector<F> combined_weights(F z) {
+  static const std::vector<F> den_inv = [] {
+    std::vector<F> d(64);
+    for (int i = 0; i < 64; i++) {
+      F si = hf::phi8((uint8_t)(64 + i)), den = F::one();
+      for (int j = 0; j < 128; j++)
+        if (j != 64 + i) den = den * (si + hf::phi8((uint8_t)j));
+      d[i] = hf::inv(den);
+    }
+    return d;
+  }();
+  std::vector<F> pre(129);
+  pre[0] = F::one();
+  for (int j = 0; j < 128; j++) pre[j + 1] = pre[j] * (z + hf::phi8((uint8_t)j));
+  std::vector<F> w(64);
+  F suf = F::one();
+  std::vector<F> sufs(129);
+  sufs[128] = F::one();
+  for (int j = 127; j >= 0; j--) sufs[j] = sufs[j + 1] * (z + hf::phi8((uint8_t)j));
+  for (int i = 0; i < 64; i++) w[i] = pre[64 + i] * sufs[65 + i] * den_inv[i];
+  (void)suf;
+  return w;
+}
+
+void bind_top(std::vector<F>& v, F r) {
+  size_t half = v.size() / 2;
+  for (size_t i = 0; i < half; i++) v[i] = v[i] + r * (v[i + half] + v[i]);
+  v.resize(half);
+}
+
+std::vector<F> what_at(int n, const Sks& sk, uint32_t q) {
+  std::vector<F> w(n);
+  if (n == 0) return w;
+  w[0] = F(q, 0);
+  for (int i = 1; i < n; i++) w[i] = w[i - 1] * w[i - 1] + sk.s[i - 1] * w[i - 1];
+  for (int i = 0; i < n; i++) w[i] = w[i] * sk.inv[i];
+  return w;
+}
+
+// MLE of the induced basis at ris ++ bits(y) (ligerito.rs:1879-1987).
+std::vector<F> induced_residual(int n, const std::vector<uint32_t>& q, const std::vector<F>& alpha, const F* ris,
+                                int prefix, int yr_log) {
+  const Sks& sk = sks_for(n);
+  auto at = eq_table(alpha);
+  std::vector<F> out((size_t)1 << yr_log);
+  for (size_t i = 0; i < q.size(); i++) {
+    auto w = what_at(n, sk, q[i]);
+    F pre = F::one();
+    for (int k = 0; k < prefix; k++) pre = pre * (F::one() + ris[k] * (F::one() + w[k]));
+    F c = at[i] * pre;
+    for (size_t y = 0; y < out.size(); y++) {
+      F suf = c;
+      for (int j = 0; j < yr_log; j++)
+        if ((y >> j) & 1) suf = suf * w[prefix + j];
+      out[y] += suf;
+    }
+  }
+  return out;
+}
+
+}  // namespace
+
+int flock_prover_verify(ProverState* S, const uint8_t* data, size_t len, int* accepted, std::string* why) {
+  *accepted = 0;
+  auto reject = [&](const char* w) {
+    if (why) *why = w;
+    return FLOCK_OK;
+  };
+  try {
+    CK(cudaSetDevice(S->device));
+    CK(cudaStreamSynchronize(S->st));
+    S->pin_off = 0;
+    cudaStream_t st = S->st;
+    Reader rd{data, len};
+    char magic[5];
+    uint8_t ver[2];
+    rd.take(magic, 5);
+    rd.take(ver, 2);
+    if (!rd.ok || memcmp(magic, "FLOCK", 5) != 0 || ver[0] != 4 || ver[1] != 2) return reject("header");
+    H32 root0;
+    rd.take(root0.data(), 32);
+    const uint64_t m64 = rd.u64(), rate0 = rd.u64(), lbs = rd.u64();
+    const uint32_t profile = rd.u32(), hash_kind = rd.u32();
+    if (!rd.ok || rate0 != 1 || lbs != 6 || profile != 0 || hash_kind != 1 || m64 < 22 || m64 > 35)
+      return reject("params");
+    const int m = (int)m64;
+    LigCfg cfg;
+    if (!lig_config(m, 0, cfg)) return reject("params");
+    // zerocheck proof
+    auto p_ab = rd.fv(64), p_c = rd.fv(64);
+    auto zc_rounds = rd.pv(64);
+    F fa = rd.f(), fb = rd.f(), final_c = rd.f();
+    // lincheck proof
+    auto lc_rounds = rd.pv(64);
+    auto z_partial = rd.fv(64);
+    // ring switch
+    uint64_t n_claims = rd.u64();
+    auto sh0 = rd.fv(128), sh1 = rd.fv(128);
+    // ligerito
+    H32 init_root;
+    rd.take(init_root.data(), 32);
+    VOpen open0;
+    read_open(rd, open0);
+    std::vector<H32> roots(rd.u64());
+    if (!rd.ok || roots.size() > 64) return reject("decode");
+    for (auto& h : roots) rd.take(h.data(), 32);
+    std::vector<VOpen> rec((size_t)rd.u64());
+    if (!rd.ok || rec.size() > 64) return reject("decode");
+    for (auto& o : rec) read_open(rd, o);
+    auto yr = rd.fv((size_t)1 << 20);
+    VOpen final_open;
+    read_open(rd, final_open);
+    auto msgs = rd.pv(1 << 12);
+    auto grind_nonces = rd.u64v(64);
+    auto ood_vals = rd.fv(64);
+    auto fold_nonces = rd.u64v(1 << 10);
+    if (!rd.ok || rd.off != len) return reject("decode");
+    if (p_ab.size() != 64 || p_c.size() != 64 || (int)zc_rounds.size() != m - 6 || lc_rounds.size() != 8 ||
+        z_partial.size() != 64 || n_claims != 2 || sh0.size() != 128 || sh1.size() != 128)
+      return reject("shape");
+
+    uint8_t digest[32];
+    flock_statement_digest(m, digest);
+    fs::Transcript tr("flock-bench-v0");
+    tr.label("flock-r1cs-v0");
+    tr.observe_bytes(digest, 32);
+    tr.observe_bytes(root0.data(), 32);
+    const Lagrange& LG = lagrange();
+
+    // ---- zerocheck (zerocheck.rs:1365-1517) ----
+    tr.label("flock-zerocheck-v0");
+    std::vector<F> r(m);
+    {
+      auto rs = tr.sample_vec(6);
+      auto ro = tr.sample_vec(m - 13);
+      for (int i = 0; i < 6; i++) r[i] = rs[i];
+      for (int i = 0; i < 3; i++) r[6 + i] = hf::phi8(zc::SMALL_CHAL[i]);
+      for (int i = 0; i < 4; i++) {
+        F g(1ULL << (1 << i), 0);
+        r[9 + i] = g * hf::inv(F::one() + g);
+      }
+      for (int i = 13; i < m; i++) r[i] = ro[i - 13];
+    }
+    tr.observe_slice(p_ab.data(), 64);
+    tr.observe_slice(p_c.data(), 64);
+    const F z = tr.sample();
+    {
+      auto wl = LG.at(z, 1);
+      if (dot(wl.data(), p_c.data(), 64) != final_c) return reject("zerocheck c-eval");
+    }
+    F running;
+    {
+      auto cw = combined_weights(z);
+      auto wl = LG.at(z, 1);
+      for (int i = 0; i < 64; i++) running += cw[i] * (p_ab[i] + p_c[i]) + wl[i] * p_c[i];
+    }
+    std::vector<F> rho;
+    for (int i = 0; i < m - 6; i++) {
+      F req = r[6 + i], g1 = zc_rounds[i].first, gi = zc_rounds[i].second;
+      F g0 = (running + req * g1) * hf::inv(F::one() + req);
+      tr.observe(g1);
+      tr.observe(gi);
+      F pch = tr.sample();
+      rho.push_back(pch);
+      F op = F::one() + pch;
+      running = g0 * op + g1 * pch + gi * pch * op;
+    }
+    if (running != fa * fb) return reject("zerocheck sumcheck final");
+    tr.observe(fa);
+    tr.observe(fb);
+
+    // ---- lincheck (lincheck.rs:1480-1660) ----
+    const int inner_rest = 14 - 6;
+    std::vector<F> x_in(rho.begin(), rho.begin() + inner_rest), x_out(rho.begin() + inner_rest, rho.end());
+    tr.label("flock-lincheck-v0");
+    F alpha = tr.sample();
+    F beta = tr.sample();
+    std::vector<F> comb(FLOCK_K);
+    {
+      if (!S->csc_ready) {
+        const HostCsc& c = flock_host_csc();
+        h2d(*S, S->csc_ap.get(c.a_ptr.size() * 4), c.a_ptr.data(), c.a_ptr.size() * 4);
+        h2d(*S, S->csc_ai.get(c.a_idx.size() * 4), c.a_idx.data(), c.a_idx.size() * 4);
+        h2d(*S, S->csc_bp.get(c.b_ptr.size() * 4), c.b_ptr.data(), c.b_ptr.size() * 4);
+        h2d(*S, S->csc_bi.get(c.b_idx.size() * 4), c.b_idx.data(), c.b_idx.size() * 4);
+        CK(cudaStreamSynchronize(st));
+        S->csc_ready = true;
+      }
+      auto lag_z = LG.at(z, 0);
+      void* dlag = S->lag.get(64 * 16);
+      h2d(*S, dlag, lag_z.data(), 64 * 16);
+      void* dxr = S->small.get(inner_rest * 16);
+      h2d(*S, dxr, x_in.data(), inner_rest * 16);
+      void* deqin = S->eqin.get(FLOCK_K * 16);
+      FK(flock_launch_lc_quirky_eq(dlag, dxr, inner_rest, deqin, st));
+      void* dcomb = S->comb.get(FLOCK_K * 16);
+      uint64_t al[2], be[2];
+      u2(alpha, al);
+      u2(beta, be);
+      FK(flock_launch_lc_comb((const uint32_t*)S->csc_ap.p, (const uint32_t*)S->csc_ai.p, (const uint32_t*)S->csc_bp.p,
+                              (const uint32_t*)S->csc_bi.p, deqin, al, be, 512, dcomb, st));
+      d2h(*S, comb.data(), dcomb, FLOCK_K * 16);
+    }
+    running = alpha * fa + fb + beta;
+    std::vector<F> rr;
+    for (auto& rdm : lc_rounds) {
+      tr.observe(rdm.first);
+      tr.observe(rdm.second);
+      F x = tr.sample();
+      F e0 = running + rdm.first;
+      F c1 = e0 + rdm.first + rdm.second;
+      running = rdm.second * x * x + c1 * x + e0;
+      bind_top(comb, x);
+      rr.push_back(x);
+    }
+    tr.observe_slice(z_partial.data(), 64);
+    if (dot(comb.data(), z_partial.data(), 64) != running) return reject("lincheck final");
+    const F r_inner_skip = tr.sample();
+    F lc_w;
+    {
+      auto l2 = LG.at(r_inner_skip, 0);
+      lc_w = dot(l2.data(), z_partial.data(), 64);
+    }
+    std::vector<F> r_inner_rest(rr.rbegin(), rr.rend());
+
+    // ---- ring switch of [ab, c] (ring_switch.rs:2708-3345, pcs.rs:1025-1110) ----
+    tr.label("flock-pcs-open-batch-v0");
+    std::vector<F> x_ab(r_inner_rest);
+    x_ab.insert(x_ab.end(), x_out.begin(), x_out.end());
+    std::vector<F> x_c(r.begin() + 6, r.end());
+    const std::vector<F>* xs[2] = {&x_ab, &x_c};
+    const std::vector<F>* shs[2] = {&sh0, &sh1};
+    const F zsk[2] = {r_inner_skip, z}, val[2] = {lc_w, final_c};
+    DBuf* tlo[2] = {&S->tlo0, &S->tlo1};
+    DBuf* thi[2] = {&S->thi0, &S->thi1};
+    std::vector<F> eqr[2];
+    F claims[2];
+    const int L = m - 7;
+    const int rs_lo = std::min(13, L - 1);
+    for (int k = 0; k < 2; k++) {
+      tr.label("flock-ring-switch-v0");
+      tr.observe_slice(shs[k]->data(), 128);
+      auto Ls = LG.at(zsk[k], 0);
+      F x0 = (*xs[k])[0], acc;
+      for (int i = 0; i < 128; i++) acc += Ls[i & 63] * ((i >> 6) & 1 ? x0 : F::one() + x0) * (*shs[k])[i];
+      if (acc != val[k]) return reject("ring switch claim");
+      auto rpp = tr.sample_vec(7);
+      eqr[k] = eq_table(rpp);
+      auto u = transpose128(*shs[k]);
+      claims[k] = dot(u.data(), eqr[k].data(), 128);
+      std::vector<F> suffix(xs[k]->begin() + 1, xs[k]->end());
+      eq_split_dev(*S, suffix, rs_lo, *tlo[k], *thi[k]);
+    }
+    F gam[2] = {tr.sample(), tr.sample()};
+    F target = gam[0] * claims[0] + gam[1] * claims[1];
+    const size_t n128 = (size_t)1 << L;
+    void* dbc = S->bc.get(n128 * 16);
+    {
+      std::vector<F> wk(2 * 128);
+      for (int k = 0; k < 2; k++)
+        for (int bb = 0; bb < 128; bb++) wk[k * 128 + bb] = gam[k] * eqr[k][bb];
+      void* dt = S->tables.get(wk.size() * 16);
+      h2d(*S, dt, wk.data(), wk.size() * 16);
+      FK(flock_launch_combined_basis(n128, S->tlo0.p, S->thi0.p, S->tlo1.p, S->thi1.p, rs_lo, dt, dbc, st));
+    }
+
+    // ---- Ligerito (ligerito.rs:6981-8544) ----
+    if (init_root != root0) return reject("ligerito root");
+    tr.label("flock-ligerito-basis-v0");
+    tr.observe(target);
+    tr.observe_bytes(root0.data(), 32);
+    const int log_n = L, k0 = cfg.initial_k, R = cfg.steps;
+    const size_t block0 = (size_t)1 << (log_n - k0 + cfg.rates[0]);
+    F t_r = target;
+    size_t tx = 0, fni = 0, oi = 0, ni = 0, rp = 0;
+    std::pair<F, F> msg;
+    auto next_msg = [&]() {
+      if (tx >= msgs.size()) return false;
+      msg = msgs[tx++];
+      tr.observe(msg.first);
+      tr.observe(msg.second);
+      return true;
+    };
+    auto fold_pow = [&](int lvl, int j) -> bool {
+      int bits = cfg.fold_bits[lvl] - j;
+      if (bits <= 0) return true;
+      return fni < fold_nonces.size() && pow_ok(tr, fold_nonces[fni++], (uint32_t)bits);
+    };
+    auto opens_ok = [&](const H32& root, size_t block_len, const std::vector<uint32_t>& q, const VOpen& o,
+                        size_t width) {
+      if (q.size() != o.rows.size()) return false;
+      std::vector<H32> leaves;
+      for (auto& row : o.rows) {
+        if (row.size() != width) return false;
+        leaves.push_back(leaf_cv((const uint8_t*)row.data(), row.size() * 16));
+      }
+      std::vector<H32> nodes(o.nodes.begin(), o.nodes.end());
+      return merkle_multi_ok(root, block_len, q, leaves, nodes);
+    };
+    auto enforced = [&](const VOpen& o, const std::vector<F>& v, const std::vector<F>& a) {
+      auto eqv = eq_table(v);
+      auto at = eq_table(a);
+      F sum;
+      for (size_t i = 0; i < o.rows.size(); i++) sum += at[i] * dot(o.rows[i].data(), eqv.data(), o.rows[i].size());
+      return sum;
+    };
+    struct OodCtx { std::vector<F> z; size_t start; F beta; };
+    struct LvlCtx { int n; std::vector<uint32_t> q; std::vector<F> alpha; size_t start; F beta; };
+    std::vector<OodCtx> oods;
+    std::vector<LvlCtx> lvls;
+    std::vector<F> ris;
+    if (!next_msg()) return reject("ligerito transcript");
+    Quad run = Quad::from(msg.first, msg.second, t_r);
+    for (int j = 0; j < k0; j++) {
+      if (!fold_pow(0, j)) return reject("ligerito fold pow");
+      F x = tr.sample();
+      ris.push_back(x);
+      t_r = run.eval(x);
+      if (!next_msg()) return reject("ligerito transcript");
+      run = Quad::from(msg.first, msg.second, t_r);
+    }
+    if (roots.empty()) return reject("ligerito roots");
+    H32 prev_root = roots[0];
+    tr.observe_bytes(prev_root.data(), 32);
+    const int n1 = log_n - k0;
+    auto do_ood = [&](int count, int nv, size_t start) -> bool {
+      for (int o = 0; o < count; o++) {
+        auto zp = tr.sample_vec(nv);
+        if (oi >= ood_vals.size()) return false;
+        F y = ood_vals[oi++];
+        tr.observe(y);
+        if (!next_msg()) return false;
+        Quad iq = Quad::from(msg.first, msg.second, y);
+        F bt = tr.sample();
+        run = Quad::fold(run, iq, bt);
+        t_r += bt * y;
+        oods.push_back({zp, start, bt});
+      }
+      return true;
+    };
+    if (!do_ood(cfg.ood[1], n1, (size_t)k0)) return reject("ligerito ood");
+    if (ni >= grind_nonces.size() || !pow_ok(tr, grind_nonces[ni++], (uint32_t)cfg.grind_bits[0]))
+      return reject("ligerito query pow");
+    auto q0 = sample_queries(tr, block0, cfg.queries[0]);
+    auto a0 = tr.sample_vec(ilog2(cfg.queries[0]));
+    if (!opens_ok(init_root, block0, q0, open0, (size_t)1 << k0)) return reject("ligerito L0 opens");
+    {
+      F es0 = enforced(open0, ris, a0);
+      if (!next_msg()) return reject("ligerito transcript");
+      Quad iq = Quad::from(msg.first, msg.second, es0);
+      F bt = tr.sample();
+      run = Quad::fold(run, iq, bt);
+      t_r += bt * es0;
+      lvls.push_back({n1, q0, a0, (size_t)k0, bt});
+    }
+    int prev_lni = cfg.ks[0], prev_lmc = n1 - prev_lni, prev_rate = cfg.rates[1];
+    int n_cur = n1;
+    for (int i = 0; i < R; i++) {
+      const int ki = cfg.ks[i];
+      std::vector<F> level_rs;
+      for (int j = 0; j < ki; j++) {
+        if (!fold_pow(i + 1, j)) return reject("ligerito fold pow");
+        F x = tr.sample();
+        ris.push_back(x);
+        level_rs.push_back(x);
+        t_r = run.eval(x);
+        if (!next_msg()) return reject("ligerito transcript");
+        run = Quad::from(msg.first, msg.second, t_r);
+      }
+      n_cur -= ki;
+      const size_t pbl = (size_t)1 << (prev_lmc + prev_rate);
+      if (i == R - 1) {
+        if (tx != msgs.size() || oi != ood_vals.size() || fni != fold_nonces.size()) return reject("ligerito trailing");
+        if (yr.size() != ((size_t)1 << n_cur)) return reject("ligerito yr size");
+        for (auto& v : yr) tr.observe(v);
+        if (ni >= grind_nonces.size() || !pow_ok(tr, grind_nonces[ni], (uint32_t)cfg.grind_bits[i + 1]))
+          return reject("ligerito last query pow");
+        auto ql = sample_queries(tr, pbl, cfg.queries[i + 1]);
+        auto alv = tr.sample_vec(ilog2(cfg.queries[i + 1]));
+        if (!opens_ok(prev_root, pbl, ql, final_open, (size_t)1 << prev_lni)) return reject("ligerito last opens");
+        F esl = enforced(final_open, level_rs, alv);
+        F bl = tr.sample();
+        t_r += bl * esl;
+        lvls.push_back({n_cur, ql, alv, ris.size(), bl});
+        const int yl = n_cur;
+        // dense residual of the combined basis: LSB folds at every r on the device
+        std::vector<F> bres((size_t)1 << yl);
+        {
+          void* cur = dbc;
+          void* alt = S->f1.get(n128 / 2 * 16);
+          void* alt2 = S->b1.get(n128 / 2 * 16);
+          size_t nlen = n128;
+          if (((size_t)1 << (yl + ris.size())) != n128) return reject("ligerito residual size");
+          for (size_t t = 0; t < ris.size(); t++) {
+            uint64_t rp2[2];
+            u2(ris[t], rp2);
+            void* dst = (cur == alt) ? alt2 : alt;
+            FK(flock_launch_fold_lsb(cur, nlen / 2, rp2, dst, st));
+            cur = dst;
+            nlen /= 2;
+          }
+          d2h(*S, bres.data(), cur, bres.size() * 16);
+        }
+        std::vector<F> cy(bres);
+        for (auto& c : lvls) {
+          auto ind = induced_residual(c.n, c.q, c.alpha, ris.data() + c.start, c.n - yl, yl);
+          for (size_t y = 0; y < cy.size(); y++) cy[y] += c.beta * ind[y];
+        }
+        for (auto& c : oods) {
+          int folded = (int)c.z.size() - yl;
+          F sc = c.beta;
+          for (int b2 = 0; b2 < folded; b2++) sc = sc * (F::one() + c.z[b2] + ris[c.start + b2]);
+          std::vector<F> tail(c.z.begin() + folded, c.z.end());
+          auto t = eq_table(tail);
+          for (size_t y = 0; y < cy.size(); y++) cy[y] += sc * t[y];
+        }
+        F inner = dot(yr.data(), cy.data(), cy.size());
+        if (inner != t_r) return reject("ligerito residual check");
+        *accepted = 1;
+        if (why) *why = "ok";
+        return FLOCK_OK;
+      }
+      if ((size_t)(i + 1) >= roots.size()) return reject("ligerito roots");
+      H32 root_next = roots[i + 1];
+      tr.observe_bytes(root_next.data(), 32);
+      if (!do_ood(cfg.ood[i + 2], n_cur, ris.size())) return reject("ligerito ood");
+      if (ni >= grind_nonces.size() || !pow_ok(tr, grind_nonces[ni++], (uint32_t)cfg.grind_bits[i + 1]))
+        return reject("ligerito query pow");
+      auto qi = sample_queries(tr, pbl, cfg.queries[i + 1]);
+      auto ai = tr.sample_vec(ilog2(cfg.queries[i + 1]));
+      if (rp >= rec.size()) return reject("ligerito openings");
+      const VOpen& lo = rec[rp++];
+      if (!opens_ok(prev_root, pbl, qi, lo, (size_t)1 << prev_lni)) return reject("ligerito level opens");
+      F esi = enforced(lo, level_rs, ai);
+      if (!next_msg()) return reject("ligerito transcript");
+      Quad iq = Quad::from(msg.first, msg.second, esi);
+      F bt = tr.sample();
+      run = Quad::fold(run, iq, bt);
+      t_r += bt * esi;
+      lvls.push_back({n_cur, qi, ai, ris.size(), bt});
+      prev_root = root_next;
+      prev_lni = cfg.ks[i + 1];
+      prev_lmc = n_cur - prev_lni;
+      prev_rate = cfg.rates[i + 2];
+    }
+    return reject("ligerito steps");
+  } catch (const Fail& f) {
+    return f.code;
   }
 }

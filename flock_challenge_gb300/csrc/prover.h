@@ -29,3 +29,9 @@ size_t flock_prover_reserved_bytes(const ProverState* s);
 // Frees the state's device buffers (after its stream is idle); the next proof
 // allocates them again.
 void flock_prover_trim(ProverState* s);
+// Verifies a serialized proof bundle (host transcript and checks, device
+// kernels for the witness-size parts); *accepted = 1 when it verifies, `why`
+// (optional) names the failed check. Returns a CUDA error code only when the
+// device work fails.
+#include <string>
+int flock_prover_verify(ProverState* s, const uint8_t* data, size_t len, int* accepted, std::string* why);

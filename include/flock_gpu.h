@@ -160,6 +160,24 @@ void* flock_stream(flock_ctx* ctx);
  * FLOCK_PHASE_TIMING prints, crates/flock-prover/src/prover.rs:958-1216). */
 int flock_last_phase_times(const flock_ctx* ctx, double* ms, int n);
 
+/* ---- Verification -------------------------------------------------------- */
+
+/* Verifies a serialized proof bundle: *accepted = 1 if it is a valid proof of
+ * its statement (the batch-of-BLAKE3-compressions R1CS of its m), 0
+ * otherwise (malformed bytes included). The transcript replay and the
+ * sumcheck, Merkle and proof-of-work checks run on the host; the lincheck
+ * matrix fold, the ring-switch combined basis and the Ligerito residual run
+ * on the device. Replaces R1csProofBundleLigerito::from_bytes +
+ * verifier::verify_ligerito (crates/flock-prover/src/proof_io.rs:161-208,
+ * crates/flock-core/src/verifier.rs). */
+int flock_verify(flock_ctx* ctx, const uint8_t* proof, size_t len, int* accepted);
+
+/* flock_verify over count proofs (accepted[i] per proof). The reference's
+ * verifier checks one bundle per call (benchmark-tools/harness verification
+ * of each trial). */
+int flock_verify_batch(flock_ctx* ctx, size_t count, const uint8_t* const* proofs, const size_t* lens,
+                       int* accepted);
+
 /* ---- Batched and served proving ---------------------------------------- */
 
 /* Device bytes one prover holds for a proof of 2^log2_size compressions (the
