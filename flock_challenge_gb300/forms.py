@@ -11,8 +11,9 @@ every batched proof must equal its plain proof byte for byte.
 Served form: requests with sizes log-uniform in 2^10..2^20 arrive as a
 Poisson process at each swept rate; the server admits them by device-memory
 budget and overlaps their work. Reported per rate: p50/p99 latency (submit to
-proof ready), sustained compressions/s, and that every served proof equals the
-plain proof of the same request.
+proof ready), sustained compressions/s, that every served proof equals the
+plain proof of the same request (sizes up to 2^16), and that every served
+proof verifies (flock_verify_batch, with its throughput).
 """
 import argparse
 import json
@@ -22,7 +23,7 @@ import time
 
 import numpy as np
 
-from . import Blake3Setup, Server, footprint_bytes
+from . import Blake3Setup, Server, footprint_bytes, verify_batch
 
 
 def log_uniform_sizes(n, lo, hi, seed):
@@ -58,9 +59,11 @@ def run_batched(count=64, workers=3, seed=20260, plain=None):
         got = srv.prove_batch(sizes, seeds)
         t_batch = time.perf_counter() - t
     same = all(a == b for a, b in zip(got, ref))
+    verified = all(verify_batch(got))
     return {"proofs": count, "sizes_log2": "log-uniform 12..18", "compressions": total, "workers": workers,
             "batched_compressions_per_s": total / t_batch, "plain_sequential_compressions_per_s": total / t_plain,
-            "speedup_vs_plain": t_plain / t_batch, "byte_identical_to_plain": same}
+            "speedup_vs_plain": t_plain / t_batch, "byte_identical_to_plain": same,
+            "all_verified": verified}
 
 
 def run_serving(rates=(4.0, 8.0), requests=60, workers=3, budget_gb=120, seed=777, plain=None):
@@ -110,11 +113,15 @@ def run_serving(rates=(4.0, 8.0), requests=60, workers=3, budget_gb=120, seed=77
         lats = np.array([lat[i] for i in ids])
         total = sum(1 << l for l in sizes)
         same = all(proofs[i] == plain.prove(l, s) for i, l, s in zip(ids, sizes, seeds) if l <= 16)
+        t = time.perf_counter()
+        verified = all(verify_batch([proofs[i] for i in ids]))
+        verify_s = time.perf_counter() - t
         out.append({"rate_per_s": rate, "requests": requests, "sizes_log2": "log-uniform 10..20",
                     "p50_ms": float(np.percentile(lats, 50)), "p99_ms": float(np.percentile(lats, 99)),
                     "sustained_compressions_per_s": total / wall, "offered_compressions_per_s": total / gaps.sum(),
                     "workers": workers, "hbm_budget_gb": budget_gb,
-                    "byte_identical_to_plain_(sizes_le_2^16)": same})
+                    "byte_identical_to_plain_(sizes_le_2^16)": same,
+                    "all_verified": verified, "verify_proofs_per_s": requests / verify_s})
     return out
 
 
