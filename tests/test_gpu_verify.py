@@ -63,3 +63,21 @@ def test_ranked_size_proof_verifies(cuda_device):
     b = bytearray(p)
     b[len(b) // 2] ^= 4
     assert not F.verify(bytes(b))
+
+
+def test_every_supported_size_proves_and_verifies(cuda_device):
+    """m = 22 .. 35 (2^8 .. 2^21 compressions): every Ligerito configuration."""
+    for log2 in range(8, 22):
+        p = F.Blake3Setup(1 << log2).prove_seed(1000 + log2)
+        assert F.verify(p), log2
+        assert len(p) < 500_000
+
+
+def test_ragged_large_input_verifies(cuda_device):
+    import torch
+    n = 100_000
+    d = F.generate_inputs(17, 5)
+    blocks = np.frombuffer(d.cpu().numpy().tobytes(), dtype=F.COMPRESSION_DTYPE)[:n].copy()
+    p = F.Blake3Setup(n).prove_fast(blocks)
+    assert F.verify(p)
+    torch.cuda.synchronize()
