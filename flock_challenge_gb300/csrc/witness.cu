@@ -50,7 +50,16 @@ __device__ __forceinline__ uint64_t transpose8x8(uint64_t x) {
 }
 
 // Writes the 16 staged words (global word index w0..w0+15) of all lanes.
-__device__ __noinline__ void flush(const WarpCtx& c, int w0) {
+// (Scalar arguments, so the call passes them in registers; the context
+// struct itself never has to live in memory.)
+__device__ __noinline__ void flush_words(uint64_t* sz, uint64_t* gz, uint64_t* ga, uint64_t* gb, uint8_t* stripe,
+                                        size_t warp_slot0, int n_valid, int lane, int w0) {
+  struct {
+    uint64_t *sz, *sa, *sb, *gz, *ga, *gb;
+    uint8_t* stripe;
+    size_t warp_slot0;
+    int n_valid, lane;
+  } c = {sz, sz + 32 * STAGE_STRIDE, sz + 64 * STAGE_STRIDE, gz, ga, gb, stripe, warp_slot0, n_valid, lane};
   __syncwarp();
   const int half = c.lane >> 4, j = c.lane & 15;
 #pragma unroll 4
@@ -105,7 +114,8 @@ struct Sink {
     c.sa[c.lane * STAGE_STRIDE + j] = a;
     c.sb[c.lane * STAGE_STRIDE + j] = b;
     word++;
-    if (word % STAGE_WORDS == 0) flush(c, word - STAGE_WORDS);
+    if (word % STAGE_WORDS == 0)
+      flush_words(c.sz, c.gz, c.ga, c.gb, c.stripe, c.warp_slot0, c.n_valid, c.lane, word - STAGE_WORDS);
   }
   // Appends `width` bits (values already masked to width).
   __device__ __forceinline__ void push(const WarpCtx& c, uint32_t z, uint32_t a, uint32_t b, int width) {
