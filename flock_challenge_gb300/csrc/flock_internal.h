@@ -27,8 +27,6 @@ struct ZcRound1Tables;
 int flock_launch_zc_round1(const void* a, const void* b, const void* c, size_t n_outer, const void* eq_out,
                            const ZcRound1Tables* d_tables, void* partials, int grid, cudaStream_t st);
 int flock_launch_reduce_rows(const void* in, size_t count, int width, void* out, cudaStream_t st);
-int flock_launch_fold_skip(const void* a, const void* b, size_t rows, const void* lag, void* out_a, void* out_b,
-                           cudaStream_t st);
 int flock_launch_eq_split(const void* r, int lo_bits, int hi_bits, void* lo, void* hi, cudaStream_t st);
 int flock_launch_zc_round(const void* A, const void* B, size_t n_pairs, int bind, const uint64_t rho[2], void* Aout,
                           void* Bout, const void* eq_lo, const void* eq_hi, int lo_bits, void* partials, int grid,
@@ -69,6 +67,9 @@ int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, cudaSt
 
 // Launch counter of this library's kernels (read through flock_kernel_launches).
 int flock_launch_fold_lsb(const void* in, size_t n_out, const uint64_t r[2], void* out, cudaStream_t st);
+int flock_launch_zc_round0_skip(const void* a, const void* b, size_t n_pairs, const void* lag, void* A0, void* B0,
+                                const void* eq_lo, const void* eq_hi, int lo_bits, void* partials, int grid,
+                                cudaStream_t st);
 void flock_count_launch();
 // Runs fn once per (current device, key), under a lock, so no thread passes
 // before the first caller's fn has finished: per-device one-time work such as

@@ -584,7 +584,6 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     void *dA1 = S->A1.get(rows0 / 2 * 16), *dB1 = S->B1.get(rows0 / 2 * 16);
     void* dlag = S->lag.get(64 * 16);
     h2d(*S, dlag, lag_z.data(), 64 * 16);
-    FK(flock_launch_fold_skip(da, db, rows0, dlag, dA0, dB0, st));
     const int n_mlv = m - 6;
     std::vector<std::pair<F, F>> zc_rounds;
     std::vector<F> rho;
@@ -600,7 +599,11 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       void* dpart = S->part.get((size_t)grid * 2 * 16);
       uint64_t rp[2] = {0, 0};
       if (i > 0) u2(rho.back(), rp);
-      FK(flock_launch_zc_round(curA, curB, n_pairs, i > 0, rp, nxtA, nxtB, S->eqlo.p, S->eqhi.p, lob, dpart, grid, st));
+      if (i == 0)  // skip fold (multilinear.rs:598-630) fused into round 0
+        FK(flock_launch_zc_round0_skip(da, db, n_pairs, dlag, dA0, dB0, S->eqlo.p, S->eqhi.p, lob, dpart, grid, st));
+      else
+        FK(flock_launch_zc_round(curA, curB, n_pairs, 1, rp, nxtA, nxtB, S->eqlo.p, S->eqhi.p, lob, dpart, grid,
+                                 st));
       if (i > 0) {
         std::swap(curA, nxtA);
         std::swap(curB, nxtB);

@@ -285,33 +285,6 @@ reduce_rows_kernel(const gf128* __restrict__ in, size_t count, int width, gf128*
   }
 }
 
-// Skip fold at z: out[x] = sum_s bit_s(W[x]) L_s(z), with 8 byte tables of the
-// 64 Lagrange weights (multilinear.rs:598-630).
-__global__ void __launch_bounds__(256)
-fold_skip_kernel(const uint64_t* __restrict__ W0, const uint64_t* __restrict__ W1, size_t rows,
-                 const gf128* __restrict__ lag, gf128* __restrict__ out0, gf128* __restrict__ out1) {
-  __shared__ gf128 tab[8 * 256];
-  for (int e = threadIdx.x; e < 8 * 256; e += blockDim.x) {
-    int c = e >> 8, v = e & 255;
-    gf128 acc = gf_zero();
-    for (int j = 0; j < 8; j++)
-      if ((v >> j) & 1) acc = gf_add(acc, lag[8 * c + j]);
-    tab[e] = acc;
-  }
-  __syncthreads();
-  for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < rows; x += (size_t)gridDim.x * blockDim.x) {
-    uint64_t a = W0[x], b = W1[x];
-    gf128 ra = gf_zero(), rb = gf_zero();
-#pragma unroll
-    for (int c = 0; c < 8; c++) {
-      ra = gf_add(ra, tab[c * 256 + ((a >> (8 * c)) & 255)]);
-      rb = gf_add(rb, tab[c * 256 + ((b >> (8 * c)) & 255)]);
-    }
-    out0[x] = ra;
-    out1[x] = rb;
-  }
-}
-
 // eq table split: lo[i] = prod_{k<lo_bits} f(r_k, bit k of i), hi[i] over the
 // next hi_bits variables; f(r, 1) = r, f(r, 0) = 1 + r.
 __global__ void eq_split_kernel(const gf128* __restrict__ r, int lo_bits, int hi_bits, gf128* __restrict__ lo,
@@ -401,6 +374,69 @@ zc_round_kernel(const gf128* __restrict__ A, const gf128* __restrict__ B, size_t
   }
 }
 
+// Round 0 fused with the skip fold: the tables A0, B0 (sum_s bit_s(W[x]) L_s(z),
+// eight byte tables of the 64 Lagrange weights) are computed from the bit rows
+// of a and b, written for round 1, and used at once for round 0's message
+// (G(1), G(inf) as in zc_round_kernel), so A0/B0 are never read back here and
+// the table lookups overlap the round's GF(2^128) products.
+__global__ void __launch_bounds__(RND_THREADS, ZC_RND_MIN_BLOCKS)
+zc_round0_skip_kernel(const uint64_t* __restrict__ W0, const uint64_t* __restrict__ W1, size_t n_pairs,
+                      const gf128* __restrict__ lag, gf128* __restrict__ A0, gf128* __restrict__ B0,
+                      const gf128* __restrict__ eq_lo, const gf128* __restrict__ eq_hi, int lo_bits,
+                      gf128* __restrict__ partials) {
+  extern __shared__ gf128 tab[];  // [8][256]
+  for (int e = threadIdx.x; e < 8 * 256; e += blockDim.x) {
+    int c = e >> 8, v = e & 255;
+    gf128 acc = gf_zero();
+    for (int j = 0; j < 8; j++)
+      if ((v >> j) & 1) acc = gf_add(acc, lag[8 * c + j]);
+    tab[e] = acc;
+  }
+  __syncthreads();
+  auto skip = [&](uint64_t w) {
+    gf128 r = gf_zero();
+#pragma unroll
+    for (int c = 0; c < 8; c++) r = gf_add(r, tab[c * 256 + ((w >> (8 * c)) & 255)]);
+    return r;
+  };
+  const size_t lo_n = (size_t)1 << lo_bits;
+  const size_t n_hi = (n_pairs + lo_n - 1) / lo_n;
+  gf256 g1 = {{0, 0, 0, 0}}, gi = {{0, 0, 0, 0}};
+  for (size_t h = blockIdx.x; h < n_hi; h += gridDim.x) {
+    gf256 l1 = {{0, 0, 0, 0}}, li = {{0, 0, 0, 0}};
+    size_t base = h * lo_n;
+    size_t end = base + lo_n < n_pairs ? base + lo_n : n_pairs;
+    for (size_t j = base + threadIdx.x; j < end; j += RND_THREADS) {
+      const uint64_t x0 = W0[2 * j], x1 = W0[2 * j + 1], y0 = W1[2 * j], y1 = W1[2 * j + 1];
+      const gf128 a0 = skip(x0), a1 = skip(x1), b0 = skip(y0), b1 = skip(y1);
+      A0[2 * j] = a0; A0[2 * j + 1] = a1;
+      B0[2 * j] = b0; B0[2 * j + 1] = b1;
+      const gf128 e = eq_lo[j - base];
+      gf256_acc(l1, gf_mul_wide(e, gf_mul(a1, b1)));
+      gf256_acc(li, gf_mul_wide(e, gf_mul(gf_add(a0, a1), gf_add(b0, b1))));
+    }
+    const gf128 eh = eq_hi[h];
+    gf256_acc(g1, gf_mul_wide(eh, gf256_reduce(l1)));
+    gf256_acc(gi, gf_mul_wide(eh, gf256_reduce(li)));
+  }
+  __shared__ gf256 red[2][RND_THREADS / 32];
+  for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      g1.r[k] ^= __shfl_xor_sync(0xffffffffu, g1.r[k], off);
+      gi.r[k] ^= __shfl_xor_sync(0xffffffffu, gi.r[k], off);
+    }
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { red[0][warp] = g1; red[1][warp] = gi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    gf256 s1 = {{0, 0, 0, 0}}, si = {{0, 0, 0, 0}};
+    for (int w = 0; w < RND_THREADS / 32; w++) { gf256_acc(s1, red[0][w]); gf256_acc(si, red[1][w]); }
+    partials[2 * blockIdx.x] = gf256_reduce(s1);
+    partials[2 * blockIdx.x + 1] = gf256_reduce(si);
+  }
+}
+
 // Final bind of the last round: out[j] = A0 + rho (A0 + A1).
 __global__ void bind_pairs_kernel(const gf128* __restrict__ A, const gf128* __restrict__ B, size_t n, gf128 rho,
                                   gf128* __restrict__ Aout, gf128* __restrict__ Bout) {
@@ -427,15 +463,6 @@ int flock_launch_zc_round1(const void* a, const void* b, const void* c, size_t n
 
 int flock_launch_reduce_rows(const void* in, size_t count, int width, void* out, cudaStream_t st) {
   reduce_rows_kernel<<<(width + 7) / 8, 256, 0, st>>>((const gf128*)in, count, width, (gf128*)out); flock_count_launch();
-  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
-}
-
-int flock_launch_fold_skip(const void* a, const void* b, size_t rows, const void* lag, void* out_a, void* out_b,
-                           cudaStream_t st) {
-  size_t grid = (rows + 255) / 256;
-  if (grid > 152 * 16) grid = 152 * 16;
-  fold_skip_kernel<<<(unsigned)grid, 256, 0, st>>>((const uint64_t*)a, (const uint64_t*)b, rows, (const gf128*)lag,
-                                                   (gf128*)out_a, (gf128*)out_b); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
@@ -467,5 +494,15 @@ int flock_launch_bind_pairs(const void* A, const void* B, size_t n, const uint64
   if (grid > 152 * 8) grid = 152 * 8;
   bind_pairs_kernel<<<(unsigned)grid, 256, 0, st>>>((const gf128*)A, (const gf128*)B, n, r, (gf128*)Aout,
                                                     (gf128*)Bout); flock_count_launch();
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_launch_zc_round0_skip(const void* a, const void* b, size_t n_pairs, const void* lag, void* A0, void* B0,
+                                const void* eq_lo, const void* eq_hi, int lo_bits, void* partials, int grid,
+                                cudaStream_t st) {
+  zc_round0_skip_kernel<<<grid, RND_THREADS, 8 * 256 * sizeof(gf128), st>>>(
+      (const uint64_t*)a, (const uint64_t*)b, n_pairs, (const gf128*)lag, (gf128*)A0, (gf128*)B0,
+      (const gf128*)eq_lo, (const gf128*)eq_hi, lo_bits, (gf128*)partials);
+  flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
