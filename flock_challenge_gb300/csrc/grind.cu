@@ -6,6 +6,8 @@
 // tests one nonce of a window and lowers a device minimum with atomicMin; the
 // host scans windows in increasing order and stops at the first window with a
 // hit, so the result is the global minimum.
+#include <cstring>
+
 #include "blake3.cuh"
 #include "flock_internal.h"
 
@@ -25,14 +27,18 @@ __device__ __forceinline__ bool leading_zeros_ok(const uint32_t h[8], uint32_t b
   return true;
 }
 
-__global__ void grind_kernel(const uint32_t* __restrict__ digest, uint64_t start, uint64_t count, uint32_t bits,
+struct Digest {
+  uint32_t w[8];
+};
+
+__global__ void grind_kernel(const __grid_constant__ Digest digest, uint64_t start, uint64_t count, uint32_t bits,
                              unsigned long long* __restrict__ best) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   uint64_t nonce = start + i;
   uint32_t m[16];
 #pragma unroll
-  for (int k = 0; k < 8; k++) m[k] = digest[k];
+  for (int k = 0; k < 8; k++) m[k] = digest.w[k];
   m[8] = (uint32_t)nonce;
   m[9] = (uint32_t)(nonce >> 32);
 #pragma unroll
@@ -46,18 +52,22 @@ __global__ void grind_kernel(const uint32_t* __restrict__ digest, uint64_t start
 
 }  // namespace
 
-// Returns the smallest satisfying nonce. d_scratch: >= 40 bytes of device memory.
-int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, cudaStream_t st, uint64_t* nonce) {
+// Returns the smallest satisfying nonce. d_scratch: >= 8 bytes of device
+// memory; h_best: 8 bytes of host memory the window result is read into
+// (pinned memory keeps the read cheap). The digest travels as a kernel
+// argument, so nothing is copied to the device.
+int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, uint64_t* h_best, cudaStream_t st,
+                uint64_t* nonce) {
   if (bits == 0) {
     *nonce = 0;
     return FLOCK_OK;
   }
   if (bits > 60) return FLOCK_ERR_SHAPE;
   unsigned long long* d_best = (unsigned long long*)d_scratch;
-  uint32_t* d_dig = (uint32_t*)((char*)d_scratch + 8);
+  Digest dg;
+  memcpy(dg.w, digest, 32);
   const unsigned long long none = ~0ull;
-  if (cudaMemcpyAsync(d_dig, digest, 32, cudaMemcpyHostToDevice, st) != cudaSuccess) return FLOCK_ERR_CUDA;
-  if (cudaMemcpyAsync(d_best, &none, 8, cudaMemcpyHostToDevice, st) != cudaSuccess) return FLOCK_ERR_CUDA;
+  if (cudaMemsetAsync(d_best, 0xFF, 8, st) != cudaSuccess) return FLOCK_ERR_CUDA;
   // About two expected hits per window: a miss costs one more window, an
   // oversized window wastes work on every grind (most grinds are 2..14 bits).
   int wlog = (int)bits + 1;
@@ -65,13 +75,13 @@ int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, cudaSt
   if (wlog > 26) wlog = 26;
   uint64_t window = (uint64_t)1 << wlog;
   for (uint64_t start = 0;; start += window) {
-    grind_kernel<<<(unsigned)((window + 255) / 256), 256, 0, st>>>(d_dig, start, window, bits, d_best); flock_count_launch();
+    grind_kernel<<<(unsigned)((window + 255) / 256), 256, 0, st>>>(dg, start, window, bits, d_best);
+    flock_count_launch();
     if (cudaGetLastError() != cudaSuccess) return FLOCK_ERR_CUDA;
-    unsigned long long best = 0;
-    if (cudaMemcpyAsync(&best, d_best, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess) return FLOCK_ERR_CUDA;
+    if (cudaMemcpyAsync(h_best, d_best, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess) return FLOCK_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return FLOCK_ERR_CUDA;
-    if (best != none) {
-      *nonce = best;
+    if (*h_best != none) {
+      *nonce = *h_best;
       return FLOCK_OK;
     }
     if (start > ((uint64_t)1 << 62)) return FLOCK_ERR_TIMEOUT;

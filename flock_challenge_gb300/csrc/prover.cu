@@ -756,7 +756,9 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       uint8_t dg[32];
       tr.digest(dg);
       uint64_t nonce = 0;
-      FK(flock_grind(dg, bits, dgr, st, &nonce));
+      uint64_t local_best = 0;
+      uint64_t* h_best = S->pin ? reinterpret_cast<uint64_t*>(S->pin + kPinH2D) : &local_best;
+      FK(flock_grind(dg, bits, dgr, h_best, st, &nonce));
       tr.absorb_nonce(nonce);
       return nonce;
     };
