@@ -331,7 +331,8 @@ const void* flock_ntt_twiddles_prepared(int log_d) {
 // variant on a scratch buffer of the same shape (two runs each, CUDA events
 // on the caller's stream) and keeps the fastest for later calls. The variants
 // compute identical results; only speed differs. FLOCK_NTT_TUNE=0 in the
-// environment turns tuning off (the default variant everywhere).
+// environment turns tuning off (the default variant everywhere);
+// FLOCK_NTT_VARIANT=0|1|2 fixes one shape.
 namespace {
 
 struct TuneKey {
@@ -384,6 +385,10 @@ int tune_variant(const TuneKey& k, const void* tw, cudaStream_t st) {
 }
 
 int pick_variant(int log_d, int log_lanes, int start, const void* tw, cudaStream_t st) {
+  if (const char* f = std::getenv("FLOCK_NTT_VARIANT")) {  // a fixed shape, for measurements
+    const int v = f[0] - '0';
+    if (v >= 0 && v < kVariants) return v;
+  }
   if (!tuning_enabled()) return kDefaultVariant;
   TuneKey k{0, log_d, log_lanes, start};
   cudaGetDevice(&k.dev);
