@@ -8,7 +8,7 @@
 // is formed from sixteen 32x32->64 integer multiplies of operands masked to
 // every fourth bit: with four-bit spacing each output position sums at most
 // eight partial bits, so the count never carries into the next position of
-// the same residue class, and masking the residue keeps exactly the parity.
+// the same residue class, and keeping the residue's bits keeps the parity.
 // 128x128 uses two levels of Karatsuba (nine 32-bit products) and the
 // reference's fold of the upper half (gf2_128.rs:192-216).
 #pragma once
@@ -45,17 +45,46 @@ __device__ __forceinline__ uint64_t mulw(uint32_t a, uint32_t b) {
   return r;
 }
 
-// 32x32 -> 64 carry-less product via masked integer multiplies.
-__device__ __forceinline__ uint64_t clmul32(uint32_t a, uint32_t b) {
+// 32x32 -> 64 unsigned multiply-add (one IMAD.WIDE.U32 with accumulator).
+__device__ __forceinline__ uint64_t madw(uint32_t a, uint32_t b, uint64_t c) {
+  uint64_t r;
+  asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(r) : "r"(a), "r"(b), "l"(c));
+  return r;
+}
+
+// (x & ~m) | (y & m): one 3-input logic op.
+__device__ __forceinline__ uint32_t bit_select(uint32_t x, uint32_t y, uint32_t m) { return (x & ~m) | (y & m); }
+
+// Combines the four residue-class partial products: class k keeps the bits at
+// positions = k (mod 4). Selecting per class (instead of masking each and
+// OR-ing) is three logic ops per 32-bit half.
+__device__ __forceinline__ uint64_t clmul_combine(uint64_t r0, uint64_t r1, uint64_t r2, uint64_t r3) {
+  const uint32_t m1 = 0x22222222u, m3 = 0x88888888u, m23 = 0xCCCCCCCCu;
+  const uint32_t lo = bit_select(bit_select((uint32_t)r0, (uint32_t)r1, m1), bit_select((uint32_t)r2, (uint32_t)r3, m3), m23);
+  const uint32_t hi = bit_select(bit_select((uint32_t)(r0 >> 32), (uint32_t)(r1 >> 32), m1),
+                                 bit_select((uint32_t)(r2 >> 32), (uint32_t)(r3 >> 32), m3), m23);
+  return ((uint64_t)hi << 32) | lo;
+}
+
+// 32x32 -> 64 carry-less product of a and the four masked parts (b0..b3) of b.
+// Products of operands masked to every fourth bit hold, at each position, the
+// count of its partial bits (at most 8), so the count's low bit is the XOR.
+// Two products whose counts sit in neighbouring columns of the same residue
+// class (offsets i + j and i + j + 4) sum to at most 15 per column, so such
+// pairs are added by the multiplier's accumulator instead of an XOR.
+__device__ __forceinline__ uint64_t clmul32_m(uint32_t a, uint32_t b0, uint32_t b1, uint32_t b2, uint32_t b3) {
   const uint32_t m0 = 0x11111111u, m1 = 0x22222222u, m2 = 0x44444444u, m3 = 0x88888888u;
-  uint32_t a0 = a & m0, a1 = a & m1, a2 = a & m2, a3 = a & m3;
-  uint32_t b0 = b & m0, b1 = b & m1, b2 = b & m2, b3 = b & m3;
-  uint64_t r0 = mulw(a0, b0) ^ mulw(a1, b3) ^ mulw(a2, b2) ^ mulw(a3, b1);
-  uint64_t r1 = mulw(a0, b1) ^ mulw(a1, b0) ^ mulw(a2, b3) ^ mulw(a3, b2);
-  uint64_t r2 = mulw(a0, b2) ^ mulw(a1, b1) ^ mulw(a2, b0) ^ mulw(a3, b3);
-  uint64_t r3 = mulw(a0, b3) ^ mulw(a1, b2) ^ mulw(a2, b1) ^ mulw(a3, b0);
-  return (r0 & 0x1111111111111111ull) | (r1 & 0x2222222222222222ull) | (r2 & 0x4444444444444444ull) |
-         (r3 & 0x8888888888888888ull);
+  const uint32_t a0 = a & m0, a1 = a & m1, a2 = a & m2, a3 = a & m3;
+  const uint64_t r0 = madw(a0, b0, mulw(a1, b3)) ^ mulw(a2, b2) ^ mulw(a3, b1);
+  const uint64_t r1 = madw(a0, b1, mulw(a2, b3)) ^ madw(a1, b0, mulw(a3, b2));
+  const uint64_t r2 = madw(a0, b2, mulw(a3, b3)) ^ mulw(a1, b1) ^ mulw(a2, b0);
+  const uint64_t r3 = mulw(a0, b3) ^ mulw(a1, b2) ^ mulw(a2, b1) ^ mulw(a3, b0);
+  return clmul_combine(r0, r1, r2, r3);
+}
+
+// 32x32 -> 64 carry-less product.
+__device__ __forceinline__ uint64_t clmul32(uint32_t a, uint32_t b) {
+  return clmul32_m(a, b & 0x11111111u, b & 0x22222222u, b & 0x44444444u, b & 0x88888888u);
 }
 
 // 64x64 -> 128 carry-less product (Karatsuba over 32-bit halves).
@@ -135,16 +164,7 @@ __host__ __device__ inline gf128p gf_prepare(gf128 b) {
   return p;
 }
 
-__device__ __forceinline__ uint64_t clmul32_p(uint32_t a, uint4 b) {
-  const uint32_t m0 = 0x11111111u, m1 = 0x22222222u, m2 = 0x44444444u, m3 = 0x88888888u;
-  uint32_t a0 = a & m0, a1 = a & m1, a2 = a & m2, a3 = a & m3;
-  uint64_t r0 = mulw(a0, b.x) ^ mulw(a1, b.w) ^ mulw(a2, b.z) ^ mulw(a3, b.y);
-  uint64_t r1 = mulw(a0, b.y) ^ mulw(a1, b.x) ^ mulw(a2, b.w) ^ mulw(a3, b.z);
-  uint64_t r2 = mulw(a0, b.z) ^ mulw(a1, b.y) ^ mulw(a2, b.x) ^ mulw(a3, b.w);
-  uint64_t r3 = mulw(a0, b.w) ^ mulw(a1, b.z) ^ mulw(a2, b.y) ^ mulw(a3, b.x);
-  return (r0 & 0x1111111111111111ull) | (r1 & 0x2222222222222222ull) | (r2 & 0x4444444444444444ull) |
-         (r3 & 0x8888888888888888ull);
-}
+__device__ __forceinline__ uint64_t clmul32_p(uint32_t a, uint4 b) { return clmul32_m(a, b.x, b.y, b.z, b.w); }
 
 __device__ __forceinline__ gf256 gf_mul_wide_p(gf128 a, const gf128p& p) {
   const uint32_t a0 = a.w[0], a1 = a.w[1], a2 = a.w[2], a3 = a.w[3];
