@@ -28,6 +28,10 @@
 namespace {
 
 constexpr int R1_THREADS = 384;
+#ifndef ZC1_PAR_UNROLL
+#define ZC1_PAR_UNROLL 1
+#endif
+constexpr int kZc1ParUnroll = ZC1_PAR_UNROLL;  // 1: one loop body for both row parities
 
 // 143-bit accumulator (five 32-bit words) for shifted table values.
 struct Acc5 {
@@ -159,9 +163,10 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
     for (int j = 0; j < 16; j++) t[j] = 0;
     if (live) {
       const size_t row0 = xo * 128 + (size_t)xm * 8;
+
 #pragma unroll 1
       for (int xs2 = 0; xs2 < 4; xs2++)
-#pragma unroll
+#pragma unroll kZc1ParUnroll
       for (int par = 0; par < 2; par++) {
         const int xs = 2 * xs2 + par;
         uint64_t ra = A[row0 + xs], rb = B[row0 + xs], rc = C[row0 + xs];
@@ -188,7 +193,9 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
         // bit j of the constant is set).
         const uint8_t* mm = T->e8_mat[xs];
         const uint8_t e8c = T->e8c[xs >> 1];
-        uint64_t* tt = t + 8 * par;
+        // c goes to the parity-par half of t; with the parity a runtime value
+        // (one loop body for both parities) the halves take rc or 0
+        const uint64_t c_even = par ? 0 : rc, c_odd = par ? rc : 0;
 #pragma unroll
         for (int j = 0; j < 8; j++) {
           uint64_t acc = 0;
@@ -196,7 +203,10 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
           for (int k = 0; k < 8; k++)
             if ((mm[j] >> k) & 1) acc ^= y[k];
           w[j] ^= acc;
-          if ((e8c >> j) & 1) tt[j] ^= rc;
+          if ((e8c >> j) & 1) {
+            t[j] ^= c_even;
+            t[8 + j] ^= c_odd;
+          }
         }
       }
     }
