@@ -135,10 +135,15 @@ ntt_pass_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t s
       ti[j] = i0 >> (F - t);
     }
     if constexpr (PREP) {
+      // Block 0 of every layer has twiddle 0 (the table's subset sums start
+      // at the empty sum; all other blocks are non-zero): its butterflies
+      // need no product. Blocks are uniform over a tile, so the test rarely
+      // diverges.
       const gf128p* twl = reinterpret_cast<const gf128p*>(tw_any) + twb;
+      const bool hi0 = hi == 0;
 #pragma unroll
       for (int j = 0; j < H; j++) {
-        y[j] = gf_add(y[j], gf_mul_p(y[j + H], gf_load_p(&twl[ti[j]])));
+        if (!(hi0 && ti[j] == 0)) y[j] = gf_add(y[j], gf_mul_p(y[j + H], gf_load_p(&twl[ti[j]])));
         y[j + H] = gf_add(y[j + H], y[j]);
       }
     } else {
