@@ -19,6 +19,8 @@ e2e:   the public C ABI with pinned host buffers (flock_prove): the 28 MB
   timer.
 Working set > 5 GB (1 GiB codeword, 0.5 GiB witness planes) >> 129 MB L2, so no
 explicit L2 flush is needed between steps.
+chain: the hash-chain proof of 2^18 linked compressions (flock_prove_chain),
+  median of 5, and its verification (flock_verify_chain).
 forms: the batched form (64 proofs of 2^12..2^18 through the proof server vs
   the same proofs in sequence) and the served form (Poisson arrivals of
   2^10..2^20 proofs, p50/p99 latency); see flock_challenge_gb300/forms.py.
@@ -214,6 +216,31 @@ def kernel_roofline(F, ctx_handle, stream_ptr, log2, peaks, torch, dev):
                     "see profiles/ntt_pass_l0_2e16.md for issue-slot and pipe utilisation"}
 
 
+def run_chain(F, setup, log2, reps=5):
+    """Hash-chain proof (flock_prove_chain, host inputs in, bundle bytes out) of
+    2^log2 linked compressions built as the flock_chain CLI builds them."""
+    import statistics
+    blocks = F.chain_inputs(1 << log2, 42)
+    first = setup.prove_chain(blocks)  # warm-up: the chain tables are allocated here
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        b = setup.prove_chain(blocks)
+        ts.append((time.perf_counter() - t0) * 1e3)
+        if b != first:
+            raise SystemExit("chain proof not deterministic")
+    t0 = time.perf_counter()
+    ok = F.verify_chain(first, ctx=setup.ctx)
+    v_ms = (time.perf_counter() - t0) * 1e3
+    if not ok:
+        raise SystemExit("a chain proof was rejected by flock_verify_chain")
+    ms = statistics.median(ts)
+    return {"workload": f"BLAKE3 chain of 2^{log2} compressions (flock_chain CLI inputs, domain flock_chain-cli)",
+            "impl": "flock_prove_chain, host inputs -> bundle bytes", "ms_per_proof": ms,
+            "compressions_per_s": (1 << log2) / (ms * 1e-3), "proof_bytes": len(first),
+            "verify_ms": v_ms, "accepted": ok, "reps": reps}
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -320,6 +347,8 @@ def run_gpu(args):
             "roofline": roof,
             "clocks": clk.summary(),
         }
+        if ws == 1:
+            line["chain"] = run_chain(F, setup, log2)
         line["cpu_baseline"] = oracle_baseline(budget_s=20.0, gpu_proof=first, gpu_m=14 + log2)
         if args.forms and ws == 1:
             from flock_challenge_gb300 import forms

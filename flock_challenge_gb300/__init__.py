@@ -169,6 +169,9 @@ def _proto_lib():
                                         ctypes.c_size_t, szp]
         L.flock_verify.argtypes = [P, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_int)]
         L.flock_verify_batch.argtypes = [P, ctypes.c_size_t, ctypes.POINTER(P), szp, ctypes.POINTER(ctypes.c_int)]
+        L.flock_prove_chain.argtypes = [P, P, ctypes.c_size_t, ctypes.c_char_p, P, ctypes.c_size_t, szp]
+        L.flock_verify_chain.argtypes = [P, P, ctypes.c_size_t, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
+        L.flock_chain_inputs.argtypes = [ctypes.c_size_t, ctypes.c_uint64, P, P]
         L._proto_ready = True
     return L
 
@@ -236,6 +239,20 @@ class Blake3Setup:
     def verify(self, proof):
         """True when `proof` (bundle bytes) verifies (flock_verify, on this context's GPU)."""
         return verify(proof, ctx=self.ctx)
+
+    def prove_chain(self, blocks, domain=None):
+        """Hash-chain proof of n_blocks = 2^k compressions whose cvs link
+        (Blake3Setup::prove_chain, crates/flock-prover/src/r1cs_hashes/blake3.rs:3785-3805):
+        the ChainProofBundleLigerito bytes, endpoints taken from the blocks."""
+        blocks = np.ascontiguousarray(blocks, dtype=COMPRESSION_DTYPE)
+        if len(blocks) != self.n_blocks or self.n_blocks != 1 << self.n_blocks_log:
+            raise ValueError("prove_chain needs exactly n_blocks = 2^k blocks")
+        return self._call(_proto_lib().flock_prove_chain, blocks.ctypes.data_as(ctypes.c_void_p), len(blocks),
+                          _domain_bytes(domain))
+
+    def verify_chain(self, bundle, domain=None):
+        """True when the chain bundle verifies (flock_verify_chain)."""
+        return verify_chain(bundle, domain, ctx=self.ctx)
 
     def stream_handle(self):
         """cudaStream_t the prover launches on (for event timing)."""
@@ -389,3 +406,33 @@ def verify_batch(proofs, ctx=None, device=0):
     acc = (ctypes.c_int * n)()
     check(_proto_lib().flock_verify_batch(ctx.handle, n, ptrs, lens, acc), "flock_verify_batch")
     return [bool(a) for a in acc]
+
+
+def _domain_bytes(domain):
+    return domain.encode() if isinstance(domain, str) else domain
+
+
+def verify_chain(bundle, domain=None, ctx=None, device=0):
+    """flock_verify_chain: True when the chain bundle verifies under `domain`
+    (None = "flock_chain-cli"); Blake3Setup::verify_chain on
+    ChainProofBundleLigerito::from_bytes (blake3.rs:3807-3830, proof_io.rs:494-497)."""
+    if ctx is None:
+        ctx = _VERIFY_CTX.get(device)
+        if ctx is None:
+            ctx = _VERIFY_CTX[device] = Context(device)
+    buf = np.frombuffer(bytes(bundle), np.uint8)
+    ok = ctypes.c_int()
+    check(_proto_lib().flock_verify_chain(ctx.handle, buf.ctypes.data_as(ctypes.c_void_p), buf.size,
+                                          _domain_bytes(domain),
+                                          ctypes.byref(ok)), "flock_verify_chain")
+    return bool(ok.value)
+
+
+def chain_inputs(steps, seed, cv0=None):
+    """Honest BLAKE3 chain as the flock_chain CLI builds it (host, sequential):
+    records whose cv is the previous record's compression output."""
+    out = np.zeros(steps, COMPRESSION_DTYPE)
+    c = None if cv0 is None else np.ascontiguousarray(cv0, dtype=np.uint32)
+    check(_proto_lib().flock_chain_inputs(steps, seed, None if c is None else c.ctypes.data_as(ctypes.c_void_p),
+                                          out.ctypes.data_as(ctypes.c_void_p)), "flock_chain_inputs")
+    return out

@@ -5,6 +5,7 @@
 
 #include "flock_internal.h"
 #include "prover.h"
+#include "host_blake3.h"
 #include "r1cs_setup.h"
 
 #include <atomic>
@@ -174,6 +175,68 @@ int flock_verify_batch(flock_ctx* ctx, size_t count, const uint8_t* const* proof
   for (size_t i = 0; i < count; i++) {
     int rc = flock_verify(ctx, proofs[i], lens[i], &accepted[i]);
     if (rc != FLOCK_OK) return rc;
+  }
+  return FLOCK_OK;
+}
+
+int flock_prove_chain(flock_ctx* ctx, const flock_compression* in, size_t n, const char* domain, uint8_t* out,
+                      size_t cap, size_t* len) {
+  if (!ctx || !len || !in) return FLOCK_ERR_ARG;
+  if (n < 256 || n > ((size_t)1 << 21) || (n & (n - 1))) return FLOCK_ERR_SHAPE;
+  int n_log = 0;
+  while (((size_t)1 << n_log) < n) n_log++;
+  if (ctx->hbm_budget && flock_footprint_bytes((uint32_t)n_log) > ctx->hbm_budget) return FLOCK_ERR_OOM;
+  if (!ctx->prover) {
+    ctx->prover = flock_prover_create(ctx->device);
+    if (!ctx->prover) return FLOCK_ERR_CUDA;
+  }
+  ChainReq req;
+  if (domain) req.domain = domain;
+  memcpy(req.cv0, in[0].cv, 32);
+  uint32_t o[16];
+  const flock_compression& l = in[n - 1];
+  hb3::compress(l.cv, l.m, l.counter, l.block_len, l.flags, o);
+  memcpy(req.cv_last, o, 32);
+  int rc = flock_prover_prove(ctx->prover, in, n, n_log, ctx->last_proof, false, &req);
+  if (rc != FLOCK_OK) return rc;
+  *len = ctx->last_proof.size();
+  if (!out || cap < ctx->last_proof.size()) return FLOCK_ERR_CAPACITY;
+  memcpy(out, ctx->last_proof.data(), ctx->last_proof.size());
+  return FLOCK_OK;
+}
+
+int flock_verify_chain(flock_ctx* ctx, const uint8_t* bundle, size_t len, const char* domain, int* accepted) {
+  if (!ctx || (!bundle && len) || !accepted) return FLOCK_ERR_ARG;
+  if (!ctx->prover) {
+    ctx->prover = flock_prover_create(ctx->device);
+    if (!ctx->prover) return FLOCK_ERR_CUDA;
+  }
+  return flock_prover_verify_chain(ctx->prover, bundle, len, domain, accepted, nullptr);
+}
+
+int flock_chain_inputs(size_t steps, uint64_t seed, const uint32_t* cv0, flock_compression* out) {
+  if (!out && steps) return FLOCK_ERR_ARG;
+  static const uint32_t kIV[8] = {0x6A09E667u, 0xBB67AE85u, 0x3C6EF372u, 0xA54FF53Au,
+                                  0x510E527Fu, 0x9B05688Cu, 0x1F83D9ABu, 0x5BE0CD19u};
+  uint32_t cv[8];
+  memcpy(cv, cv0 ? cv0 : kIV, 32);
+  uint64_t s = seed;
+  for (size_t i = 0; i < steps; i++) {
+    flock_compression& c = out[i];
+    memcpy(c.cv, cv, 32);
+    for (int j = 0; j < 16; j++) {
+      s += 0x9E3779B97F4A7C15ull;
+      uint64_t z = s;
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+      c.m[j] = (uint32_t)(z ^ (z >> 31));
+    }
+    c.counter = 0;
+    c.block_len = 64;
+    c.flags = 0;
+    uint32_t o[16];
+    hb3::compress(c.cv, c.m, 0, 64, 0, o);
+    memcpy(cv, o, 32);
   }
   return FLOCK_OK;
 }

@@ -77,5 +77,19 @@ void flock_count_launch();
 // raising a kernel's shared-memory limit.
 void flock_once_per_device(const void* key, void (*fn)());
 
+// Hash-chain relation (chain.cu). g = [in || out] region folds of n_inst
+// instances; W the shift-sumcheck weights; chain_round binds (bind != 0) the
+// 2h-entry tables at r and writes per-block (q(1), q(inf)) partials of the
+// h-entry tables; claim_basis adds c[p] eq(point, i) at word 128 i + p, p < 4.
+int flock_launch_chain_fold_io(const void* z, size_t n_inst, const uint64_t e0[2], const uint64_t e1[2], void* g,
+                               cudaStream_t st);
+int flock_launch_chain_weights(const void* lo, const void* hi, int lo_bits, size_t n_inst, const uint64_t alpha[2],
+                               void* W, cudaStream_t st);
+int flock_chain_round_grid(size_t h);
+int flock_launch_chain_round(void* W, void* g, size_t h, int bind, const uint64_t r[2], void* partials, int grid,
+                             cudaStream_t st);
+int flock_launch_chain_claim_basis(void* b, size_t n_inst, const void* lo, const void* hi, int lo_bits,
+                                   const uint64_t c[8], cudaStream_t st);
+
 // Benchmark inputs (inputs.cu): n records from SplitMix64 state `state0`.
 int flock_launch_gen_inputs(uint64_t state0, size_t n, void* d_out, cudaStream_t st);

@@ -282,7 +282,7 @@ struct ProverState {
   ZcRound1Tables* d_r1t = nullptr;
   DBuf in, z, a, b, stripe, cw, tree, A0, B0, A1, B1, eqlo, eqhi, eqout, rdev, part, red, lag, small, eqin, comb,
       zvec, zvec0, lcmsg, tlo0, thi0, tlo1, thi1, tables, bc, f1, b1, W, LO, HI, basis, qbuf, abuf, rows, nidx, nodes,
-      grind, lvl_cw[2], lvl_tree[2];
+      grind, lvl_cw[2], lvl_tree[2], chW, chG;
   DBuf csc_ap, csc_ai, csc_bp, csc_bi;
   bool csc_ready = false;
   FlockPhaseTimes times;
@@ -296,7 +296,7 @@ struct ProverState {
     return {&in, &z, &a, &b, &stripe, &cw, &tree, &A0, &B0, &A1, &B1, &eqlo, &eqhi, &eqout, &rdev, &part, &red,
             &lag, &small, &eqin, &comb, &zvec, &zvec0, &lcmsg, &tlo0, &thi0, &tlo1, &thi1, &tables, &bc, &f1, &b1,
             &W, &LO, &HI, &basis, &qbuf, &abuf, &rows, &nidx, &nodes, &grind, &lvl_cw[0], &lvl_cw[1],
-            &lvl_tree[0], &lvl_tree[1], &csc_ap, &csc_ai, &csc_bp, &csc_bi};
+            &lvl_tree[0], &lvl_tree[1], &chW, &chG, &csc_ap, &csc_ai, &csc_bp, &csc_bi};
   }
   std::vector<const DBuf*> bufs() const {
     auto v = const_cast<ProverState*>(this)->bufs();
@@ -457,7 +457,7 @@ int flock_prover_prove_seed(ProverState* S, int log2, uint64_t seed, std::vector
 }
 
 int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, int n_log, std::vector<uint8_t>& out,
-                       bool input_on_device) {
+                       bool input_on_device, const ChainReq* chain) {
   try {
     CK(cudaSetDevice(S->device));
     CK(cudaStreamSynchronize(S->st));  // the staging area of the previous proof is free again
@@ -466,6 +466,8 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     LigCfg cfg;
     if (!lig_config(m, 0, cfg)) return FLOCK_ERR_SHAPE;
     if (n > ((size_t)1 << n_log) || n_log < 8) return FLOCK_ERR_SHAPE;
+    // the chain shift relation covers every slot: the steps must fill 2^n_log
+    if (chain && n != ((size_t)1 << n_log)) return FLOCK_ERR_SHAPE;
     cudaStream_t st = S->st;
     FlockPhaseTimes& T = S->times;
     T = FlockPhaseTimes();
@@ -515,8 +517,9 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
 
     Wire w;
     w.raw("FLOCK", 5);
-    uint8_t ver[2] = {4, 2};
+    uint8_t ver[2] = {4, (uint8_t)(chain ? 3 : 2)};  // flavor 2 = R1CS, 3 = chain (proof_io.rs:8-13)
     w.raw(ver, 2);
+    if (chain) w.u32(0);  // HashKind::Blake3 of the chain bundle
     w.raw(root0, 32);
     w.u64(m);
     w.u64(rate0);
@@ -524,7 +527,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     w.u32(0);  // LigeritoProfile::Fast
     w.u32(1);  // HashKind::Blake3
 
-    fs::Transcript tr("flock-bench-v0");
+    fs::Transcript tr(chain ? chain->domain : "flock-bench-v0");
     // bind_statement (crates/flock-core/src/proof.rs:51-59)
     tr.label("flock-r1cs-v0");
     tr.observe_bytes(digest, 32);
@@ -693,6 +696,50 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     w.pv(lc_rounds);
     w.fv(z_partial);
 
+    // ---- chain: region fold and shift sumcheck (chain_common.rs:316-320, chain.rs:155-233) ----
+    std::vector<F> pd_inst;
+    F pd_tau, pd_sel0, pd_value;
+    if (chain) {
+      pd_tau = tr.sample_vec(1)[0];
+      const size_t N = (size_t)1 << n_log;
+      void* dW = S->chW.get(2 * N * 16);
+      void* dg = S->chG.get(2 * N * 16);
+      uint64_t e0[2], e1[2];
+      u2(F::one() + pd_tau, e0);
+      u2(pd_tau, e1);
+      FK(flock_launch_chain_fold_io(dz, N, e0, e1, dg, st));
+      auto tau = tr.sample_vec(n_log);
+      F al = tr.sample();
+      int lob = std::min(n_log, 12);
+      eq_split_dev(*S, tau, lob, S->eqlo, S->eqhi);
+      uint64_t alu[2];
+      u2(al, alu);
+      FK(flock_launch_chain_weights(S->eqlo.p, S->eqhi.p, lob, N, alu, dW, st));
+      std::vector<std::pair<F, F>> rounds;
+      std::vector<F> rs;
+      for (int k = 0; k <= n_log; k++) {
+        const size_t h = (2 * N) >> k;
+        int grid = flock_chain_round_grid(h);
+        void* dpart = S->part.get((size_t)grid * 2 * 16);
+        uint64_t rp[2] = {0, 0};
+        if (k > 0) u2(rs.back(), rp);
+        FK(flock_launch_chain_round(dW, dg, h, k > 0, rp, dpart, grid, st));
+        auto sm = reduce_partials(*S, dpart, grid, 2);
+        tr.observe(sm[0]);
+        tr.observe(sm[1]);
+        rounds.push_back({sm[0], sm[1]});
+        rs.push_back(tr.sample());
+      }
+      F g2[2];
+      d2h(*S, g2, dg, 32);
+      pd_value = g2[0] + rs.back() * (g2[1] + g2[0]);
+      // round k bound coordinate n - k: instance coordinates are rs[n..1], the selector rs[0]
+      pd_sel0 = rs[0];
+      pd_inst.assign(rs.rbegin(), rs.rend() - 1);
+      w.pv(rounds);
+      w.f(pd_value);
+    }
+
     // ---- PCS open: ring switch of [ab, c] (pcs.rs:1025-1110) ----
     tr.label("flock-pcs-open-batch-v0");
     std::vector<F> x_ab(r_inner_rest);
@@ -738,6 +785,19 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       void* dt = S->tables.get(wk.size() * 16);
       h2d(*S, dt, wk.data(), wk.size() * 16);
       FK(flock_launch_combined_basis(n128, S->tlo0.p, S->thi0.p, S->tlo1.p, S->thi1.p, rs_lo, dt, dbc, st));
+    }
+    if (chain) {
+      // packed-direct chain claim (pcs.rs:1055-1090): point [tau, sel0, 0^5, instance]
+      tr.label("flock-pcs-packed-direct-v0");
+      tr.observe(pd_value);
+      F gpd = tr.sample();
+      target += gpd * pd_value;
+      const F et[2] = {F::one() + pd_tau, pd_tau}, es[2] = {F::one() + pd_sel0, pd_sel0};
+      uint64_t c[8];
+      for (int p = 0; p < 4; p++) u2(gpd * et[p & 1] * es[p >> 1], c + 2 * p);
+      int lob = std::min(n_log, 12);
+      eq_split_dev(*S, pd_inst, lob, S->eqlo, S->eqhi);
+      FK(flock_launch_chain_claim_basis(dbc, (size_t)1 << n_log, S->eqlo.p, S->eqhi.p, lob, c, st));
     }
     T.ring_switch_ms = clk.lap();
     w.u64(2);
@@ -934,6 +994,15 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     w.fv(ood_vals);
     w.u64(fold_nonces.size());
     for (auto x : fold_nonces) w.u64(x);
+    if (chain) {
+      // cv_0_phys, cv_last_phys: Vec<bool>, bit 32 w + b = bit b of word w (blake3.rs:3762-3770)
+      for (const uint32_t* cv : {chain->cv0, chain->cv_last}) {
+        w.u64(256);
+        uint8_t bits[256];
+        for (int i = 0; i < 256; i++) bits[i] = (uint8_t)((cv[i / 32] >> (i % 32)) & 1);
+        w.raw(bits, 256);
+      }
+    }
     out.swap(w.v);
     T.serialize_ms = clk.lap();
     return FLOCK_OK;
@@ -1192,10 +1261,36 @@ std::vector<F> induced_residual(int n, const std::vector<uint32_t>& q, const std
   return out;
 }
 
+// chain.rs:78-100: the successor relation's MLE.
+F shift_mle(const std::vector<F>& a, const std::vector<F>& b) {
+  const size_t n = a.size();
+  std::vector<F> pre(n + 1, F::one()), suf(n + 1, F::one());
+  for (size_t j = 0; j < n; j++) pre[j + 1] = pre[j] * (a[j] * (F::one() + b[j]));
+  for (size_t j = n; j-- > 0;) suf[j] = suf[j + 1] * (F::one() + a[j] + b[j]);
+  F acc;
+  for (size_t j = 0; j < n; j++) acc += pre[j] * ((F::one() + a[j]) * b[j]) * suf[j + 1];
+  return acc;
+}
+
+// chain_common.rs:88-113: the 256 endpoint bits packed into two words, eq(tau)-weighted.
+F fold_phys(const std::vector<uint8_t>& bits, F tau) {
+  F w[2];
+  for (size_t i = 0; i < bits.size(); i++) {
+    if (!bits[i]) continue;
+    const size_t pos = i / 128, b = i % 128;
+    if (b < 64) w[pos].lo ^= 1ULL << b;
+    else w[pos].hi ^= 1ULL << (b - 64);
+  }
+  return (F::one() + tau) * w[0] + tau * w[1];
+}
+
 }  // namespace
 
-int flock_prover_verify(ProverState* S, const uint8_t* data, size_t len, int* accepted, std::string* why) {
+// R1CS bundle (chain_domain == nullptr) or chain bundle under chain_domain.
+static int verify_impl(ProverState* S, const uint8_t* data, size_t len, const char* chain_domain, int* accepted,
+                std::string* why) {
   *accepted = 0;
+  const bool chain = chain_domain != nullptr;
   auto reject = [&](const char* w) {
     if (why) *why = w;
     return FLOCK_OK;
@@ -1210,7 +1305,8 @@ int flock_prover_verify(ProverState* S, const uint8_t* data, size_t len, int* ac
     uint8_t ver[2];
     rd.take(magic, 5);
     rd.take(ver, 2);
-    if (!rd.ok || memcmp(magic, "FLOCK", 5) != 0 || ver[0] != 4 || ver[1] != 2) return reject("header");
+    if (!rd.ok || memcmp(magic, "FLOCK", 5) != 0 || ver[0] != 4 || ver[1] != (chain ? 3 : 2)) return reject("header");
+    if (chain && rd.u32() != 0) return reject("hash kind");  // HashKind::Blake3
     H32 root0;
     rd.take(root0.data(), 32);
     const uint64_t m64 = rd.u64(), rate0 = rd.u64(), lbs = rd.u64();
@@ -1227,6 +1323,13 @@ int flock_prover_verify(ProverState* S, const uint8_t* data, size_t len, int* ac
     // lincheck proof
     auto lc_rounds = rd.pv(64);
     auto z_partial = rd.fv(64);
+    // chain shift proof
+    std::vector<std::pair<F, F>> sh_rounds;
+    F sh_g;
+    if (chain) {
+      sh_rounds = rd.pv(64);
+      sh_g = rd.f();
+    }
     // ring switch
     uint64_t n_claims = rd.u64();
     auto sh0 = rd.fv(128), sh1 = rd.fv(128);
@@ -1248,6 +1351,16 @@ int flock_prover_verify(ProverState* S, const uint8_t* data, size_t len, int* ac
     auto grind_nonces = rd.u64v(64);
     auto ood_vals = rd.fv(64);
     auto fold_nonces = rd.u64v(1 << 10);
+    std::vector<uint8_t> ends[2];
+    if (chain)
+      for (auto& e : ends) {
+        const uint64_t k = rd.u64();
+        if (!rd.ok || k > 256) return reject("chain endpoints");  // at most one 256-bit region
+        e.resize(k);
+        rd.take(e.data(), k);
+        for (uint8_t x : e)
+          if (x > 1) return reject("decode");
+      }
     if (!rd.ok || rd.off != len) return reject("decode");
     if (p_ab.size() != 64 || p_c.size() != 64 || (int)zc_rounds.size() != m - 6 || lc_rounds.size() != 8 ||
         z_partial.size() != 64 || n_claims != 2 || sh0.size() != 128 || sh1.size() != 128)
@@ -1255,7 +1368,7 @@ int flock_prover_verify(ProverState* S, const uint8_t* data, size_t len, int* ac
 
     uint8_t digest[32];
     flock_statement_digest(m, digest);
-    fs::Transcript tr("flock-bench-v0");
+    fs::Transcript tr(chain ? chain_domain : "flock-bench-v0");
     tr.label("flock-r1cs-v0");
     tr.observe_bytes(digest, 32);
     tr.observe_bytes(root0.data(), 32);
@@ -1357,6 +1470,41 @@ int flock_prover_verify(ProverState* S, const uint8_t* data, size_t len, int* ac
     }
     std::vector<F> r_inner_rest(rr.rbegin(), rr.rend());
 
+    // ---- chain: endpoints and shift sumcheck (chain_common.rs:366-377, chain.rs:238-302) ----
+    std::vector<F> pd_inst;
+    F pd_tau, pd_sel0;
+    const int n_log = m - 14;
+    if (chain) {
+      pd_tau = tr.sample_vec(1)[0];
+      const F x0 = fold_phys(ends[0], pd_tau), xl = fold_phys(ends[1], pd_tau);
+      if ((int)sh_rounds.size() != n_log + 1) return reject("chain shift");
+      auto tau = tr.sample_vec(n_log);
+      const F al = tr.sample();
+      F ones = F::one();
+      for (auto& t : tau) ones = ones * t;
+      F claim = ones * xl + al * x0;
+      std::vector<F> rs;
+      for (auto& q : sh_rounds) {
+        tr.observe(q.first);
+        tr.observe(q.second);
+        F x = tr.sample();
+        F e0 = claim + q.first;
+        F c1 = e0 + q.first + q.second;
+        claim = q.second * x * x + c1 * x + e0;
+        rs.push_back(x);
+      }
+      pd_inst.assign(rs.rbegin(), rs.rend() - 1);
+      pd_sel0 = rs[0];
+      F eq_tt = F::one(), eq_t0 = F::one();
+      for (int j = 0; j < n_log; j++) {
+        eq_tt = eq_tt * (F::one() + tau[j] + pd_inst[j]);
+        eq_t0 = eq_t0 * (F::one() + pd_inst[j]);
+      }
+      const F o0 = F::one() + pd_sel0;
+      const F wfin = shift_mle(tau, pd_inst) * o0 + eq_tt * pd_sel0 + al * eq_t0 * o0;
+      if (claim != wfin * sh_g) return reject("chain shift");
+    }
+
     // ---- ring switch of [ab, c] (ring_switch.rs:2708-3345, pcs.rs:1025-1110) ----
     tr.label("flock-pcs-open-batch-v0");
     std::vector<F> x_ab(r_inner_rest);
@@ -1396,6 +1544,19 @@ int flock_prover_verify(ProverState* S, const uint8_t* data, size_t len, int* ac
       void* dt = S->tables.get(wk.size() * 16);
       h2d(*S, dt, wk.data(), wk.size() * 16);
       FK(flock_launch_combined_basis(n128, S->tlo0.p, S->thi0.p, S->tlo1.p, S->thi1.p, rs_lo, dt, dbc, st));
+    }
+    if (chain) {
+      // packed-direct chain claim (pcs.rs:1755-1770): its eq tensor joins the basis
+      tr.label("flock-pcs-packed-direct-v0");
+      tr.observe(sh_g);
+      F gpd = tr.sample();
+      target += gpd * sh_g;
+      const F et[2] = {F::one() + pd_tau, pd_tau}, es[2] = {F::one() + pd_sel0, pd_sel0};
+      uint64_t c[8];
+      for (int p = 0; p < 4; p++) u2(gpd * et[p & 1] * es[p >> 1], c + 2 * p);
+      int lob = std::min(n_log, 12);
+      eq_split_dev(*S, pd_inst, lob, S->eqlo, S->eqhi);
+      FK(flock_launch_chain_claim_basis(dbc, (size_t)1 << n_log, S->eqlo.p, S->eqhi.p, lob, c, st));
     }
 
     // ---- Ligerito (ligerito.rs:6981-8544) ----
@@ -1581,4 +1742,13 @@ int flock_prover_verify(ProverState* S, const uint8_t* data, size_t len, int* ac
   } catch (const Fail& f) {
     return f.code;
   }
+}
+
+int flock_prover_verify(ProverState* S, const uint8_t* data, size_t len, int* accepted, std::string* why) {
+  return verify_impl(S, data, len, nullptr, accepted, why);
+}
+
+int flock_prover_verify_chain(ProverState* S, const uint8_t* data, size_t len, const char* domain, int* accepted,
+                              std::string* why) {
+  return verify_impl(S, data, len, domain ? domain : "flock_chain-cli", accepted, why);
 }

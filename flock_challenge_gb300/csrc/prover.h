@@ -15,11 +15,20 @@ struct FlockPhaseTimes {
          ligerito_ms = 0, serialize_ms = 0;
 };
 
+// A hash-chain proof (Blake3Setup::prove_chain, crates/flock-prover/src/r1cs_hashes/blake3.rs:3785-3805):
+// the transcript domain and the public endpoints written into the bundle.
+struct ChainReq {
+  const char* domain = "flock_chain-cli";
+  uint32_t cv0[8] = {0}, cv_last[8] = {0};
+};
+
 ProverState* flock_prover_create(int device);
 void flock_prover_destroy(ProverState* s);
 // Proves n host compressions in 2^n_log slots; `out` receives the wire bytes.
+// With `chain`, the n = 2^n_log compressions form a cv chain and `out` is the
+// chain bundle (ChainProofBundleLigerito) instead of the R1CS bundle.
 int flock_prover_prove(ProverState* s, const flock_compression* in, size_t n, int n_log, std::vector<uint8_t>& out,
-                       bool input_on_device = false);
+                       bool input_on_device = false, const ChainReq* chain = nullptr);
 cudaStream_t flock_prover_stream(const ProverState* s);
 // Generates the 2^log2 benchmark inputs of `seed` on the device, then proves them.
 int flock_prover_prove_seed(ProverState* s, int log2, uint64_t seed, std::vector<uint8_t>& out);
@@ -35,3 +44,6 @@ void flock_prover_trim(ProverState* s);
 // device work fails.
 #include <string>
 int flock_prover_verify(ProverState* s, const uint8_t* data, size_t len, int* accepted, std::string* why);
+// Verifies a chain bundle (verify_chain, blake3.rs:3807-3830) under `domain`.
+int flock_prover_verify_chain(ProverState* s, const uint8_t* data, size_t len, const char* domain, int* accepted,
+                              std::string* why);

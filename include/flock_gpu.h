@@ -178,6 +178,34 @@ int flock_verify(flock_ctx* ctx, const uint8_t* proof, size_t len, int* accepted
 int flock_verify_batch(flock_ctx* ctx, size_t count, const uint8_t* const* proofs, const size_t* lens,
                        int* accepted);
 
+/* ---- Hash chains ---------------------------------------------------------- */
+
+/* Proves that n = 2^k compressions (2^8 <= n <= 2^21) form a sequential chain,
+ * in[i + 1].cv == the first 8 output words of compress(in[i]), with public
+ * endpoints cv_0 = in[0].cv and cv_last = the first 8 output words of
+ * compress(in[n - 1]): the R1CS proof of the n compressions plus the shift
+ * sumcheck, opened together with one PCS opening. Writes the chain bundle
+ * ("FLOCK" 4 3, hash kind, commitment, proof, endpoint bits). A broken chain
+ * still yields a bundle; the verifier rejects it. domain NULL =
+ * "flock_chain-cli". Replaces Blake3Setup::prove_chain
+ * (crates/flock-prover/src/r1cs_hashes/blake3.rs:3785-3805) and
+ * ChainProofBundleLigerito::to_bytes (crates/flock-prover/src/proof_io.rs:486-493)
+ * as the flock_chain CLI calls them (crates/flock-prover/src/bin/flock_chain.rs:222-262). */
+int flock_prove_chain(flock_ctx* ctx, const flock_compression* in, size_t n, const char* domain, uint8_t* out,
+                      size_t cap, size_t* len);
+
+/* Verifies a chain bundle under domain (NULL = "flock_chain-cli"); *accepted
+ * as in flock_verify. Replaces ChainProofBundleLigerito::from_bytes +
+ * Blake3Setup::verify_chain (proof_io.rs:494-497, blake3.rs:3807-3830). */
+int flock_verify_chain(flock_ctx* ctx, const uint8_t* bundle, size_t len, const char* domain, int* accepted);
+
+/* Host-side honest chain as the flock_chain CLI builds it
+ * (crates/flock-prover/src/bin/flock_chain.rs:180-196, :222-245): message words
+ * are the low 32 bits of SplitMix64(seed) draws, counter 0, block_len 64,
+ * flags 0, each cv the previous output; cv0 NULL = the BLAKE3 IV. Sequential
+ * by nature (each cv depends on the previous compression). */
+int flock_chain_inputs(size_t steps, uint64_t seed, const uint32_t* cv0, flock_compression* out);
+
 /* ---- Batched and served proving ---------------------------------------- */
 
 /* Device bytes one prover holds for a proof of 2^log2_size compressions (the

@@ -190,6 +190,58 @@ int oracle_verify(const uint8_t* bytes, size_t len, int m, char* why, size_t why
   return ok ? 0 : -2;
 }
 
+// Honest BLAKE3 chain of `steps` compressions (flock_chain CLI generator);
+// cv0 = NULL starts from the BLAKE3 IV.
+void oracle_chain_inputs(size_t steps, uint64_t seed, const uint32_t* cv0, Compression* out) {
+  auto v = chain_inputs(steps, seed, cv0);
+  memcpy(out, v.data(), v.size() * sizeof(Compression));
+}
+
+// Chain proof of 2^n_blocks_log compressions (ChainProofBundleLigerito bytes).
+// Returns 0, -5 when cap is too small (len receives the needed size), -3 when
+// the steps do not fill 2^n_blocks_log.
+int oracle_prove_chain(const Compression* blocks, size_t n, int n_blocks_log, const char* domain, uint8_t* out,
+                       size_t cap, size_t* len) {
+  if (n != ((size_t)1 << n_blocks_log)) return -3;
+  std::vector<Compression> v(blocks, blocks + n);
+  uint8_t dg[32];
+  digest_for(K_LOG + n_blocks_log, dg);
+  ChainBundle cb = prove_chain(v, n_blocks_log, dg, domain ? domain : "flock_chain-cli");
+  auto bytes = encode_chain_bundle(cb);
+  *len = bytes.size();
+  if (bytes.size() > cap) return -5;
+  memcpy(out, bytes.data(), bytes.size());
+  return 0;
+}
+
+// 0 = accepted; -1 = malformed; -2 = rejected (why gets a short reason).
+int oracle_verify_chain(const uint8_t* bytes, size_t len, const char* domain, char* why, size_t why_cap) {
+  ChainBundle cb;
+  if (!decode_chain_bundle(bytes, len, cb)) {
+    if (why && why_cap) snprintf(why, why_cap, "malformed");
+    return -1;
+  }
+  uint8_t dg[32];
+  digest_for(cb.b.params.m, dg);
+  std::string w;
+  bool ok = cb.b.params.m > K_LOG + 7 &&
+            verify_chain(cb, cb.b.params.m, dg, mats().A, mats().B, domain ? domain : "flock_chain-cli", &w);
+  if (why && why_cap) snprintf(why, why_cap, "%s", ok ? "ok" : (w.empty() ? "params" : w.c_str()));
+  return ok ? 0 : -2;
+}
+
+// shift(a, b) of chain.rs:78-100 for n-coordinate points (2 u64 per element).
+void oracle_shift_mle(const uint64_t* a, const uint64_t* b, int n, uint64_t* out) {
+  std::vector<F128> x(n), y(n);
+  for (int i = 0; i < n; i++) {
+    x[i] = f128(a[2 * i], a[2 * i + 1]);
+    y[i] = f128(b[2 * i], b[2 * i + 1]);
+  }
+  F128 r = shift_mle(x, y);
+  out[0] = r.lo;
+  out[1] = r.hi;
+}
+
 // F8 NTT extension S -> Lambda of one 64-bit row through the reference's
 // recursive additive NTT (inverse on S = {0..63}, forward on 64 + span).
 void oracle_f8_extend_ntt(uint64_t row, uint8_t* out64) {

@@ -1259,7 +1259,12 @@ static RsOut ring_switch_prove(const std::vector<F128>& z, const std::vector<F12
   return o;
 }
 
-Bundle prove(const std::vector<Compression>& blocks, int n_log, const uint8_t digest[32], const std::string& domain) {
+// The R1CS proof (prover.rs:194-289); with `chain`, the hash-chain proof of
+// chain_common.rs:290-346: after lincheck the packed-position fold and the
+// shift sumcheck, then one opening over [ab, c] plus the packed-direct chain
+// claim (pcs.rs:1055-1090).
+static Bundle prove_impl(const std::vector<Compression>& blocks, int n_log, const uint8_t digest[32],
+                         const std::string& domain, ChainBundle* chain) {
   Bundle out;
   Witness w = build_witness(blocks, n_log, true);
   int m = w.m;
@@ -1280,6 +1285,17 @@ Bundle prove(const std::vector<Compression>& blocks, int n_log, const uint8_t di
   }
   LcClaim lc;
   out.lc = lc_prove(w.stripe.data(), m, A, B, zc.z, x_in, x_out, tr, lc);
+  std::vector<F128> pd_point;
+  F128 pd_value;
+  if (chain) {
+    F128 tau = tr.sample_vec(1)[0];
+    std::vector<F128> in_vals, out_vals;
+    chain_fold_io(w.z, (size_t)1 << n_log, tau, in_vals, out_vals);
+    ChainClaims cl;
+    chain->shift = prove_chain_shift(in_vals, out_vals, tr, cl);
+    pd_point = chain_claim_point(tau, cl);
+    pd_value = cl.value;
+  }
   // Claims [ab, c]; x_full = x_inner_rest ++ x_outer (prover.rs:138-146).
   std::vector<F128> x_ab(lc.r_inner_rest);
   x_ab.insert(x_ab.end(), x_out.begin(), x_out.end());
@@ -1293,14 +1309,39 @@ Bundle prove(const std::vector<Compression>& blocks, int n_log, const uint8_t di
   std::vector<F128> b(rs0.size());
   for (size_t i = 0; i < b.size(); i++) b[i] = g0 * rs0[i] + g1 * rs1[i];
   F128 target = g0 * o0.claim + g1 * o1.claim;
+  if (chain) {
+    tr.label("flock-pcs-packed-direct-v0");
+    tr.observe_f128(pd_value);
+    F128 g2 = tr.sample();
+    auto e = eq_table(pd_point);
+    for (size_t i = 0; i < b.size(); i++) b[i] += g2 * e[i];
+    target += g2 * pd_value;
+  }
   LigConfig cfg;
   if (!ligerito_config(m, 0, cfg)) throw std::runtime_error("no ligerito config for m");
   out.lig = ligerito_prove(cfg, w.z, std::move(b), target, cd, tr);
   return out;
 }
 
-bool verify(const Bundle& bd, int m, const uint8_t digest[32], const SparseRows& A, const SparseRows& B,
-            const std::string& domain, std::string* why) {
+Bundle prove(const std::vector<Compression>& blocks, int n_log, const uint8_t digest[32], const std::string& domain) {
+  return prove_impl(blocks, n_log, digest, domain, nullptr);
+}
+
+ChainBundle prove_chain(const std::vector<Compression>& blocks, int n_log, const uint8_t digest[32],
+                        const std::string& domain) {
+  if (blocks.empty() || blocks.size() != ((size_t)1 << n_log)) throw std::runtime_error("chain: steps must fill 2^n");
+  ChainBundle cb;
+  cb.b = prove_impl(blocks, n_log, digest, domain, &cb);
+  uint32_t o[16];
+  const Compression& l = blocks.back();
+  b3_compress(l.cv, l.m, l.counter, l.block_len, l.flags, o);
+  cb.cv0_phys = cv_to_phys(blocks[0].cv);
+  cb.cvlast_phys = cv_to_phys(o);
+  return cb;
+}
+
+static bool verify_impl(const Bundle& bd, int m, const uint8_t digest[32], const SparseRows& A, const SparseRows& B,
+                        const std::string& domain, std::string* why, const ChainBundle* chain) {
   if (bd.params.m != m || bd.params.log_inv_rate != 1 || bd.params.log_batch_size != 6) {
     if (why) *why = "params";
     return false;
@@ -1313,6 +1354,23 @@ bool verify(const Bundle& bd, int m, const uint8_t digest[32], const SparseRows&
   std::vector<F128> x_out(zc.mlv.begin() + (K_LOG - K_SKIP), zc.mlv.end());
   LcClaim lc;
   if (!lc_verify(bd.lc, A, B, zc.z, x_in, zc.a_eval, zc.b_eval, tr, lc, why)) return false;
+  std::vector<F128> pd_point;
+  F128 pd_value;
+  if (chain) {
+    if (chain->cv0_phys.size() > 256 || chain->cvlast_phys.size() > 256) {
+      if (why) *why = "chain endpoints";
+      return false;
+    }
+    F128 tau = tr.sample_vec(1)[0];
+    F128 x0 = fold_public_phys(chain->cv0_phys, tau), xl = fold_public_phys(chain->cvlast_phys, tau);
+    ChainClaims cl;
+    if (!verify_chain_shift(chain->shift, x0, xl, m - K_LOG, tr, cl)) {
+      if (why) *why = "chain shift";
+      return false;
+    }
+    pd_point = chain_claim_point(tau, cl);
+    pd_value = cl.value;
+  }
   std::vector<F128> x_ab(lc.r_inner_rest);
   x_ab.insert(x_ab.end(), x_out.begin(), x_out.end());
   const std::vector<F128>& x_c = zc.r_rest;
@@ -1351,9 +1409,27 @@ bool verify(const Bundle& bd, int m, const uint8_t digest[32], const SparseRows&
     b.resize(r0.size());
     for (size_t i = 0; i < b.size(); i++) b[i] = g0 * r0[i] + g1 * r1[i];
   }
+  if (chain) {
+    tr.label("flock-pcs-packed-direct-v0");
+    tr.observe_f128(pd_value);
+    F128 g2 = tr.sample();
+    auto e = eq_table(pd_point);
+    for (size_t i = 0; i < b.size(); i++) b[i] += g2 * e[i];
+    target += g2 * pd_value;
+  }
   LigConfig cfg;
   if (!ligerito_config(m, 0, cfg)) return false;
   return ligerito_verify(cfg, bd.lig, m - 7, target, bd.root, b, tr, why);
+}
+
+bool verify(const Bundle& bd, int m, const uint8_t digest[32], const SparseRows& A, const SparseRows& B,
+            const std::string& domain, std::string* why) {
+  return verify_impl(bd, m, digest, A, B, domain, why, nullptr);
+}
+
+bool verify_chain(const ChainBundle& cb, int m, const uint8_t digest[32], const SparseRows& A, const SparseRows& B,
+                  const std::string& domain, std::string* why) {
+  return verify_impl(cb.b, m, digest, A, B, domain, why, &cb);
 }
 
 // ============================================================================
@@ -1373,12 +1449,8 @@ struct W {
   void open(const LevelOpen& o) { u64(o.rows.size()); for (auto& r : o.rows) fv(r); hv(o.proof); }
 };
 
-std::vector<uint8_t> encode_bundle(const Bundle& b) {
-  W w;
-  const char* magic = "FLOCK";
-  for (int i = 0; i < 5; i++) w.u8((uint8_t)magic[i]);
-  w.u8(4);
-  w.u8(2);
+// Commitment, zerocheck, lincheck, [chain shift,] BatchOpeningProofLigerito.
+static void write_body(W& w, const Bundle& b, const ChainShiftProof* shift) {
   // Commitment { root, params { m, log_inv_rate, log_batch_size, profile, merkle_hash } }
   w.h(b.root);
   w.u64(b.params.m);
@@ -1396,6 +1468,11 @@ std::vector<uint8_t> encode_bundle(const Bundle& b) {
   // LincheckProof
   w.pv(b.lc.rounds);
   w.fv(b.lc.z_partial);
+  // ChainShiftProof { rounds, g_at_point } (chain.rs:105-116)
+  if (shift) {
+    w.pv(shift->rounds);
+    w.f(shift->g_at_point);
+  }
   // BatchOpeningProofLigerito
   w.u64(b.s_hat_v.size());
   for (auto& s : b.s_hat_v) w.fv(s);
@@ -1411,6 +1488,33 @@ std::vector<uint8_t> encode_bundle(const Bundle& b) {
   w.uv(l.grinding_nonces);
   w.fv(l.ood_values);
   w.uv(l.fold_nonces);
+}
+
+static void write_header(W& w, uint8_t flavor) {
+  const char* magic = "FLOCK";
+  for (int i = 0; i < 5; i++) w.u8((uint8_t)magic[i]);
+  w.u8(4);
+  w.u8(flavor);
+}
+
+std::vector<uint8_t> encode_bundle(const Bundle& b) {
+  W w;
+  write_header(w, 2);
+  write_body(w, b, nullptr);
+  return w.v;
+}
+
+// proof_io.rs:486-493: flavor 3, HashKind::Blake3 = 0, the body with the
+// shift proof, then the endpoint bits as Vec<bool> (one byte each).
+std::vector<uint8_t> encode_chain_bundle(const ChainBundle& cb) {
+  W w;
+  write_header(w, 3);
+  w.u32(0);
+  write_body(w, cb.b, &cb.shift);
+  for (const auto* v : {&cb.cv0_phys, &cb.cvlast_phys}) {
+    w.u64(v->size());
+    for (uint8_t x : *v) w.u8(x);
+  }
   return w.v;
 }
 
@@ -1432,9 +1536,7 @@ struct R {
   LevelOpen open() { LevelOpen o; size_t k = len(8); o.rows.resize(k); for (auto& r : o.rows) r = fv(); o.proof = hv(); return o; }
 };
 
-bool decode_bundle(const uint8_t* p, size_t n, Bundle& b) {
-  if (n < 7 || memcmp(p, "FLOCK", 5) != 0 || p[5] != 4 || p[6] != 2) return false;
-  R r{p, n, 7};
+static void read_body(R& r, Bundle& b, ChainShiftProof* shift) {
   b.root = r.h();
   b.params.m = (int)r.u64();
   b.params.log_inv_rate = (int)r.u64();
@@ -1449,6 +1551,10 @@ bool decode_bundle(const uint8_t* p, size_t n, Bundle& b) {
   b.zc.final_c = r.f();
   b.lc.rounds = r.pv();
   b.lc.z_partial = r.fv();
+  if (shift) {
+    shift->rounds = r.pv();
+    shift->g_at_point = r.f();
+  }
   size_t k = r.len(8);
   b.s_hat_v.resize(k);
   for (auto& s : b.s_hat_v) s = r.fv();
@@ -1465,7 +1571,29 @@ bool decode_bundle(const uint8_t* p, size_t n, Bundle& b) {
   l.grinding_nonces = r.uv();
   l.ood_values = r.fv();
   l.fold_nonces = r.uv();
+}
+
+bool decode_bundle(const uint8_t* p, size_t n, Bundle& b) {
+  if (n < 7 || memcmp(p, "FLOCK", 5) != 0 || p[5] != 4 || p[6] != 2) return false;
+  R r{p, n, 7};
+  read_body(r, b, nullptr);
   return r.ok && r.at == n;  // trailing bytes rejected
+}
+
+bool decode_chain_bundle(const uint8_t* p, size_t n, ChainBundle& cb) {
+  if (n < 7 || memcmp(p, "FLOCK", 5) != 0 || p[5] != 4 || p[6] != 3) return false;
+  R r{p, n, 7};
+  if (r.u32() != 0) return false;  // HashKind::Blake3 only
+  read_body(r, cb.b, &cb.shift);
+  for (auto* v : {&cb.cv0_phys, &cb.cvlast_phys}) {
+    size_t k = r.len(1);
+    v->resize(k);
+    for (auto& x : *v) {
+      x = r.u8();
+      if (x > 1) return false;  // bincode bools are 0 or 1
+    }
+  }
+  return r.ok && r.at == n;
 }
 
 }  // namespace oracle

@@ -88,4 +88,43 @@ Bundle prove(const std::vector<Compression>& blocks, int n_blocks_log, const uin
 bool verify(const Bundle& b, int m, const uint8_t digest[32], const SparseRows& A, const SparseRows& B,
             const std::string& domain = "flock-bench-v0", std::string* why = nullptr);
 
+// ---------------------------------------------------------------------------
+// Hash-chain relation (chain.cpp; crates/flock-prover/src/chain.rs,
+// r1cs_hashes/chain_common.rs, r1cs_hashes/blake3.rs:3750-3830).
+// ---------------------------------------------------------------------------
+struct ChainShiftProof {
+  std::vector<std::pair<F128, F128>> rounds;  // (q(1), q(inf)) per round
+  F128 g_at_point;
+};
+struct ChainClaims {
+  std::vector<F128> instance_point;
+  F128 sel0, value;
+};
+// Wire order of ChainProofBundleLigerito (proof_io.rs:152-158): hash kind,
+// commitment, { zerocheck, lincheck, shift, pcs_open }, cv_0 and cv_last bits.
+struct ChainBundle {
+  Bundle b;
+  ChainShiftProof shift;
+  std::vector<uint8_t> cv0_phys, cvlast_phys;  // 256 entries, 0 or 1
+};
+F128 shift_mle(const std::vector<F128>& a, const std::vector<F128>& b);
+ChainShiftProof prove_chain_shift(const std::vector<F128>& in_vals, const std::vector<F128>& out_vals, Transcript& tr,
+                                  ChainClaims& cl);
+bool verify_chain_shift(const ChainShiftProof& pf, F128 x0, F128 xlast, int n, Transcript& tr, ChainClaims& cl);
+void chain_fold_io(const std::vector<F128>& z, size_t n_inst, F128 tau, std::vector<F128>& in_vals,
+                   std::vector<F128>& out_vals);
+std::vector<F128> chain_claim_point(F128 tau, const ChainClaims& cl);
+F128 fold_public_phys(const std::vector<uint8_t>& phys, F128 tau);
+std::vector<uint8_t> cv_to_phys(const uint32_t cv[8]);
+std::vector<Compression> chain_inputs(size_t steps, uint64_t seed, const uint32_t cv0[8]);
+
+// Blake3Setup::prove_chain / verify_chain (blake3.rs:3785-3830) through the
+// generic chain prover (chain_common.rs:290-346, verifier :351-405).
+ChainBundle prove_chain(const std::vector<Compression>& blocks, int n_blocks_log, const uint8_t digest[32],
+                        const std::string& domain = "flock_chain-cli");
+bool verify_chain(const ChainBundle& cb, int m, const uint8_t digest[32], const SparseRows& A, const SparseRows& B,
+                  const std::string& domain = "flock_chain-cli", std::string* why = nullptr);
+std::vector<uint8_t> encode_chain_bundle(const ChainBundle& cb);
+bool decode_chain_bundle(const uint8_t* p, size_t n, ChainBundle& out);
+
 }  // namespace oracle

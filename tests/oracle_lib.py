@@ -176,6 +176,11 @@ def _proto():
         L.oracle_prove.argtypes = [P, ctypes.c_size_t, ctypes.c_int, P, ctypes.c_size_t,
                                    ctypes.POINTER(ctypes.c_size_t)]
         L.oracle_verify.argtypes = [P, ctypes.c_size_t, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]
+        L.oracle_chain_inputs.argtypes = [ctypes.c_size_t, ctypes.c_uint64, P, P]
+        L.oracle_prove_chain.argtypes = [P, ctypes.c_size_t, ctypes.c_int, ctypes.c_char_p, P, ctypes.c_size_t,
+                                         ctypes.POINTER(ctypes.c_size_t)]
+        L.oracle_verify_chain.argtypes = [P, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]
+        L.oracle_shift_mle.argtypes = [P, P, ctypes.c_int, P]
         L.oracle_f8_extend_ntt.argtypes = [ctypes.c_uint64, P]
         L.oracle_f8_extend_lagrange.argtypes = [ctypes.c_uint64, P]
         L._proto_ready = True
@@ -201,6 +206,48 @@ def verify(proof_bytes, m):
     why = ctypes.create_string_buffer(256)
     rc = L.oracle_verify(ptr(buf), len(proof_bytes), m, why, 256)
     return rc == 0, why.value.decode()
+
+
+def chain_inputs(steps, seed, cv0=None):
+    """Honest BLAKE3 chain (the flock_chain CLI's generator): each cv is the
+    previous compression's first 8 output words; cv0 None = the BLAKE3 IV."""
+    L = _proto()
+    out = np.zeros(steps, COMP_DTYPE)
+    c = None if cv0 is None else ptr(np.ascontiguousarray(cv0, dtype=np.uint32))
+    L.oracle_chain_inputs(steps, seed, c, ptr(out))
+    return out
+
+
+def prove_chain(blocks, domain=b"flock_chain-cli"):
+    """Oracle chain proof (ChainProofBundleLigerito bytes) of 2^k compressions."""
+    L = _proto()
+    blocks = np.ascontiguousarray(blocks)
+    n_log = int(len(blocks)).bit_length() - 1
+    cap = 4_000_000
+    out = np.zeros(cap, np.uint8)
+    ln = ctypes.c_size_t()
+    rc = L.oracle_prove_chain(ptr(blocks), len(blocks), n_log, domain, ptr(out), cap, ctypes.byref(ln))
+    assert rc == 0, rc
+    return out[:ln.value].tobytes()
+
+
+def verify_chain(proof_bytes, domain=b"flock_chain-cli"):
+    """Oracle chain verifier: returns (accepted, reason)."""
+    L = _proto()
+    buf = np.frombuffer(proof_bytes, np.uint8).copy()
+    why = ctypes.create_string_buffer(256)
+    rc = L.oracle_verify_chain(ptr(buf), len(proof_bytes), domain, why, 256)
+    return rc == 0, why.value.decode()
+
+
+def shift_mle(a, b):
+    """shift(a, b) for points given as lists of (lo, hi) u64 pairs."""
+    L = _proto()
+    x = np.array(a, dtype=np.uint64).reshape(-1)
+    y = np.array(b, dtype=np.uint64).reshape(-1)
+    out = np.zeros(2, np.uint64)
+    L.oracle_shift_mle(ptr(x), ptr(y), len(a), ptr(out))
+    return int(out[0]), int(out[1])
 
 
 def f8_extend(row, via="ntt"):
