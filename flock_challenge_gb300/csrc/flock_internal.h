@@ -71,6 +71,14 @@ int flock_launch_fold_lsb(const void* in, size_t n_out, const uint64_t r[2], voi
 int flock_launch_zc_round0_skip(const void* a, const void* b, size_t n_pairs, const void* lag, void* A0, void* B0,
                                 const void* eq_lo, const void* eq_hi, int lo_bits, void* partials, int grid,
                                 cudaStream_t st);
+// Zerocheck rounds 0..5 with the fixed-challenge eq factorisation
+// (zc_round_grp_kernel): skip != 0 is round 0 from the bit rows in0, in1 (lag:
+// the 64 skip Lagrange weights); otherwise in0, in1 are bound at rho. eq_lo
+// covers the phi8 and lowest general variables (lo_bits), eq_hi the rest.
+int flock_launch_zc_round_grp(const void* in0, const void* in1, size_t n_pairs, int skip, const uint64_t rho[2],
+                              const void* lag, void* Aout, void* Bout, const void* eq_lo, const void* eq_hi,
+                              int lo_bits, int a_bits, int m_bits, int m_mul, void* partials, int grid,
+                              cudaStream_t st);
 void flock_count_launch();
 // Runs fn once per (current device, key), under a lock, so no thread passes
 // before the first caller's fn has finished: per-device one-time work such as

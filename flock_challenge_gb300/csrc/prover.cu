@@ -591,27 +591,53 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     std::vector<std::pair<F, F>> zc_rounds;
     std::vector<F> rho;
     void *curA = dA0, *curB = dB0, *nxtA = dA1, *nxtB = dB1;
+    // r[9..12] = g / (1 + g), g = x^(2^(k-9)): eq(r_k, b) = (1 + r_k) x^(b 2^(k-9))
+    auto shift_var = [&](int k) { return (F::one() + r[k]) * F(1ULL << (1 << (k - 9)), 0) == r[k]; };
     for (int i = 0; i < n_mlv; i++) {
       size_t n_pairs = rows0 >> (i + 1);  // pairs of the round-i table
       std::vector<F> rr(r.begin() + 6 + i + 1, r.end());
       int nv = (int)rr.size();
-      int lob = std::min(nv, 12);
-      eq_split_dev(*S, rr, lob, S->eqlo, S->eqhi);
-      int grid = (int)std::min<size_t>(((n_pairs >> lob) + 0), 152 * 4);
-      if (grid < 1) grid = 1;
-      void* dpart = S->part.get((size_t)grid * 2 * 16);
       uint64_t rp[2] = {0, 0};
       if (i > 0) u2(rho.back(), rp);
-      if (i == 0)  // skip fold (multilinear.rs:598-630) fused into round 0
-        FK(flock_launch_zc_round0_skip(da, db, n_pairs, dlag, dA0, dB0, S->eqlo.p, S->eqhi.p, lob, dpart, grid, st));
-      else
-        FK(flock_launch_zc_round(curA, curB, n_pairs, 1, rp, nxtA, nxtB, S->eqlo.p, S->eqhi.p, lob, dpart, grid,
-                                 st));
+      // lowest variables of rr that are fixed challenges: phi8 ones (r7, r8)
+      // and shift ones (r9..r12); rounds 0..5 factor their eq weight
+      const int a_bits = std::max(0, 2 - i), f0 = std::max(9, 7 + i), m_bits = std::max(0, 13 - f0);
+      bool grp = m_bits > 0 && nv > a_bits + m_bits;
+      for (int k = f0; grp && k < 13; k++) grp = shift_var(k);
+      std::vector<F> g;
+      if (grp) {
+        F dinv = F::one();
+        for (int k = f0; k < 13; k++) dinv = dinv * (F::one() + r[k]);
+        std::vector<F> rg(rr.begin(), rr.begin() + a_bits);
+        rg.insert(rg.end(), rr.begin() + a_bits + m_bits, rr.end());
+        const int lob = std::min(nv - m_bits, 8);
+        eq_split_dev(*S, rg, lob, S->eqlo, S->eqhi);
+        int grid = (int)std::min<size_t>(n_pairs >> (lob + m_bits), 152 * 4);
+        void* dpart = S->part.get((size_t)grid * 2 * 16);
+        FK(flock_launch_zc_round_grp(i == 0 ? da : curA, i == 0 ? db : curB, n_pairs, i == 0, rp, dlag,
+                                     i == 0 ? dA0 : nxtA, i == 0 ? dB0 : nxtB, S->eqlo.p, S->eqhi.p, lob, a_bits,
+                                     m_bits, 1 << (f0 - 9), dpart, grid, st));
+        g = reduce_partials(*S, dpart, grid, 2);
+        g[0] = g[0] * dinv;
+        g[1] = g[1] * dinv;
+      } else {
+        int lob = std::min(nv, 12);
+        eq_split_dev(*S, rr, lob, S->eqlo, S->eqhi);
+        int grid = (int)std::min<size_t>(((n_pairs >> lob) + 0), 152 * 4);
+        if (grid < 1) grid = 1;
+        void* dpart = S->part.get((size_t)grid * 2 * 16);
+        if (i == 0)  // skip fold (multilinear.rs:598-630) fused into round 0
+          FK(flock_launch_zc_round0_skip(da, db, n_pairs, dlag, dA0, dB0, S->eqlo.p, S->eqhi.p, lob, dpart, grid,
+                                         st));
+        else
+          FK(flock_launch_zc_round(curA, curB, n_pairs, 1, rp, nxtA, nxtB, S->eqlo.p, S->eqhi.p, lob, dpart, grid,
+                                   st));
+        g = reduce_partials(*S, dpart, grid, 2);
+      }
       if (i > 0) {
         std::swap(curA, nxtA);
         std::swap(curB, nxtB);
       }
-      auto g = reduce_partials(*S, dpart, grid, 2);
       zc_rounds.push_back({g[0], g[1]});
       tr.observe(g[0]);
       tr.observe(g[1]);

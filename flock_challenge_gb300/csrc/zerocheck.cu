@@ -447,6 +447,113 @@ zc_round0_skip_kernel(const uint64_t* __restrict__ W0, const uint64_t* __restric
   }
 }
 
+// Block reduction of two unreduced sums into partials[2 * block], [2 * block + 1].
+__device__ __forceinline__ void block_reduce2(gf256 g1, gf256 gi, gf128* __restrict__ partials) {
+  __shared__ gf256 red[2][RND_THREADS / 32];
+  for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      g1.r[k] ^= __shfl_xor_sync(0xffffffffu, g1.r[k], off);
+      gi.r[k] ^= __shfl_xor_sync(0xffffffffu, gi.r[k], off);
+    }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { red[0][warp] = g1; red[1][warp] = gi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    gf256 s1 = {{0, 0, 0, 0}}, si = {{0, 0, 0, 0}};
+    for (int w = 0; w < RND_THREADS / 32; w++) { gf256_acc(s1, red[0][w]); gf256_acc(si, red[1][w]); }
+    partials[2 * blockIdx.x] = gf256_reduce(s1);
+    partials[2 * blockIdx.x + 1] = gf256_reduce(si);
+  }
+}
+
+// Multilinear rounds 0..5, whose lowest eq variables are fixed challenges
+// (zerocheck/univariate_skip_optimized.rs:85-130): r7, r8 are phi8 constants
+// and r9..r12 are g / (1 + g) with g = x^(2^k), so eq(r_k, b) = (1 + r_k) x^(b 2^k).
+// With s = a_bits + m_bits, pair j = h per_h + (g << s) + (jm << a_bits) + ja
+// (ja over the phi8 variables, jm over the shift variables, g and h over the
+// rest) has eq(j) = eq_lo[(g << a_bits) | ja] x^(m_mul jm) Dinv eq_hi[h], where
+// eq_lo / eq_hi are the eq tables of the phi8 and remaining variables and
+// Dinv = prod (1 + r_k) over the shift variables (applied on the host). So the
+// products a1 b1 and (a0 + a1)(b0 + b1) of an item's 2^m_bits pairs are summed
+// as shifted 143-bit XORs and weighted by eq_lo once per item: two GF(2^128)
+// products per pair instead of four. SKIP: round 0, the pairs' values come
+// from the skip fold of the bit rows (as in zc_round0_skip_kernel) and are
+// written to Aout, Bout; otherwise the 2 n_pairs-entry tables in0, in1 are
+// bound at rho into Aout, Bout (as in zc_round_kernel).
+template <bool SKIP>
+__global__ void __launch_bounds__(RND_THREADS, ZC_RND_MIN_BLOCKS)
+zc_round_grp_kernel(const void* __restrict__ in0, const void* __restrict__ in1, size_t n_pairs,
+                    const __grid_constant__ gf128p rho, const gf128* __restrict__ lag, gf128* __restrict__ Aout,
+                    gf128* __restrict__ Bout, const gf128* __restrict__ eq_lo, const gf128* __restrict__ eq_hi,
+                    int lo_bits, int a_bits, int m_bits, int m_mul, gf128* __restrict__ partials) {
+  extern __shared__ gf128 tab[];  // SKIP: [8][256] subset sums of the Lagrange weights
+  if constexpr (SKIP) {
+    for (int e = threadIdx.x; e < 8 * 256; e += blockDim.x) {
+      const int c = e >> 8, v = e & 255;
+      gf128 acc = gf_zero();
+      for (int k = 0; k < 8; k++)
+        if ((v >> k) & 1) acc = gf_add(acc, lag[8 * c + k]);
+      tab[e] = acc;
+    }
+    __syncthreads();
+  }
+  auto skip = [&](uint64_t w) {
+    gf128 r = gf_zero();
+#pragma unroll
+    for (int c = 0; c < 8; c++) r = gf_add(r, tab[c * 256 + ((w >> (8 * c)) & 255)]);
+    return r;
+  };
+  const int s = a_bits + m_bits;
+  const size_t items = (size_t)1 << lo_bits;
+  const size_t per_h = items << m_bits;
+  const size_t n_hi = n_pairs / per_h;
+  const size_t amask = ((size_t)1 << a_bits) - 1;
+  gf256 g1 = {{0, 0, 0, 0}}, gi = {{0, 0, 0, 0}};
+  for (size_t h = blockIdx.x; h < n_hi; h += gridDim.x) {
+    gf256 l1 = {{0, 0, 0, 0}}, li = {{0, 0, 0, 0}};
+    const size_t base = h * per_h;
+    for (size_t it = threadIdx.x; it < items; it += RND_THREADS) {
+      const size_t j0 = base + ((it >> a_bits) << s) + (it & amask);
+      Acc5 t1, ti;
+#pragma unroll
+      for (int k = 0; k < 5; k++) { t1.w[k] = 0; ti.w[k] = 0; }
+      for (int jm = 0; jm < (1 << m_bits); jm++) {
+        const size_t j = j0 + ((size_t)jm << a_bits);
+        gf128 a0, a1, b0, b1;
+        if constexpr (SKIP) {
+          const uint64_t* W0 = reinterpret_cast<const uint64_t*>(in0);
+          const uint64_t* W1 = reinterpret_cast<const uint64_t*>(in1);
+          const uint64_t x0 = W0[2 * j], x1 = W0[2 * j + 1], y0 = W1[2 * j], y1 = W1[2 * j + 1];
+          a0 = skip(x0); a1 = skip(x1); b0 = skip(y0); b1 = skip(y1);
+        } else {
+          const gf128* A = reinterpret_cast<const gf128*>(in0);
+          const gf128* B = reinterpret_cast<const gf128*>(in1);
+          const gf128 p0 = A[4 * j], p1 = A[4 * j + 1], p2 = A[4 * j + 2], p3 = A[4 * j + 3];
+          a0 = gf_add(p0, gf_mul_p(gf_add(p0, p1), rho));
+          a1 = gf_add(p2, gf_mul_p(gf_add(p2, p3), rho));
+          const gf128 q0 = B[4 * j], q1 = B[4 * j + 1], q2 = B[4 * j + 2], q3 = B[4 * j + 3];
+          b0 = gf_add(q0, gf_mul_p(gf_add(q0, q1), rho));
+          b1 = gf_add(q2, gf_mul_p(gf_add(q2, q3), rho));
+        }
+        Aout[2 * j] = a0; Aout[2 * j + 1] = a1;
+        Bout[2 * j] = b0; Bout[2 * j + 1] = b1;
+        const gf128 p1 = gf_mul(a1, b1), pi = gf_mul(gf_add(a0, a1), gf_add(b0, b1));
+        const uint32_t sh = (uint32_t)(jm * m_mul);
+        acc_shift_xor_v(t1, make_uint4(p1.w[0], p1.w[1], p1.w[2], p1.w[3]), sh);
+        acc_shift_xor_v(ti, make_uint4(pi.w[0], pi.w[1], pi.w[2], pi.w[3]), sh);
+      }
+      const gf128 e = eq_lo[it];
+      gf256_acc(l1, gf_mul_wide(e, acc_reduce(t1)));
+      gf256_acc(li, gf_mul_wide(e, acc_reduce(ti)));
+    }
+    const gf128 eh = eq_hi[h];
+    gf256_acc(g1, gf_mul_wide(eh, gf256_reduce(l1)));
+    gf256_acc(gi, gf_mul_wide(eh, gf256_reduce(li)));
+  }
+  block_reduce2(g1, gi, partials);
+}
+
 // Final bind of the last round: out[j] = A0 + rho (A0 + A1).
 __global__ void bind_pairs_kernel(const gf128* __restrict__ A, const gf128* __restrict__ B, size_t n, gf128 rho,
                                   gf128* __restrict__ Aout, gf128* __restrict__ Bout) {
@@ -504,6 +611,29 @@ int flock_launch_bind_pairs(const void* A, const void* B, size_t n, const uint64
   if (grid > 152 * 8) grid = 152 * 8;
   bind_pairs_kernel<<<(unsigned)grid, 256, 0, st>>>((const gf128*)A, (const gf128*)B, n, r, (gf128*)Aout,
                                                     (gf128*)Bout); flock_count_launch();
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_launch_zc_round_grp(const void* in0, const void* in1, size_t n_pairs, int skip, const uint64_t rho[2],
+                              const void* lag, void* Aout, void* Bout, const void* eq_lo, const void* eq_hi,
+                              int lo_bits, int a_bits, int m_bits, int m_mul, void* partials, int grid,
+                              cudaStream_t st) {
+  // the item sums of 2^m_bits shifted products must stay below bit 143
+  if (a_bits < 0 || a_bits > lo_bits || m_bits < 1 || m_bits > 4 || m_mul < 1 || m_mul * ((1 << m_bits) - 1) > 15)
+    return FLOCK_ERR_SHAPE;
+  const size_t per_h = ((size_t)1 << lo_bits) << m_bits;
+  if (n_pairs % per_h != 0 || grid < 1) return FLOCK_ERR_SHAPE;
+  gf128 r;
+  r.w[0] = (uint32_t)rho[0]; r.w[1] = (uint32_t)(rho[0] >> 32); r.w[2] = (uint32_t)rho[1]; r.w[3] = (uint32_t)(rho[1] >> 32);
+  if (skip)
+    zc_round_grp_kernel<true><<<grid, RND_THREADS, 8 * 256 * sizeof(gf128), st>>>(
+        in0, in1, n_pairs, gf_prepare(r), (const gf128*)lag, (gf128*)Aout, (gf128*)Bout, (const gf128*)eq_lo,
+        (const gf128*)eq_hi, lo_bits, a_bits, m_bits, m_mul, (gf128*)partials);
+  else
+    zc_round_grp_kernel<false><<<grid, RND_THREADS, 0, st>>>(
+        in0, in1, n_pairs, gf_prepare(r), (const gf128*)lag, (gf128*)Aout, (gf128*)Bout, (const gf128*)eq_lo,
+        (const gf128*)eq_hi, lo_bits, a_bits, m_bits, m_mul, (gf128*)partials);
+  flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
