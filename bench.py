@@ -49,7 +49,11 @@ PUBLISHED = 483866.0  # README.md:110-116, unmodified reference, Apple M4 Pro ru
 # dram__bytes_read.sum + dram__bytes_write.sum of the L0 commit NTT passes per
 # launch set, from ncu on a 2^18-position case scaled by positions (traffic
 # grows in proportion): profiles/ntt_pass_l0_2e16.md.
-NTT_TRAFFIC_PER_SET = {20: 7.75e9}
+# DRAM bytes (read + write) per NTT pass at the bench's shape (2^20 positions x
+# 64 lanes): 486.5 MB per pass measured by ncu at 2^18 positions (mean of the
+# five L0 passes in profiles/ntt_pass_l0_2e16.md), times 4 for 4x the positions.
+NTT_TRAFFIC_PER_PASS = {20: 4 * 486.5e6}
+NTT_MAX_LAYERS = {0: 4, 1: 6, 2: 8}  # layers per pass of the autotuner's pass shapes
 
 
 def load_peaks():
@@ -201,16 +205,21 @@ def kernel_roofline(F, ctx_handle, stream_ptr, log2, peaks, torch, dev):
         e1.record(s)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
-    passes = (log_d - 1 + 5) // 6
+    F.lib().flock_ntt_tuned_variant.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    variant = F.lib().flock_ntt_tuned_variant(dev.index or 0, log_d, 6, 1)
+    max_f = NTT_MAX_LAYERS.get(variant, 6)
+    passes = (log_d - 1 + max_f - 1) // max_f
     # algorithmic bytes: the first pass reads the 2^(log_d-1) x 64 x 16 B message,
     # every pass writes the 2^log_d x 64 x 16 B codeword, later passes read it
     cw = (1 << (log_d + 6)) * 16
     alg = cw // 2 + cw + (passes - 1) * 2 * cw
     achieved = alg / (ms * 1e-3) / 1e9
     muls = (log_d - 1) * (1 << (log_d - 1)) * 64
-    return {"kernel": f"ntt_pass_kernel (L0 commit, layers 1..{log_d - 1}, {passes} passes)", "bound": "hbm",
+    return {"kernel": f"ntt_pass_kernel (L0 commit, layers 1..{log_d - 1}, {passes} passes of <= {max_f} layers)",
+            "bound": "hbm",
             "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-            "traffic": NTT_TRAFFIC_PER_SET.get(log_d), "algorithmic_bytes_per_set": alg,
+            "traffic": (passes * NTT_TRAFFIC_PER_PASS[log_d]) if log_d in NTT_TRAFFIC_PER_PASS else None,
+            "algorithmic_bytes_per_set": alg, "pass_shape": variant,
             "ms_per_launch_set": ms, "gf128_muls_per_s": muls / (ms * 1e-3),
             "note": "the passes are bound by the GF(2^128) multiply issue rate, not HBM: "
                     "see profiles/ntt_pass_l0_2e16.md for issue-slot and pipe utilisation"}
