@@ -28,8 +28,12 @@ constexpr int PF_GROUP = 8;  // stripes per table round (64 outer indices)
 __global__ void __launch_bounds__(PF_THREADS, 2)
 lc_partial_fold_kernel(const uint8_t* __restrict__ stripe, size_t n_stripes, const gf128* __restrict__ eq_lo,
                        const gf128* __restrict__ eq_hi, int lo_bits, gf128* __restrict__ partials) {
-  __shared__ gf128 t8[PF_GROUP][256];
-  __shared__ gf128 e8v[PF_GROUP * 8];
+  // t8[v][q]: subset sums of stripe q's eight eq weights; entry (v, q) sits in
+  // bank group q, and lane l starts at stripe l mod 8, so eight consecutive
+  // lanes read eight distinct bank groups. e8v[r][q]: weight of bit r of stripe q.
+  __shared__ gf128 t8[256][PF_GROUP];
+  __shared__ gf128 e8v[8][PF_GROUP];
+  const int lane8 = threadIdx.x & 7;
   gf128 acc[PF_PER_THREAD];
 #pragma unroll
   for (int k = 0; k < PF_PER_THREAD; k++) acc[k] = gf_zero();
@@ -41,8 +45,8 @@ lc_partial_fold_kernel(const uint8_t* __restrict__ stripe, size_t n_stripes, con
   for (size_t g = part; g < n_groups; g += parts) {
     const size_t s0 = g * PF_GROUP;
     if (threadIdx.x < PF_GROUP * 8) {
-      size_t o = 8 * s0 + threadIdx.x;
-      e8v[threadIdx.x] = gf_mul(eq_lo[o & lo_mask], eq_hi[o >> lo_bits]);
+      size_t o = 8 * s0 + threadIdx.x;  // stripe threadIdx.x / 8, bit threadIdx.x % 8
+      e8v[threadIdx.x & 7][threadIdx.x >> 3] = gf_mul(eq_lo[o & lo_mask], eq_hi[o >> lo_bits]);
     }
     // this thread's bytes of the group's stripes (loads overlap the table build)
     uint4 bytes[PF_GROUP];
@@ -51,21 +55,26 @@ lc_partial_fold_kernel(const uint8_t* __restrict__ stripe, size_t n_stripes, con
       bytes[q] = *reinterpret_cast<const uint4*>(stripe + (s0 + q) * FLOCK_K + col0);
     __syncthreads();
     for (int e = threadIdx.x; e < PF_GROUP * 256; e += PF_THREADS) {
-      const int q = e >> 8, v = e & 255;
+      const int v = e >> 3, q = e & 7;
       gf128 acc8 = gf_zero();
 #pragma unroll
       for (int r = 0; r < 8; r++)
-        if ((v >> r) & 1) acc8 = gf_add(acc8, e8v[8 * q + r]);
-      t8[q][v] = acc8;
+        if ((v >> r) & 1) acc8 = gf_add(acc8, e8v[r][q]);
+      t8[v][q] = acc8;
     }
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < PF_GROUP; q++) {
-      const uint32_t wds[4] = {bytes[q].x, bytes[q].y, bytes[q].z, bytes[q].w};
+    for (int st = 0; st < PF_GROUP; st++) {
+      const int q = (lane8 + st) & (PF_GROUP - 1);  // rotated stripe
+      uint4 bq = bytes[0];
+#pragma unroll
+      for (int qq = 1; qq < PF_GROUP; qq++)
+        if (q == qq) bq = bytes[qq];
+      const uint32_t wds[4] = {bq.x, bq.y, bq.z, bq.w};
 #pragma unroll
       for (int k = 0; k < PF_PER_THREAD; k++) {
         uint32_t b = (wds[k >> 2] >> (8 * (k & 3))) & 255;
-        if (b) acc[k] = gf_add(acc[k], t8[q][b]);
+        if (b) acc[k] = gf_add(acc[k], t8[b][q]);
       }
     }
     __syncthreads();

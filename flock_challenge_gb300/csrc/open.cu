@@ -94,8 +94,8 @@ combined_basis_kernel(int lo_bits, int slices, const gf128* __restrict__ lo0, co
                       const gf128* __restrict__ lo1, const gf128* __restrict__ hi1, const gf128* __restrict__ w,
                       gf128* __restrict__ b) {
   extern __shared__ gf128 cb[];
-  gf128* tab = cb;                  // [2][16][256]
-  gf128* beta = cb + 2 * 16 * 256;  // [2][128]
+  gf128* tab = cb;                  // [2][256 v][16 q]: entry (k, v, q) in bank group q mod 8
+  gf128* beta = cb + 2 * 16 * 256;  // [2][8 t][16 q]: L_k(x^(8q+t) h)
   const size_t h = blockIdx.x / slices;
   const int slice = blockIdx.x % slices;
   {
@@ -106,31 +106,37 @@ combined_basis_kernel(int lo_bits, int slices, const gf128* __restrict__ lo0, co
 #pragma unroll 4
     for (int bb = 0; bb < 128; bb++)
       if ((y.w[bb >> 5] >> (bb & 31)) & 1) acc = gf_add(acc, wk[bb]);
-    beta[k * 128 + i] = acc;
+    beta[k * 128 + (i & 7) * 16 + (i >> 3)] = acc;
   }
   __syncthreads();
   for (int e = threadIdx.x; e < 2 * 16 * 256; e += CB_THREADS) {
-    const int k = e >> 12, q = (e >> 8) & 15, v = e & 255;
-    const gf128* bq = beta + k * 128 + 8 * q;
+    const int k = e >> 12, v = (e >> 4) & 255, q = e & 15;
+    const gf128* bq = beta + k * 128 + q;
     gf128 acc = gf_zero();
 #pragma unroll
     for (int t = 0; t < 8; t++)
-      if ((v >> t) & 1) acc = gf_add(acc, bq[t]);
+      if ((v >> t) & 1) acc = gf_add(acc, bq[16 * t]);
     tab[e] = acc;
   }
   __syncthreads();
   const size_t lo_n = (size_t)1 << lo_bits;
   const size_t per = lo_n / slices;
   const size_t j0 = (size_t)slice * per;
+  // lane l starts at byte position l mod 16: eight consecutive lanes read
+  // eight distinct bank groups (conflict-free random lookups)
+  const int rot = threadIdx.x & 15;
   for (size_t j = j0 + threadIdx.x; j < j0 + per; j += CB_THREADS) {
     const gf128 u0 = lo0[j], u1 = lo1[j];
+    const uint4 x0 = make_uint4(u0.w[0], u0.w[1], u0.w[2], u0.w[3]), x1 = make_uint4(u1.w[0], u1.w[1], u1.w[2], u1.w[3]);
     gf128 acc = gf_zero();
 #pragma unroll
-    for (int q = 0; q < 16; q++) {
-      const uint32_t b0 = (u0.w[q >> 2] >> (8 * (q & 3))) & 255;
-      const uint32_t b1 = (u1.w[q >> 2] >> (8 * (q & 3))) & 255;
-      acc = gf_add(acc, tab[q * 256 + b0]);
-      acc = gf_add(acc, tab[4096 + q * 256 + b1]);
+    for (int t = 0; t < 16; t++) {
+      const int q = (rot + t) & 15;
+      const uint32_t w0 = (q & 8) ? ((q & 4) ? x0.w : x0.z) : ((q & 4) ? x0.y : x0.x);
+      const uint32_t w1 = (q & 8) ? ((q & 4) ? x1.w : x1.z) : ((q & 4) ? x1.y : x1.x);
+      const uint32_t b0 = (w0 >> (8 * (q & 3))) & 255, b1 = (w1 >> (8 * (q & 3))) & 255;
+      acc = gf_add(acc, tab[(b0 << 4) + q]);
+      acc = gf_add(acc, tab[4096 + (b1 << 4) + q]);
     }
     b[(h << lo_bits) + j] = acc;
   }

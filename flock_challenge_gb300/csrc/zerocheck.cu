@@ -112,10 +112,12 @@ __device__ __forceinline__ void acc_shift_xor_v(Acc5& a, const uint4 v, uint32_t
 }
 
 // Shared memory of the round-1 kernel (32-bit words):
-//   ext  [8 byte positions c][4 quarters q][256 values] of 16 B (a value's
-//        eight 64-bit planes, quarter q = planes 2q, 2q+1): consecutive values
-//        of one quarter are consecutive 16-byte slots, so random lookups spread
-//        over all bank groups;
+//   ext  [4 quarters q][256 values v][8 byte positions c] of 16 B (a value's
+//        eight 64-bit planes, quarter q = planes 2q, 2q+1): the table of byte
+//        position c lies in bank group c (16-byte slot index = c mod 8), and at
+//        step k lane l looks up byte position (l + k) mod 8, so any eight
+//        consecutive lanes hit eight distinct bank groups and the random
+//        lookups are conflict-free;
 //   phi  [256] of 16 B;
 //   xch  per warp, per half: [3 sets][16 xm] rows of 20 words (64 bytes used;
 //        the odd 80-byte row pitch makes the 16-byte stores conflict-free),
@@ -136,7 +138,7 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
   uint32_t* xch = reinterpret_cast<uint32_t*>(phi + 256);            // per warp [2][R1_HALF]
   const uint64_t* ext_src = &T->ext[0][0][0];
   for (int i = threadIdx.x; i < 8 * 4 * 256; i += R1_THREADS) {
-    const int c = i >> 10, q = (i >> 8) & 3, v = i & 255;
+    const int q = i >> 11, v = (i >> 3) & 255, c = i & 7;
     const uint64_t* e = ext_src + ((size_t)(c * 256 + v) << 3) + 2 * q;
     ext[i] = make_uint4((uint32_t)e[0], (uint32_t)(e[0] >> 32), (uint32_t)e[1], (uint32_t)(e[1] >> 32));
   }
@@ -174,12 +176,13 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
 #pragma unroll
         for (int j = 0; j < 8; j++) { ea[j] = 0; eb[j] = 0; }
 #pragma unroll
-        for (int c = 0; c < 8; c++) {
-          const uint4* pa = ext + c * 1024 + ((ra >> (8 * c)) & 255);
-          const uint4* pb = ext + c * 1024 + ((rb >> (8 * c)) & 255);
+        for (int k = 0; k < 8; k++) {
+          const int c = (lane + k) & 7;  // rotated byte position: conflict-free bank groups
+          const uint4* pa = ext + ((((uint32_t)(ra >> (8 * c))) & 255) << 3) + c;
+          const uint4* pb = ext + ((((uint32_t)(rb >> (8 * c))) & 255) << 3) + c;
 #pragma unroll
           for (int q = 0; q < 4; q++) {
-            uint4 va = pa[q * 256], vb = pb[q * 256];
+            uint4 va = pa[q * 2048], vb = pb[q * 2048];
             ea[2 * q] ^= ((uint64_t)va.y << 32) | va.x;
             ea[2 * q + 1] ^= ((uint64_t)va.w << 32) | va.z;
             eb[2 * q] ^= ((uint64_t)vb.y << 32) | vb.x;
@@ -296,20 +299,40 @@ reduce_rows_kernel(const gf128* __restrict__ in, size_t count, int width, gf128*
 }
 
 // eq table split: lo[i] = prod_{k<lo_bits} f(r_k, bit k of i), hi[i] over the
-// next hi_bits variables; f(r, 1) = r, f(r, 0) = 1 + r.
-__global__ void eq_split_kernel(const gf128* __restrict__ r, int lo_bits, int hi_bits, gf128* __restrict__ lo,
-                                gf128* __restrict__ hi) {
-  size_t nlo = (size_t)1 << lo_bits, nhi = (size_t)1 << hi_bits;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < nlo + nhi; e += (size_t)gridDim.x * blockDim.x) {
-    bool is_lo = e < nlo;
-    size_t idx = is_lo ? e : e - nlo;
-    int nb = is_lo ? lo_bits : hi_bits;
-    const gf128* rr = is_lo ? r : r + lo_bits;
+// next hi_bits variables; f(r, 1) = r, f(r, 0) = 1 + r. Each CTA first builds
+// the eq tables of 7-bit chunks of the variables in shared memory (at most
+// 4 x 128 entries per set), so an entry costs (chunks - 1) products instead
+// of one per variable.
+constexpr int EQ_CHUNK = 7, EQ_MAX_CHUNKS = 4;
+__global__ void __launch_bounds__(256)
+eq_split_kernel(const gf128* __restrict__ r, int lo_bits, int hi_bits, gf128* __restrict__ lo,
+                gf128* __restrict__ hi) {
+  __shared__ gf128 t[2][EQ_MAX_CHUNKS][1 << EQ_CHUNK];
+  for (int e = threadIdx.x; e < 2 * EQ_MAX_CHUNKS * (1 << EQ_CHUNK); e += blockDim.x) {
+    const int set = e / (EQ_MAX_CHUNKS << EQ_CHUNK), c = (e >> EQ_CHUNK) % EQ_MAX_CHUNKS, v = e & ((1 << EQ_CHUNK) - 1);
+    const int nb = set ? hi_bits : lo_bits;
+    const gf128* rr = (set ? r + lo_bits : r) + EQ_CHUNK * c;
+    const int cb = nb - EQ_CHUNK * c < EQ_CHUNK ? nb - EQ_CHUNK * c : EQ_CHUNK;
+    if (cb <= 0 || v >= (1 << cb)) continue;
     gf128 acc = gf_one();
-    for (int k = 0; k < nb; k++) {
+    for (int k = 0; k < cb; k++) {
       gf128 rk = rr[k];
-      if (!((idx >> k) & 1)) rk.w[0] ^= 1;
+      if (!((v >> k) & 1)) rk.w[0] ^= 1;
       acc = gf_mul(acc, rk);
+    }
+    t[set][c][v] = acc;
+  }
+  __syncthreads();
+  const size_t nlo = (size_t)1 << lo_bits, nhi = (size_t)1 << hi_bits;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < nlo + nhi; e += (size_t)gridDim.x * blockDim.x) {
+    const bool is_lo = e < nlo;
+    const size_t idx = is_lo ? e : e - nlo;
+    const int set = is_lo ? 0 : 1, nb = is_lo ? lo_bits : hi_bits;
+    const int nch = (nb + EQ_CHUNK - 1) / EQ_CHUNK;
+    gf128 acc = gf_one();
+    for (int c = 0; c < nch; c++) {
+      const gf128 f = t[set][c][(idx >> (EQ_CHUNK * c)) & ((1 << EQ_CHUNK) - 1)];
+      acc = c == 0 ? f : gf_mul(acc, f);
     }
     if (is_lo) lo[idx] = acc;
     else hi[idx] = acc;
@@ -487,10 +510,13 @@ zc_round_grp_kernel(const void* __restrict__ in0, const void* __restrict__ in1, 
                     const __grid_constant__ gf128p rho, const gf128* __restrict__ lag, gf128* __restrict__ Aout,
                     gf128* __restrict__ Bout, const gf128* __restrict__ eq_lo, const gf128* __restrict__ eq_hi,
                     int lo_bits, int a_bits, int m_bits, int m_mul, gf128* __restrict__ partials) {
-  extern __shared__ gf128 tab[];  // SKIP: [8][256] subset sums of the Lagrange weights
+  // SKIP: [256 v][8 c] subset sums of the Lagrange weights of byte position c;
+  // entry (v, c) sits in bank group c and lane l starts at byte position l mod
+  // 8, so eight consecutive lanes read eight distinct bank groups
+  extern __shared__ gf128 tab[];
   if constexpr (SKIP) {
     for (int e = threadIdx.x; e < 8 * 256; e += blockDim.x) {
-      const int c = e >> 8, v = e & 255;
+      const int v = e >> 3, c = e & 7;
       gf128 acc = gf_zero();
       for (int k = 0; k < 8; k++)
         if ((v >> k) & 1) acc = gf_add(acc, lag[8 * c + k]);
@@ -498,10 +524,14 @@ zc_round_grp_kernel(const void* __restrict__ in0, const void* __restrict__ in1, 
     }
     __syncthreads();
   }
+  const int lane8 = threadIdx.x & 7;
   auto skip = [&](uint64_t w) {
     gf128 r = gf_zero();
 #pragma unroll
-    for (int c = 0; c < 8; c++) r = gf_add(r, tab[c * 256 + ((w >> (8 * c)) & 255)]);
+    for (int k = 0; k < 8; k++) {
+      const int c = (lane8 + k) & 7;
+      r = gf_add(r, tab[((((uint32_t)(w >> (8 * c))) & 255) << 3) + c]);
+    }
     return r;
   };
   const int s = a_bits + m_bits;
@@ -584,9 +614,11 @@ int flock_launch_reduce_rows(const void* in, size_t count, int width, void* out,
 }
 
 int flock_launch_eq_split(const void* r, int lo_bits, int hi_bits, void* lo, void* hi, cudaStream_t st) {
+  if (lo_bits < 0 || hi_bits < 0 || lo_bits > EQ_CHUNK * EQ_MAX_CHUNKS || hi_bits > EQ_CHUNK * EQ_MAX_CHUNKS)
+    return FLOCK_ERR_SHAPE;
   size_t n = ((size_t)1 << lo_bits) + ((size_t)1 << hi_bits);
-  size_t grid = (n + 255) / 256;
-  if (grid > 4096) grid = 4096;
+  size_t grid = (n + 2047) / 2048;  // >= 8 entries per thread: the chunk tables are built per CTA
+  if (grid > 152) grid = 152;
   eq_split_kernel<<<(unsigned)grid, 256, 0, st>>>((const gf128*)r, lo_bits, hi_bits, (gf128*)lo, (gf128*)hi); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
