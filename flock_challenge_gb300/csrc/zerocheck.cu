@@ -118,14 +118,19 @@ __device__ __forceinline__ void acc_shift_xor_v(Acc5& a, const uint4 v, uint32_t
 //        step k lane l looks up byte position (l + k) mod 8, so any eight
 //        consecutive lanes hit eight distinct bank groups and the random
 //        lookups are conflict-free;
-//   phi  [256] of 16 B;
-//   xch  per warp, per half: [3 sets][16 xm] rows of 20 words (64 bytes used;
-//        the odd 80-byte row pitch makes the 16-byte stores conflict-free),
-//        halves 976 words apart (16 mod 32 banks) so both halves' reads of
-//        one row index hit disjoint banks.
+//   phi  [256 v][8 replicas] of 16 B: lane l reads replica l mod 8, which
+//        lies in bank group l mod 8, so the lookups are conflict-free;
+//   xch  per warp, per half: [16 xm] rows of 20 words (64 bytes used; the
+//        odd 80-byte row pitch makes the 16-byte stores conflict-free), one
+//        plane set at a time, halves 336 words apart (16 mod 32 banks) so both
+//        halves' reads of one row index hit disjoint banks.
+// Measured against three-set exchange areas (which leave no room for the
+// phi replicas at 12 warps) and a two-stage exchange, the one-set exchange
+// with 12 warps is fastest despite its register spills.
 constexpr int R1_ROW = 20;
-constexpr int R1_HALF = 3 * 16 * R1_ROW + 16;
-constexpr size_t R1_SMEM = (size_t)8 * 4 * 256 * 16 + 256 * 16 + (size_t)(R1_THREADS / 32) * 2 * R1_HALF * 4;
+constexpr int R1_HALF = 16 * R1_ROW + 16;
+constexpr size_t R1_SMEM = (size_t)8 * 4 * 256 * 16 + 8 * 256 * 16 + (size_t)(R1_THREADS / 32) * 2 * R1_HALF * 4;
+static_assert(R1_SMEM <= 232448, "round-1 shared memory above the 227 KB per-block limit");
 
 // grid: each warp walks pairs of outer blocks; lane: xm = lane & 15, xo half = lane >> 4.
 __global__ void __launch_bounds__(R1_THREADS, 1)
@@ -134,15 +139,15 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
                  gf128* __restrict__ partials) {
   extern __shared__ uint4 sm[];
   uint4* ext = sm;                                                   // [8][4][256]
-  uint4* phi = sm + 8 * 4 * 256;                                     // [256]
-  uint32_t* xch = reinterpret_cast<uint32_t*>(phi + 256);            // per warp [2][R1_HALF]
+  uint4* phi = sm + 8 * 4 * 256;                                     // [256][8]
+  uint32_t* xch = reinterpret_cast<uint32_t*>(phi + 8 * 256);        // per warp [2][R1_HALF]
   const uint64_t* ext_src = &T->ext[0][0][0];
   for (int i = threadIdx.x; i < 8 * 4 * 256; i += R1_THREADS) {
     const int q = i >> 11, v = (i >> 3) & 255, c = i & 7;
     const uint64_t* e = ext_src + ((size_t)(c * 256 + v) << 3) + 2 * q;
     ext[i] = make_uint4((uint32_t)e[0], (uint32_t)(e[0] >> 32), (uint32_t)e[1], (uint32_t)(e[1] >> 32));
   }
-  for (int i = threadIdx.x; i < 256; i += R1_THREADS) phi[i] = reinterpret_cast<const uint4*>(T->phi8)[i];
+  for (int i = threadIdx.x; i < 8 * 256; i += R1_THREADS) phi[i] = reinterpret_cast<const uint4*>(T->phi8)[i >> 3];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int xm = lane & 15, half = lane >> 4;
@@ -213,21 +218,23 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
         }
       }
     }
-    // Hand the three plane sets to the lanes of this half as bytes: the lane
-    // of point quad xm reads word xm of every (set, producer) row.
-    __syncwarp();
-    planes_to_bytes(w, my_x + (0 * 16 + xm) * R1_ROW);
-    planes_to_bytes(t, my_x + (1 * 16 + xm) * R1_ROW);
-    planes_to_bytes(t + 8, my_x + (2 * 16 + xm) * R1_ROW);
-    __syncwarp();
-    if (live) {
-      // this lane handles points / skip positions 4*xm .. 4*xm+3 of its half
-      // (and both parities t of the c statistic), one plane set at a time
-      const gf128 e = gf_load(&eq_out[xo]);
-      // one plane set per iteration (not unrolled: the body holds four GF
-      // products, which keeps the loop inside the instruction cache)
+    // Hand the three plane sets, one at a time, to the lanes of this half as
+    // bytes: the lane of point quad xm reads word xm of every producer row,
+    // and handles points / skip positions 4*xm .. 4*xm+3 of its half (and
+    // both parities t of the c statistic).
+    const gf128 e = live ? gf_load(&eq_out[xo]) : gf_zero();
+    const uint4* my_phi = phi + (lane & 7);
+    // one plane set per iteration (not unrolled: the body holds four GF
+    // products, which keeps the loop inside the instruction cache)
 #pragma unroll 1
-      for (int set = 0; set < 3; set++) {
+    for (int set = 0; set < 3; set++) {
+      uint64_t pl[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) pl[j] = set == 0 ? w[j] : set == 1 ? t[j] : t[8 + j];
+      __syncwarp();
+      planes_to_bytes(pl, my_x + xm * R1_ROW);
+      __syncwarp();
+      if (live) {
         Acc5 v[4];
 #pragma unroll
         for (int q = 0; q < 4; q++)
@@ -235,9 +242,9 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
           for (int k = 0; k < 5; k++) v[q].w[k] = 0;
 #pragma unroll 4
         for (int mm2 = 0; mm2 < 16; mm2++) {
-          const uint32_t bw = my_x[(set * 16 + mm2) * R1_ROW + xm];
+          const uint32_t bw = my_x[mm2 * R1_ROW + xm];
 #pragma unroll
-          for (int q = 0; q < 4; q++) acc_shift_xor_v(v[q], phi[(bw >> (8 * q)) & 255], (uint32_t)mm2);
+          for (int q = 0; q < 4; q++) acc_shift_xor_v(v[q], my_phi[((bw >> (8 * q)) & 255) << 3], (uint32_t)mm2);
         }
 #pragma unroll
         for (int q = 0; q < 4; q++) {
@@ -251,7 +258,7 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
     __syncwarp();
   }
   // lanes l and l + 16 hold the same points: combine; then reduce the warps
-  // of the block in shared memory (reusing the exchange area) and write one
+  // of the block in shared memory (reusing the extension tables) and write one
   // row of 192 partial sums per block: 64 P^AB values, then S[0..128).
 #pragma unroll
   for (int q = 0; q < 4; q++)
@@ -262,7 +269,7 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
 #pragma unroll
     for (int k = 0; k < 4; k++) sum_c[q].w[k] ^= __shfl_xor_sync(0xffffffffu, sum_c[q].w[k], 16);
   __syncthreads();
-  gf128* red = reinterpret_cast<gf128*>(xch);  // [warps][192]
+  gf128* red = reinterpret_cast<gf128*>(ext);  // [warps][192], in the no longer needed extension tables
   if (half == 0) {
     gf128* o = red + warp * 192;
 #pragma unroll
