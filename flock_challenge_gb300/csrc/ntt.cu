@@ -279,6 +279,155 @@ int run_pass(int f, gf128* dst, const gf128* src, size_t mask, const gf128* tw, 
 }
 constexpr int kMaxPassLayers = variant_max_layers(kDefaultVariant);
 
+// ---- table passes --------------------------------------------------------
+//
+// In the upper layers a twiddle multiplies many elements: layer l has 2^l
+// twiddles, each shared by the 2^(log_d - l - 1) butterflies of its block in
+// every lane. Multiplication by a fixed t is GF(2)-linear, so a CTA builds
+// byte tables T[(v << 4) + k] = t * v * x^(8k) (16 byte positions k, 256
+// values v, 64 KiB) once and then needs 16 table lookups per product instead
+// of a carry-less multiply: the products run on the load/store and ALU pipes
+// at about twice the rate. A table pass applies layers l and l + 1 to one
+// block of layer l (three twiddles: t_A = tw[2^l - 1 + hi] for layer l and
+// t_B, t_C for the two halves at layer l + 1); each thread owns a quad of
+// positions of one lane.
+constexpr int TAB_THREADS = 512;
+constexpr int TAB_ENTRIES = 16 * 256;
+constexpr size_t TAB_SMEM = (size_t)3 * TAB_ENTRIES * 16 + (size_t)3 * 128 * 16;
+
+// t * x^i for 0 <= i < 128: shift into 256 bits, then reduce.
+__device__ __forceinline__ gf128 gf_mul_xpow_small(gf128 h, int i) {
+  const uint64_t lo = h.w[0] | ((uint64_t)h.w[1] << 32), hi = h.w[2] | ((uint64_t)h.w[3] << 32);
+  const int wsh = i >> 6, bsh = i & 63;
+  const uint64_t s0 = lo << bsh, s1 = (hi << bsh) | (bsh ? lo >> (64 - bsh) : 0), s2 = bsh ? hi >> (64 - bsh) : 0;
+  return wsh == 0 ? gf_reduce(s0, s1, s2, 0) : gf_reduce(0, s0, s1, s2);
+}
+
+__device__ __forceinline__ uint32_t sel_word(const gf128& y, uint32_t j) {
+  return (j & 2) ? ((j & 1) ? y.w[3] : y.w[2]) : ((j & 1) ? y.w[1] : y.w[0]);
+}
+
+// t * y from t's byte tables. Lane rotation rot visits byte positions rot,
+// rot + 1, ... (mod 16); table slot (v << 4) + k lies in bank group k mod 8, so
+// eight consecutive lanes (distinct rot mod 8) read eight distinct bank groups.
+__device__ __forceinline__ gf128 gf_mul_tab(const uint4* __restrict__ T, const gf128& y, uint32_t rot) {
+  const uint32_t wr = rot >> 2, br = (rot & 3) * 8;
+  uint32_t q[5];
+#pragma unroll
+  for (int i = 0; i < 4; i++) q[i] = sel_word(y, (wr + i) & 3);
+  q[4] = q[0];
+  uint32_t r[4];  // byte s of r = byte (rot + s) mod 16 of y
+#pragma unroll
+  for (int i = 0; i < 4; i++) r[i] = __funnelshift_r(q[i], q[i + 1], br);
+  uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+#pragma unroll
+  for (int st = 0; st < 16; st++) {
+    const uint32_t b = (r[st >> 2] >> (8 * (st & 3))) & 255;
+    const uint4 v = T[(b << 4) | ((rot + st) & 15)];
+    a0 ^= v.x; a1 ^= v.y; a2 ^= v.z; a3 ^= v.w;
+  }
+  gf128 o;
+  o.w[0] = a0; o.w[1] = a1; o.w[2] = a2; o.w[3] = a3;
+  return o;
+}
+
+// Builds the byte tables of t into T (TAB_ENTRIES slots) via its 128 images
+// t x^i in basis[] (stored [b][k] = t x^(8k + b), so the fill's reads of one
+// step hit distinct bank groups). All threads of the CTA take part.
+__device__ void build_tab(gf128 t, uint4* __restrict__ T, uint4* __restrict__ basis) {
+  for (int i = threadIdx.x; i < 128; i += blockDim.x) {
+    const gf128 v = gf_mul_xpow_small(t, i);
+    basis[(i & 7) * 16 + (i >> 3)] = make_uint4(v.w[0], v.w[1], v.w[2], v.w[3]);
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < TAB_ENTRIES; e += blockDim.x) {
+    const int v = e >> 4, k = e & 15;
+    uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+#pragma unroll
+    for (int b = 0; b < 8; b++)
+      if ((v >> b) & 1) {
+        const uint4 x = basis[b * 16 + k];
+        a0 ^= x.x; a1 ^= x.y; a2 ^= x.z; a3 ^= x.w;
+      }
+    T[e] = make_uint4(a0, a1, a2, a3);
+  }
+}
+
+// Layers l, l + 1 of the transform for block hi of layer l (blockIdx.x / cph)
+// in all lanes; the cph CTAs of a block split its quads. Position p of a quad:
+// (hi << (lo_bits + 2)) | (b << lo_bits) | lo, b = 2-bit quad index.
+__global__ void __launch_bounds__(TAB_THREADS, 1)
+ntt_tab2_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t src_pos_mask,
+                const gf128* __restrict__ tw, int log_d, int log_lanes, int l, int cph) {
+  extern __shared__ uint4 tabs[];  // [3][TAB_ENTRIES], then 3 x 128 basis images
+  const size_t hi = blockIdx.x / cph;
+  const int part = blockIdx.x % cph;
+  const gf128 ta = tw[((size_t)1 << l) - 1 + hi];
+  const gf128 tb = tw[((size_t)1 << (l + 1)) - 1 + 2 * hi];
+  const gf128 tc = tw[((size_t)1 << (l + 1)) - 1 + 2 * hi + 1];
+  uint4* basis = tabs + 3 * TAB_ENTRIES;
+  build_tab(ta, tabs, basis);
+  build_tab(tb, tabs + TAB_ENTRIES, basis + 128);
+  build_tab(tc, tabs + 2 * TAB_ENTRIES, basis + 256);
+  __syncthreads();
+  // block 0 of every layer has twiddle 0: its butterflies need no product
+  const bool za = hi == 0, zb = hi == 0;
+  const int lo_bits = log_d - l - 2;
+  const size_t nl = (size_t)1 << log_lanes;
+  const size_t items = ((size_t)1 << lo_bits) << log_lanes;
+  const uint32_t rot = threadIdx.x & 15;
+  for (size_t it = (size_t)part * TAB_THREADS + threadIdx.x; it < items; it += (size_t)cph * TAB_THREADS) {
+    const size_t lane = it & (nl - 1), lo = it >> log_lanes;
+    const size_t p0 = (hi << (lo_bits + 2)) | lo;
+    gf128 y[4];
+#pragma unroll
+    for (int b = 0; b < 4; b++)
+      y[b] = gf_load(&src[((p0 | ((size_t)b << lo_bits)) & src_pos_mask) * nl + lane]);
+    // layer l: pairs (b, b + 2) with t_A
+    if (!za) {
+      y[0] = gf_add(y[0], gf_mul_tab(tabs, y[2], rot));
+      y[1] = gf_add(y[1], gf_mul_tab(tabs, y[3], rot));
+    }
+    y[2] = gf_add(y[2], y[0]);
+    y[3] = gf_add(y[3], y[1]);
+    // layer l + 1: pairs (0, 1) with t_B, (2, 3) with t_C
+    if (!zb) y[0] = gf_add(y[0], gf_mul_tab(tabs + TAB_ENTRIES, y[1], rot));
+    y[1] = gf_add(y[1], y[0]);
+    y[2] = gf_add(y[2], gf_mul_tab(tabs + 2 * TAB_ENTRIES, y[3], rot));
+    y[3] = gf_add(y[3], y[2]);
+#pragma unroll
+    for (int b = 0; b < 4; b++) gf_store(&dst[(p0 | ((size_t)b << lo_bits)) * nl + lane], y[b]);
+  }
+}
+
+// Layers [start, end) handled by table passes: pairs of layers while at least
+// three layers remain for the multiply passes (the deep layers have too few
+// products per twiddle to pay for a table) and the lanes give reuse.
+int tab_layers_end(int log_d, int log_lanes, int start) {
+  if (log_lanes < 6) return start;
+  int l = start;
+  while (l + 1 < log_d - 3) l += 2;
+  return l;
+}
+
+int launch_tab2(gf128* dst, const gf128* src, size_t mask, const gf128* tw, int log_d, int log_lanes, int l,
+                cudaStream_t st) {
+  flock_once_per_device((const void*)ntt_tab2_kernel, [] {
+    cudaFuncSetAttribute(ntt_tab2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAB_SMEM);
+  });
+  const size_t n_hi = (size_t)1 << l;
+  const size_t items = ((size_t)1 << (log_d - l - 2)) << log_lanes;
+  // about two CTAs per SM in all, each with at least one item per thread
+  size_t cph = (304 + n_hi - 1) / n_hi;
+  const size_t max_cph = (items + TAB_THREADS - 1) / TAB_THREADS;
+  if (cph > max_cph) cph = max_cph;
+  if (cph < 1) cph = 1;
+  ntt_tab2_kernel<<<(unsigned)(n_hi * cph), TAB_THREADS, TAB_SMEM, st>>>(dst, src, mask, tw, log_d, log_lanes, l,
+                                                                         (int)cph);
+  flock_count_launch();
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
 __global__ void prepare_twiddles_kernel(const gf128* __restrict__ tw, size_t n, gf128p* __restrict__ out) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     out[i] = gf_prepare(tw[i]);
@@ -440,8 +589,22 @@ int flock_launch_ntt(void* d_data, const void* d_src, int log_d, int log_lanes, 
     }
     return FLOCK_OK;
   }
-  const int v = pick_variant(log_d, log_lanes, start_layer, tw, stream);
-  return run_passes<true>(v, data, src, mask, tw, log_d, log_lanes, start_layer, stream);
+  // upper layers in table passes, then the multiply passes of the tuned shape
+  int l = start_layer;
+  const int tab_end = tab_layers_end(log_d, log_lanes, start_layer);
+  if (tab_end > l) {
+    const gf128* twp = (const gf128*)flock_ntt_twiddles(log_d);
+    if (!twp) return FLOCK_ERR_OOM;
+    for (; l + 2 <= tab_end; l += 2) {
+      int rc = launch_tab2(data, src, mask, twp, log_d, log_lanes, l, stream);
+      if (rc != FLOCK_OK) return rc;
+      src = data;
+      mask = ~(size_t)0;
+    }
+  }
+  if (l == log_d) return FLOCK_OK;
+  const int v = pick_variant(log_d, log_lanes, l, tw, stream);
+  return run_passes<true>(v, data, src, mask, tw, log_d, log_lanes, l, stream);
 }
 
 // ---- NTT without device allocation -----------------------------------------
