@@ -293,7 +293,7 @@ constexpr int kMaxPassLayers = variant_max_layers(kDefaultVariant);
 // positions of one lane.
 constexpr int TAB_THREADS = 512;
 constexpr int TAB_ENTRIES = 16 * 256;
-constexpr size_t TAB_SMEM = (size_t)3 * TAB_ENTRIES * 16 + (size_t)3 * 128 * 16;
+constexpr size_t TAB_SMEM = (size_t)3 * TAB_ENTRIES * 16 + (size_t)3 * 512 * 16;
 
 // t * x^i for 0 <= i < 128: shift into 256 bits, then reduce.
 __device__ __forceinline__ gf128 gf_mul_xpow_small(gf128 h, int i) {
@@ -331,25 +331,33 @@ __device__ __forceinline__ gf128 gf_mul_tab(const uint4* __restrict__ T, const g
   return o;
 }
 
-// Builds the byte tables of t into T (TAB_ENTRIES slots) via its 128 images
-// t x^i in basis[] (stored [b][k] = t x^(8k + b), so the fill's reads of one
-// step hit distinct bank groups). All threads of the CTA take part.
-__device__ void build_tab(gf128 t, uint4* __restrict__ T, uint4* __restrict__ basis) {
-  for (int i = threadIdx.x; i < 128; i += blockDim.x) {
-    const gf128 v = gf_mul_xpow_small(t, i);
-    basis[(i & 7) * 16 + (i >> 3)] = make_uint4(v.w[0], v.w[1], v.w[2], v.w[3]);
+__host__ __device__ constexpr int ctz4(int j) { return (j & 1) ? 0 : (j & 2) ? 1 : (j & 4) ? 2 : 3; }
+
+// Builds the byte tables of the three twiddles t[0..2] into T (3 x TAB_ENTRIES
+// slots). Entry (v, k) = L[v & 15][k] + H[v >> 4][k], where L[j][k] = t j x^(8k)
+// and H[g][k] = t g x^(8k + 4) are the nibble tables (each 16 values per byte
+// position, made by 32 threads per twiddle with a Gray-code walk over the
+// images t x^i); LH holds them as [twiddle][L, H][16][16 k] so that the fill's
+// reads of one step hit distinct bank groups. All threads of the CTA take part.
+__device__ void build_tabs3(const gf128 t[3], uint4* __restrict__ T, uint4* __restrict__ LH) {
+  if (threadIdx.x < 96) {
+    const int x = threadIdx.x >> 5, part = (threadIdx.x >> 4) & 1, k = threadIdx.x & 15;
+    gf128 B[4];
+#pragma unroll
+    for (int b = 0; b < 4; b++) B[b] = gf_mul_xpow_small(t[x], 8 * k + 4 * part + b);
+    gf128 v[16];
+    v[0] = gf_zero();
+#pragma unroll
+    for (int j = 1; j < 16; j++) v[j] = gf_add(v[j & (j - 1)], B[ctz4(j)]);
+    uint4* out = LH + x * 512 + part * 256;
+#pragma unroll
+    for (int j = 0; j < 16; j++) out[j * 16 + k] = make_uint4(v[j].w[0], v[j].w[1], v[j].w[2], v[j].w[3]);
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < TAB_ENTRIES; e += blockDim.x) {
-    const int v = e >> 4, k = e & 15;
-    uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-#pragma unroll
-    for (int b = 0; b < 8; b++)
-      if ((v >> b) & 1) {
-        const uint4 x = basis[b * 16 + k];
-        a0 ^= x.x; a1 ^= x.y; a2 ^= x.z; a3 ^= x.w;
-      }
-    T[e] = make_uint4(a0, a1, a2, a3);
+  for (int e = threadIdx.x; e < 3 * TAB_ENTRIES; e += blockDim.x) {
+    const int x = e / TAB_ENTRIES, r = e % TAB_ENTRIES, v = r >> 4, k = r & 15;
+    const uint4 lo = LH[x * 512 + (v & 15) * 16 + k], hi = LH[x * 512 + 256 + (v >> 4) * 16 + k];
+    T[e] = make_uint4(lo.x ^ hi.x, lo.y ^ hi.y, lo.z ^ hi.z, lo.w ^ hi.w);
   }
 }
 
@@ -359,16 +367,12 @@ __device__ void build_tab(gf128 t, uint4* __restrict__ T, uint4* __restrict__ ba
 __global__ void __launch_bounds__(TAB_THREADS, 1)
 ntt_tab2_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t src_pos_mask,
                 const gf128* __restrict__ tw, int log_d, int log_lanes, int l, int cph) {
-  extern __shared__ uint4 tabs[];  // [3][TAB_ENTRIES], then 3 x 128 basis images
+  extern __shared__ uint4 tabs[];  // [3][TAB_ENTRIES], then the nibble tables [3][2][16][16]
   const size_t hi = blockIdx.x / cph;
   const int part = blockIdx.x % cph;
-  const gf128 ta = tw[((size_t)1 << l) - 1 + hi];
-  const gf128 tb = tw[((size_t)1 << (l + 1)) - 1 + 2 * hi];
-  const gf128 tc = tw[((size_t)1 << (l + 1)) - 1 + 2 * hi + 1];
-  uint4* basis = tabs + 3 * TAB_ENTRIES;
-  build_tab(ta, tabs, basis);
-  build_tab(tb, tabs + TAB_ENTRIES, basis + 128);
-  build_tab(tc, tabs + 2 * TAB_ENTRIES, basis + 256);
+  const gf128 t3[3] = {tw[((size_t)1 << l) - 1 + hi], tw[((size_t)1 << (l + 1)) - 1 + 2 * hi],
+                       tw[((size_t)1 << (l + 1)) - 1 + 2 * hi + 1]};
+  build_tabs3(t3, tabs, tabs + 3 * TAB_ENTRIES);
   __syncthreads();
   // block 0 of every layer has twiddle 0: its butterflies need no product
   const bool za = hi == 0, zb = hi == 0;
