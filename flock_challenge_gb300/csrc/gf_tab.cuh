@@ -1,0 +1,87 @@
+// Multiplication by a fixed GF(2^128) element through byte tables in shared
+// memory. y -> t y is GF(2)-linear, so with T[(v << 4) + k] = t v x^(8k) (16
+// byte positions k, 256 byte values v: 64 KiB) a product is the XOR of 16
+// table entries, one per byte of y, with no carry-less multiply. Worth it when
+// one CTA multiplies many elements by the same t (NTT twiddles of the upper
+// layers, a sumcheck round's binding challenge). Slot (v << 4) + k lies in
+// bank group k mod 8 and a thread with rotation rot visits byte positions
+// rot, rot + 1, ... (mod 16), so eight consecutive threads with distinct rot
+// mod 8 read eight distinct bank groups: the random lookups are
+// conflict-free.
+#pragma once
+#include "gf128.cuh"
+
+constexpr int GF_TAB_ENTRIES = 16 * 256;      // slots of one byte-table set
+constexpr int GF_TAB_NIBBLE_SLOTS = 2 * 256;  // slots of its nibble tables
+
+// t * x^i for 0 <= i < 128: shift into 256 bits, then reduce.
+__device__ __forceinline__ gf128 gf_mul_xpow_small(gf128 h, int i) {
+  const uint64_t lo = h.w[0] | ((uint64_t)h.w[1] << 32), hi = h.w[2] | ((uint64_t)h.w[3] << 32);
+  const int wsh = i >> 6, bsh = i & 63;
+  const uint64_t s0 = lo << bsh, s1 = (hi << bsh) | (bsh ? lo >> (64 - bsh) : 0), s2 = bsh ? hi >> (64 - bsh) : 0;
+  return wsh == 0 ? gf_reduce(s0, s1, s2, 0) : gf_reduce(0, s0, s1, s2);
+}
+
+__device__ __forceinline__ uint32_t gf_sel_word(const gf128& y, uint32_t j) {
+  return (j & 2) ? ((j & 1) ? y.w[3] : y.w[2]) : ((j & 1) ? y.w[1] : y.w[0]);
+}
+
+// t * y from t's byte tables T.
+__device__ __forceinline__ gf128 gf_mul_tab(const uint4* __restrict__ T, const gf128& y, uint32_t rot) {
+  const uint32_t wr = rot >> 2, br = (rot & 3) * 8;
+  uint32_t q[5];
+#pragma unroll
+  for (int i = 0; i < 4; i++) q[i] = gf_sel_word(y, (wr + i) & 3);
+  q[4] = q[0];
+  uint32_t r[4];  // byte s of r = byte (rot + s) mod 16 of y
+#pragma unroll
+  for (int i = 0; i < 4; i++) r[i] = __funnelshift_r(q[i], q[i + 1], br);
+  uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+#pragma unroll
+  for (int st = 0; st < 16; st++) {
+    const uint32_t b = (r[st >> 2] >> (8 * (st & 3))) & 255;
+    const uint4 v = T[(b << 4) | ((rot + st) & 15)];
+    a0 ^= v.x; a1 ^= v.y; a2 ^= v.z; a3 ^= v.w;
+  }
+  gf128 o;
+  o.w[0] = a0; o.w[1] = a1; o.w[2] = a2; o.w[3] = a3;
+  return o;
+}
+
+__host__ __device__ constexpr int gf_tab_ctz4(int j) { return (j & 1) ? 0 : (j & 2) ? 1 : (j & 4) ? 2 : 3; }
+
+// Nibble tables of t into LH (GF_TAB_NIBBLE_SLOTS slots): L[j][k] = t j x^(8k)
+// at j * 16 + k and H[g][k] = t g x^(8k + 4) at 256 + g * 16 + k, for nibbles
+// j, g < 16. Called by 32 threads, part = 0..31 (k = part & 15, L or H by
+// part >> 4), each with a Gray-code walk over four images t x^i.
+__device__ __forceinline__ void gf_tab_nibbles(gf128 t, uint4* __restrict__ LH, int part) {
+  const int half = part >> 4, k = part & 15;
+  gf128 B[4];
+#pragma unroll
+  for (int b = 0; b < 4; b++) B[b] = gf_mul_xpow_small(t, 8 * k + 4 * half + b);
+  gf128 v[16];
+  v[0] = gf_zero();
+#pragma unroll
+  for (int j = 1; j < 16; j++) v[j] = gf_add(v[j & (j - 1)], B[gf_tab_ctz4(j)]);
+  uint4* out = LH + half * 256;
+#pragma unroll
+  for (int j = 0; j < 16; j++) out[j * 16 + k] = make_uint4(v[j].w[0], v[j].w[1], v[j].w[2], v[j].w[3]);
+}
+
+// Byte-table slot r = (v << 4) + k from the nibble tables: L[v & 15][k] + H[v >> 4][k]
+// (the reads of consecutive slots hit distinct bank groups).
+__device__ __forceinline__ uint4 gf_tab_entry(const uint4* __restrict__ LH, int r) {
+  const int v = r >> 4, k = r & 15;
+  const uint4 lo = LH[(v & 15) * 16 + k], hi = LH[256 + (v >> 4) * 16 + k];
+  return make_uint4(lo.x ^ hi.x, lo.y ^ hi.y, lo.z ^ hi.z, lo.w ^ hi.w);
+}
+
+// Byte tables of one multiplier t into T (GF_TAB_ENTRIES slots), using LH
+// (GF_TAB_NIBBLE_SLOTS slots) as scratch. All threads of the CTA call it; it
+// ends with a barrier, after which T is ready.
+__device__ __forceinline__ void gf_tab_build(gf128 t, uint4* __restrict__ T, uint4* __restrict__ LH) {
+  if (threadIdx.x < 32) gf_tab_nibbles(t, LH, threadIdx.x);
+  __syncthreads();
+  for (int e = threadIdx.x; e < GF_TAB_ENTRIES; e += blockDim.x) T[e] = gf_tab_entry(LH, e);
+  __syncthreads();
+}

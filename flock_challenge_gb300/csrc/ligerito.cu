@@ -12,6 +12,7 @@
 //  * glue b += beta * basis, row and tree-node gathers for openings.
 #include "flock_internal.h"
 #include "gf128.cuh"
+#include "gf_tab.cuh"
 
 namespace {
 
@@ -40,21 +41,33 @@ __device__ __forceinline__ void block_reduce_write(gf256 a, gf256 b, gf256 c, gf
 
 // If fold: in has 2 * n_out elements, bound at r into out (n_out elements);
 // message over the n_out-element state. Partials: (u0, u2, 0) per block.
+// use_tab: the fold multiplies through r's byte tables (gf_tab.cuh, dynamic
+// shared memory), worth their build when a CTA folds hundreds of pairs.
 __global__ void __launch_bounds__(LG_THREADS, 2)
 lig_fold_msg_kernel(const gf128* __restrict__ f, const gf128* __restrict__ b, size_t n_out, int fold,
-                    const __grid_constant__ gf128p r,
+                    const __grid_constant__ gf128p r, const gf128 r_plain, int use_tab,
                     gf128* __restrict__ fo, gf128* __restrict__ bo, gf128* __restrict__ partials) {
+  extern __shared__ uint4 rtab[];
+  const uint32_t rot = threadIdx.x & 15;
+  if (use_tab) gf_tab_build(r_plain, rtab, rtab + GF_TAB_ENTRIES);
   gf256 u0 = {{0, 0, 0, 0}}, u2 = u0, zz = u0;
   size_t pairs = n_out / 2;
   for (size_t j = (size_t)blockIdx.x * LG_THREADS + threadIdx.x; j < pairs; j += (size_t)gridDim.x * LG_THREADS) {
     gf128 f0, f1, b0, b1;
     if (fold) {
       gf128 x0 = f[4 * j], x1 = f[4 * j + 1], x2 = f[4 * j + 2], x3 = f[4 * j + 3];
-      f0 = gf_add(x0, gf_mul_p(gf_add(x0, x1), r));
-      f1 = gf_add(x2, gf_mul_p(gf_add(x2, x3), r));
       gf128 y0 = b[4 * j], y1 = b[4 * j + 1], y2 = b[4 * j + 2], y3 = b[4 * j + 3];
-      b0 = gf_add(y0, gf_mul_p(gf_add(y0, y1), r));
-      b1 = gf_add(y2, gf_mul_p(gf_add(y2, y3), r));
+      if (use_tab) {
+        f0 = gf_add(x0, gf_mul_tab(rtab, gf_add(x0, x1), rot));
+        f1 = gf_add(x2, gf_mul_tab(rtab, gf_add(x2, x3), rot));
+        b0 = gf_add(y0, gf_mul_tab(rtab, gf_add(y0, y1), rot));
+        b1 = gf_add(y2, gf_mul_tab(rtab, gf_add(y2, y3), rot));
+      } else {
+        f0 = gf_add(x0, gf_mul_p(gf_add(x0, x1), r));
+        f1 = gf_add(x2, gf_mul_p(gf_add(x2, x3), r));
+        b0 = gf_add(y0, gf_mul_p(gf_add(y0, y1), r));
+        b1 = gf_add(y2, gf_mul_p(gf_add(y2, y3), r));
+      }
       fo[2 * j] = f0; fo[2 * j + 1] = f1;
       bo[2 * j] = b0; bo[2 * j + 1] = b1;
     } else {
@@ -181,9 +194,15 @@ int flock_lig_grid(size_t n_pairs) { return (int)grid_for(n_pairs, LG_THREADS, 1
 
 int flock_launch_lig_fold_msg(const void* f, const void* b, size_t n_out, int fold, const uint64_t r[2], void* fo,
                               void* bo, void* partials, int grid, cudaStream_t st) {
-  lig_fold_msg_kernel<<<grid, LG_THREADS, 0, st>>>((const gf128*)f, (const gf128*)b, n_out, fold,
-                                                   gf_prepare(to_gf(r)),
-                                                   (gf128*)fo, (gf128*)bo, (gf128*)partials); flock_count_launch();
+  constexpr size_t kTabSmem = (size_t)(GF_TAB_ENTRIES + GF_TAB_NIBBLE_SLOTS) * 16;
+  flock_once_per_device((const void*)lig_fold_msg_kernel, [] {
+    cudaFuncSetAttribute(lig_fold_msg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTabSmem);
+  });
+  const int use_tab = fold && (n_out / 2) / (size_t)grid >= 512;
+  lig_fold_msg_kernel<<<grid, LG_THREADS, use_tab ? kTabSmem : 0, st>>>(
+      (const gf128*)f, (const gf128*)b, n_out, fold, gf_prepare(to_gf(r)), to_gf(r), use_tab, (gf128*)fo, (gf128*)bo,
+      (gf128*)partials);
+  flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 

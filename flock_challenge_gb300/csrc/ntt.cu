@@ -28,6 +28,7 @@
 
 #include "flock_internal.h"
 #include "gf128.cuh"
+#include "gf_tab.cuh"
 #include "host_field.h"
 
 namespace {
@@ -292,73 +293,16 @@ constexpr int kMaxPassLayers = variant_max_layers(kDefaultVariant);
 // t_B, t_C for the two halves at layer l + 1); each thread owns a quad of
 // positions of one lane.
 constexpr int TAB_THREADS = 512;
-constexpr int TAB_ENTRIES = 16 * 256;
-constexpr size_t TAB_SMEM = (size_t)3 * TAB_ENTRIES * 16 + (size_t)3 * 512 * 16;
+constexpr int TAB_ENTRIES = GF_TAB_ENTRIES;
+constexpr size_t TAB_SMEM = (size_t)3 * TAB_ENTRIES * 16 + (size_t)3 * GF_TAB_NIBBLE_SLOTS * 16;
 
-// t * x^i for 0 <= i < 128: shift into 256 bits, then reduce.
-__device__ __forceinline__ gf128 gf_mul_xpow_small(gf128 h, int i) {
-  const uint64_t lo = h.w[0] | ((uint64_t)h.w[1] << 32), hi = h.w[2] | ((uint64_t)h.w[3] << 32);
-  const int wsh = i >> 6, bsh = i & 63;
-  const uint64_t s0 = lo << bsh, s1 = (hi << bsh) | (bsh ? lo >> (64 - bsh) : 0), s2 = bsh ? hi >> (64 - bsh) : 0;
-  return wsh == 0 ? gf_reduce(s0, s1, s2, 0) : gf_reduce(0, s0, s1, s2);
-}
-
-__device__ __forceinline__ uint32_t sel_word(const gf128& y, uint32_t j) {
-  return (j & 2) ? ((j & 1) ? y.w[3] : y.w[2]) : ((j & 1) ? y.w[1] : y.w[0]);
-}
-
-// t * y from t's byte tables. Lane rotation rot visits byte positions rot,
-// rot + 1, ... (mod 16); table slot (v << 4) + k lies in bank group k mod 8, so
-// eight consecutive lanes (distinct rot mod 8) read eight distinct bank groups.
-__device__ __forceinline__ gf128 gf_mul_tab(const uint4* __restrict__ T, const gf128& y, uint32_t rot) {
-  const uint32_t wr = rot >> 2, br = (rot & 3) * 8;
-  uint32_t q[5];
-#pragma unroll
-  for (int i = 0; i < 4; i++) q[i] = sel_word(y, (wr + i) & 3);
-  q[4] = q[0];
-  uint32_t r[4];  // byte s of r = byte (rot + s) mod 16 of y
-#pragma unroll
-  for (int i = 0; i < 4; i++) r[i] = __funnelshift_r(q[i], q[i + 1], br);
-  uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-#pragma unroll
-  for (int st = 0; st < 16; st++) {
-    const uint32_t b = (r[st >> 2] >> (8 * (st & 3))) & 255;
-    const uint4 v = T[(b << 4) | ((rot + st) & 15)];
-    a0 ^= v.x; a1 ^= v.y; a2 ^= v.z; a3 ^= v.w;
-  }
-  gf128 o;
-  o.w[0] = a0; o.w[1] = a1; o.w[2] = a2; o.w[3] = a3;
-  return o;
-}
-
-__host__ __device__ constexpr int ctz4(int j) { return (j & 1) ? 0 : (j & 2) ? 1 : (j & 4) ? 2 : 3; }
-
-// Builds the byte tables of the three twiddles t[0..2] into T (3 x TAB_ENTRIES
-// slots). Entry (v, k) = L[v & 15][k] + H[v >> 4][k], where L[j][k] = t j x^(8k)
-// and H[g][k] = t g x^(8k + 4) are the nibble tables (each 16 values per byte
-// position, made by 32 threads per twiddle with a Gray-code walk over the
-// images t x^i); LH holds them as [twiddle][L, H][16][16 k] so that the fill's
-// reads of one step hit distinct bank groups. All threads of the CTA take part.
+// Byte tables of the three twiddles t[0..2] into T (3 x TAB_ENTRIES slots),
+// through their nibble tables in LH (3 x 512 slots). All threads take part.
 __device__ void build_tabs3(const gf128 t[3], uint4* __restrict__ T, uint4* __restrict__ LH) {
-  if (threadIdx.x < 96) {
-    const int x = threadIdx.x >> 5, part = (threadIdx.x >> 4) & 1, k = threadIdx.x & 15;
-    gf128 B[4];
-#pragma unroll
-    for (int b = 0; b < 4; b++) B[b] = gf_mul_xpow_small(t[x], 8 * k + 4 * part + b);
-    gf128 v[16];
-    v[0] = gf_zero();
-#pragma unroll
-    for (int j = 1; j < 16; j++) v[j] = gf_add(v[j & (j - 1)], B[ctz4(j)]);
-    uint4* out = LH + x * 512 + part * 256;
-#pragma unroll
-    for (int j = 0; j < 16; j++) out[j * 16 + k] = make_uint4(v[j].w[0], v[j].w[1], v[j].w[2], v[j].w[3]);
-  }
+  if (threadIdx.x < 96) gf_tab_nibbles(t[threadIdx.x >> 5], LH + (threadIdx.x >> 5) * 512, threadIdx.x & 31);
   __syncthreads();
-  for (int e = threadIdx.x; e < 3 * TAB_ENTRIES; e += blockDim.x) {
-    const int x = e / TAB_ENTRIES, r = e % TAB_ENTRIES, v = r >> 4, k = r & 15;
-    const uint4 lo = LH[x * 512 + (v & 15) * 16 + k], hi = LH[x * 512 + 256 + (v >> 4) * 16 + k];
-    T[e] = make_uint4(lo.x ^ hi.x, lo.y ^ hi.y, lo.z ^ hi.z, lo.w ^ hi.w);
-  }
+  for (int e = threadIdx.x; e < 3 * TAB_ENTRIES; e += blockDim.x)
+    T[e] = gf_tab_entry(LH + (e / TAB_ENTRIES) * 512, e % TAB_ENTRIES);
 }
 
 // Layers l, l + 1 of the transform for block hi of layer l (blockIdx.x / cph)

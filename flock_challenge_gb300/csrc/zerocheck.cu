@@ -23,6 +23,7 @@
 // packed word x >> 1), so the opening reuses it.
 #include "flock_internal.h"
 #include "gf128.cuh"
+#include "gf_tab.cuh"
 #include "zc_tables.h"
 
 namespace {
@@ -360,10 +361,16 @@ constexpr int kZcUnroll = ZC_UNROLL;
 #ifndef ZC_RND_MIN_BLOCKS
 #define ZC_RND_MIN_BLOCKS 2  // two resident blocks per SM (128 registers) measured best
 #endif
+// use_tab: the bind multiplies through rho's byte tables (gf_tab.cuh, dynamic
+// shared memory), worth their build when a CTA binds hundreds of pairs.
 __global__ void __launch_bounds__(RND_THREADS, ZC_RND_MIN_BLOCKS)
 zc_round_kernel(const gf128* __restrict__ A, const gf128* __restrict__ B, size_t n_pairs, int bind,
-                const __grid_constant__ gf128p rho, gf128* __restrict__ Aout, gf128* __restrict__ Bout, const gf128* __restrict__ eq_lo,
-                const gf128* __restrict__ eq_hi, int lo_bits, gf128* __restrict__ partials) {
+                const __grid_constant__ gf128p rho, const gf128 rho_plain, int use_tab, gf128* __restrict__ Aout,
+                gf128* __restrict__ Bout, const gf128* __restrict__ eq_lo, const gf128* __restrict__ eq_hi,
+                int lo_bits, gf128* __restrict__ partials) {
+  extern __shared__ uint4 rtab[];
+  const uint32_t rot = threadIdx.x & 15;
+  if (use_tab) gf_tab_build(rho_plain, rtab, rtab + GF_TAB_ENTRIES);
   // grid-stride over hi blocks: each CTA handles whole hi indices
   const size_t lo_n = (size_t)1 << lo_bits;
   const size_t n_hi = (n_pairs + lo_n - 1) / lo_n;
@@ -377,11 +384,18 @@ zc_round_kernel(const gf128* __restrict__ A, const gf128* __restrict__ B, size_t
       gf128 a0, a1, b0, b1;
       if (bind) {
         gf128 p0 = A[4 * j], p1 = A[4 * j + 1], p2 = A[4 * j + 2], p3 = A[4 * j + 3];
-        a0 = gf_add(p0, gf_mul_p(gf_add(p0, p1), rho));
-        a1 = gf_add(p2, gf_mul_p(gf_add(p2, p3), rho));
         gf128 q0 = B[4 * j], q1 = B[4 * j + 1], q2 = B[4 * j + 2], q3 = B[4 * j + 3];
-        b0 = gf_add(q0, gf_mul_p(gf_add(q0, q1), rho));
-        b1 = gf_add(q2, gf_mul_p(gf_add(q2, q3), rho));
+        if (use_tab) {
+          a0 = gf_add(p0, gf_mul_tab(rtab, gf_add(p0, p1), rot));
+          a1 = gf_add(p2, gf_mul_tab(rtab, gf_add(p2, p3), rot));
+          b0 = gf_add(q0, gf_mul_tab(rtab, gf_add(q0, q1), rot));
+          b1 = gf_add(q2, gf_mul_tab(rtab, gf_add(q2, q3), rot));
+        } else {
+          a0 = gf_add(p0, gf_mul_p(gf_add(p0, p1), rho));
+          a1 = gf_add(p2, gf_mul_p(gf_add(p2, p3), rho));
+          b0 = gf_add(q0, gf_mul_p(gf_add(q0, q1), rho));
+          b1 = gf_add(q2, gf_mul_p(gf_add(q2, q3), rho));
+        }
         Aout[2 * j] = a0; Aout[2 * j + 1] = a1;
         Bout[2 * j] = b0; Bout[2 * j + 1] = b1;
       } else {
@@ -511,16 +525,22 @@ __device__ __forceinline__ void block_reduce2(gf256 g1, gf256 gi, gf128* __restr
 // from the skip fold of the bit rows (as in zc_round0_skip_kernel) and are
 // written to Aout, Bout; otherwise the 2 n_pairs-entry tables in0, in1 are
 // bound at rho into Aout, Bout (as in zc_round_kernel).
+// The binding rounds multiply every entry pair by rho through rho's byte
+// tables (gf_tab.cuh), built once per CTA.
 template <bool SKIP>
 __global__ void __launch_bounds__(RND_THREADS, ZC_RND_MIN_BLOCKS)
 zc_round_grp_kernel(const void* __restrict__ in0, const void* __restrict__ in1, size_t n_pairs,
-                    const __grid_constant__ gf128p rho, const gf128* __restrict__ lag, gf128* __restrict__ Aout,
+                    const gf128 rho, const gf128* __restrict__ lag, gf128* __restrict__ Aout,
                     gf128* __restrict__ Bout, const gf128* __restrict__ eq_lo, const gf128* __restrict__ eq_hi,
                     int lo_bits, int a_bits, int m_bits, int m_mul, gf128* __restrict__ partials) {
   // SKIP: [256 v][8 c] subset sums of the Lagrange weights of byte position c;
   // entry (v, c) sits in bank group c and lane l starts at byte position l mod
-  // 8, so eight consecutive lanes read eight distinct bank groups
+  // 8, so eight consecutive lanes read eight distinct bank groups.
+  // Otherwise: rho's byte tables, then their nibble tables.
   extern __shared__ gf128 tab[];
+  uint4* rtab = reinterpret_cast<uint4*>(tab);
+  const uint32_t rot = threadIdx.x & 15;
+  if constexpr (!SKIP) gf_tab_build(rho, rtab, rtab + GF_TAB_ENTRIES);
   if constexpr (SKIP) {
     for (int e = threadIdx.x; e < 8 * 256; e += blockDim.x) {
       const int v = e >> 3, c = e & 7;
@@ -567,11 +587,11 @@ zc_round_grp_kernel(const void* __restrict__ in0, const void* __restrict__ in1, 
           const gf128* A = reinterpret_cast<const gf128*>(in0);
           const gf128* B = reinterpret_cast<const gf128*>(in1);
           const gf128 p0 = A[4 * j], p1 = A[4 * j + 1], p2 = A[4 * j + 2], p3 = A[4 * j + 3];
-          a0 = gf_add(p0, gf_mul_p(gf_add(p0, p1), rho));
-          a1 = gf_add(p2, gf_mul_p(gf_add(p2, p3), rho));
+          a0 = gf_add(p0, gf_mul_tab(rtab, gf_add(p0, p1), rot));
+          a1 = gf_add(p2, gf_mul_tab(rtab, gf_add(p2, p3), rot));
           const gf128 q0 = B[4 * j], q1 = B[4 * j + 1], q2 = B[4 * j + 2], q3 = B[4 * j + 3];
-          b0 = gf_add(q0, gf_mul_p(gf_add(q0, q1), rho));
-          b1 = gf_add(q2, gf_mul_p(gf_add(q2, q3), rho));
+          b0 = gf_add(q0, gf_mul_tab(rtab, gf_add(q0, q1), rot));
+          b1 = gf_add(q2, gf_mul_tab(rtab, gf_add(q2, q3), rot));
         }
         Aout[2 * j] = a0; Aout[2 * j + 1] = a1;
         Bout[2 * j] = b0; Bout[2 * j + 1] = b1;
@@ -635,10 +655,15 @@ int flock_launch_zc_round(const void* A, const void* B, size_t n_pairs, int bind
                           int grid, cudaStream_t st) {
   gf128 r;
   r.w[0] = (uint32_t)rho[0]; r.w[1] = (uint32_t)(rho[0] >> 32); r.w[2] = (uint32_t)rho[1]; r.w[3] = (uint32_t)(rho[1] >> 32);
-  zc_round_kernel<<<grid, RND_THREADS, 0, st>>>((const gf128*)A, (const gf128*)B, n_pairs, bind, gf_prepare(r),
-                                                (gf128*)Aout,
-                                                (gf128*)Bout, (const gf128*)eq_lo, (const gf128*)eq_hi, lo_bits,
-                                                (gf128*)partials); flock_count_launch();
+  constexpr size_t kTabSmem = (size_t)(GF_TAB_ENTRIES + GF_TAB_NIBBLE_SLOTS) * 16;
+  flock_once_per_device((const void*)zc_round_kernel, [] {
+    cudaFuncSetAttribute(zc_round_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTabSmem);
+  });
+  const int use_tab = bind && n_pairs / (size_t)grid >= 512;
+  zc_round_kernel<<<grid, RND_THREADS, use_tab ? kTabSmem : 0, st>>>(
+      (const gf128*)A, (const gf128*)B, n_pairs, bind, gf_prepare(r), r, use_tab, (gf128*)Aout, (gf128*)Bout,
+      (const gf128*)eq_lo, (const gf128*)eq_hi, lo_bits, (gf128*)partials);
+  flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
@@ -664,13 +689,17 @@ int flock_launch_zc_round_grp(const void* in0, const void* in1, size_t n_pairs, 
   if (n_pairs % per_h != 0 || grid < 1) return FLOCK_ERR_SHAPE;
   gf128 r;
   r.w[0] = (uint32_t)rho[0]; r.w[1] = (uint32_t)(rho[0] >> 32); r.w[2] = (uint32_t)rho[1]; r.w[3] = (uint32_t)(rho[1] >> 32);
+  constexpr size_t kTabSmem = (size_t)(GF_TAB_ENTRIES + GF_TAB_NIBBLE_SLOTS) * 16;
+  flock_once_per_device((const void*)zc_round_grp_kernel<false>, [] {
+    cudaFuncSetAttribute(zc_round_grp_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTabSmem);
+  });
   if (skip)
     zc_round_grp_kernel<true><<<grid, RND_THREADS, 8 * 256 * sizeof(gf128), st>>>(
-        in0, in1, n_pairs, gf_prepare(r), (const gf128*)lag, (gf128*)Aout, (gf128*)Bout, (const gf128*)eq_lo,
+        in0, in1, n_pairs, r, (const gf128*)lag, (gf128*)Aout, (gf128*)Bout, (const gf128*)eq_lo,
         (const gf128*)eq_hi, lo_bits, a_bits, m_bits, m_mul, (gf128*)partials);
   else
-    zc_round_grp_kernel<false><<<grid, RND_THREADS, 0, st>>>(
-        in0, in1, n_pairs, gf_prepare(r), (const gf128*)lag, (gf128*)Aout, (gf128*)Bout, (const gf128*)eq_lo,
+    zc_round_grp_kernel<false><<<grid, RND_THREADS, kTabSmem, st>>>(
+        in0, in1, n_pairs, r, (const gf128*)lag, (gf128*)Aout, (gf128*)Bout, (const gf128*)eq_lo,
         (const gf128*)eq_hi, lo_bits, a_bits, m_bits, m_mul, (gf128*)partials);
   flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
