@@ -348,13 +348,13 @@ ntt_tab2_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t s
   }
 }
 
-// Layers [start, end) handled by table passes: pairs of layers while at least
-// three layers remain for the multiply passes (the deep layers have too few
-// products per twiddle to pay for a table) and the lanes give reuse.
+// Layers [start, end) handled by table passes: pairs of layers while a block
+// of the pass's first layer l holds at least 2^11 quad-lanes (its three tables
+// are then built for at least 8 K products; deeper blocks are left to the
+// multiply passes).
 int tab_layers_end(int log_d, int log_lanes, int start) {
-  if (log_lanes < 6) return start;
   int l = start;
-  while (l + 1 < log_d - 3) l += 2;
+  while (l + 1 < log_d && log_d - l - 2 + log_lanes >= 11) l += 2;
   return l;
 }
 
@@ -508,8 +508,10 @@ int pick_variant(int log_d, int log_lanes, int start, const void* tw, cudaStream
 }  // namespace
 
 extern "C" int flock_ntt_tuned_variant(int device, int log_d, int log_lanes, int start_layer) {
+  // the tuned multiply passes start where the table passes end
+  const int l = tab_layers_end(log_d, log_lanes, start_layer);
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  auto it = g_tuned.find(TuneKey{device, log_d, log_lanes, start_layer});
+  auto it = g_tuned.find(TuneKey{device, log_d, log_lanes, l});
   return it == g_tuned.end() ? -1 : it->second;
 }
 

@@ -41,9 +41,11 @@ def test_witness_z_only(cuda_device):
     assert np.array_equal(host(z), oz.view(np.uint8))
 
 
-# 64+ lanes run the upper layers as byte-table passes: (7, 6, 1) .. (16, 6, 1)
+# shapes whose upper layers run as byte-table passes (a block of the pass's
+# first layer holds >= 2^11 quad-lanes): (12, 6, 1), (13, 4, 3), (10, 6, 0),
+# (9, 7, 2), (16, 6, 1), (14, 3, 2)
 @pytest.mark.parametrize("log_d,log_lanes,start", [(1, 4, 0), (5, 4, 0), (7, 6, 1), (12, 6, 1), (13, 4, 3),
-                                                   (10, 6, 0), (9, 7, 2), (16, 6, 1)])
+                                                   (10, 6, 0), (9, 7, 2), (16, 6, 1), (14, 3, 2)])
 def test_ntt_matches_oracle(ctx, log_d, log_lanes, start):
     rng = np.random.default_rng(log_d * 7 + start)
     data = rng.integers(0, 2**63, (1 << (log_d + log_lanes)) * 2, dtype=np.uint64)
