@@ -365,11 +365,26 @@ int launch_tab2(gf128* dst, const gf128* src, size_t mask, const gf128* tw, int 
   });
   const size_t n_hi = (size_t)1 << l;
   const size_t items = ((size_t)1 << (log_d - l - 2)) << log_lanes;
-  // about two CTAs per SM in all, each with at least one item per thread
-  size_t cph = (304 + n_hi - 1) / n_hi;
-  const size_t max_cph = (items + TAB_THREADS - 1) / TAB_THREADS;
-  if (cph > max_cph) cph = max_cph;
-  if (cph < 1) cph = 1;
+  // CTAs per block (one resident CTA per SM): minimise waves x per-CTA time,
+  // a CTA costing its table build (about 700 products) plus its share of the
+  // block's 4 products per quad-lane, with at least one item per thread
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 152;
+  }
+  size_t cph = 1;
+  double best = 1e300;
+  for (size_t c : {1, 2, 4, 8, 16, 19, 32, 38, 64, 76, 128, 152, 256, 304, 512}) {
+    if (c > 1 && items / c < TAB_THREADS) continue;
+    const double waves = (double)((n_hi * c + sms - 1) / sms);
+    const double t = waves * (700.0 + 4.0 * (double)items / (double)c);
+    if (t < best) {
+      best = t;
+      cph = c;
+    }
+  }
   ntt_tab2_kernel<<<(unsigned)(n_hi * cph), TAB_THREADS, TAB_SMEM, st>>>(dst, src, mask, tw, log_d, log_lanes, l,
                                                                          (int)cph);
   flock_count_launch();
