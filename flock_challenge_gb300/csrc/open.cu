@@ -145,18 +145,28 @@ combined_basis_kernel(int lo_bits, int slices, const gf128* __restrict__ lo0, co
 // s_hat_v of the ab claim from lincheck's pre-sumcheck z_vec (ring_switch.rs:1275-1325):
 // packed word pos = outer * 128 + (i >> 7), bit b = i & 127, so
 // s_hat_v[b] = sum_{h < 128} eq_tail[h] * z_vec[h * 128 + b].
-__global__ void shv_from_zvec_kernel(const gf128* __restrict__ zvec, const gf128* __restrict__ eq_tail,
-                                     gf128* __restrict__ out) {
-  int b = threadIdx.x;
+// One CTA of 512 threads: thread (q, b) sums h in [32 q, 32 q + 32), then
+// the four partial sums of each b are XORed in shared memory.
+__global__ void __launch_bounds__(512)
+shv_from_zvec_kernel(const gf128* __restrict__ zvec, const gf128* __restrict__ eq_tail, gf128* __restrict__ out) {
+  __shared__ gf128 red[4][128];
+  const int b = threadIdx.x & 127, q = threadIdx.x >> 7;
   gf256 acc = {{0, 0, 0, 0}};
-  for (int h = 0; h < 128; h++) gf256_acc(acc, gf_mul_wide(eq_tail[h], zvec[h * 128 + b]));
-  out[b] = gf256_reduce(acc);
+#pragma unroll 2
+  for (int h = 32 * q; h < 32 * q + 32; h++) gf256_acc(acc, gf_mul_wide(eq_tail[h], zvec[h * 128 + b]));
+  red[q][b] = gf256_reduce(acc);
+  __syncthreads();
+  if (q == 0) {
+    gf128 v = red[0][b];
+    for (int k = 1; k < 4; k++) v = gf_add(v, red[k][b]);
+    out[b] = v;
+  }
 }
 
 }  // namespace
 
 int flock_launch_shv_from_zvec(const void* zvec, const void* eq_tail, void* out, cudaStream_t st) {
-  shv_from_zvec_kernel<<<1, 128, 0, st>>>((const gf128*)zvec, (const gf128*)eq_tail, (gf128*)out);
+  shv_from_zvec_kernel<<<1, 512, 0, st>>>((const gf128*)zvec, (const gf128*)eq_tail, (gf128*)out);
   flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }

@@ -385,10 +385,21 @@ void write_open(Wire& w, const Open& o) {
 }
 
 // Reduce `count` partial rows of `width` F128 on the device, copy to host.
+// Reduce `count` partial rows of `width` F128 (XOR), result on the host. Up to
+// 64 KiB of partials are copied and reduced on the host (one transfer instead
+// of a reduction launch plus a transfer on the round's critical path); wider
+// ones are reduced on the device first.
 std::vector<F> reduce_partials(ProverState& S, const void* part, size_t count, int width) {
+  std::vector<F> out(width);
+  if (count * (size_t)width <= 4096) {
+    std::vector<F> rows(count * (size_t)width);
+    d2h(S, rows.data(), part, rows.size() * 16);
+    for (size_t c = 0; c < count; c++)
+      for (int k = 0; k < width; k++) out[k] += rows[c * width + k];
+    return out;
+  }
   void* r = S.red.get((size_t)width * 16);
   FK(flock_launch_reduce_rows(part, count, width, r, S.st));
-  std::vector<F> out(width);
   d2h(S, out.data(), r, (size_t)width * 16);
   return out;
 }
@@ -690,15 +701,17 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       void* dzv = S->zvec.get(FLOCK_K * 16);
       FK(flock_launch_reduce_rows(dpart, grid, FLOCK_K, dzv, st));
       CK(cudaMemcpyAsync(S->zvec0.get(FLOCK_K * 16), dzv, FLOCK_K * 16, cudaMemcpyDeviceToDevice, st));
-      void* dmsg = S->lcmsg.get(32);
+      // product sumcheck on (comb, z_vec) binding the top variable
+      // (lincheck.rs:1242-1300): the same round as the chain shift sumcheck
       size_t len = FLOCK_K;
       for (int t = 0; t < inner_rest; t++) {
         uint64_t rp[2] = {0, 0};
         if (t > 0) u2(lc_rr.back(), rp);
         if (t > 0) len /= 2;
-        FK(flock_launch_lc_round(dcomb, dzv, len, t > 0, rp, 1, dmsg, st));
-        F msg[2];
-        d2h(*S, msg, dmsg, 32);
+        const int grid = flock_chain_round_grid(len);
+        void* dpart = S->part.get((size_t)grid * 2 * 16);
+        FK(flock_launch_chain_round(dcomb, dzv, len, t > 0, rp, dpart, grid, st));
+        auto msg = reduce_partials(*S, dpart, grid, 2);
         tr.observe(msg[0]);
         tr.observe(msg[1]);
         lc_rounds.push_back({msg[0], msg[1]});
@@ -706,7 +719,11 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       }
       uint64_t rp[2];
       u2(lc_rr.back(), rp);
-      FK(flock_launch_lc_round(dcomb, dzv, len / 2, 1, rp, 0, dmsg, st));
+      {  // final bind to the 64 entries of z_partial (its message is not used)
+        const int grid = flock_chain_round_grid(len / 2);
+        void* dpart = S->part.get((size_t)grid * 2 * 16);
+        FK(flock_launch_chain_round(dcomb, dzv, len / 2, 1, rp, dpart, grid, st));
+      }
       d2h(*S, z_partial.data(), dzv, 64 * 16);
     }
     tr.observe_slice(z_partial.data(), 64);
