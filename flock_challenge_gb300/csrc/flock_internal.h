@@ -40,12 +40,7 @@ int flock_launch_lc_comb(const uint32_t* a_ptr, const uint32_t* a_idx, const uin
                          const uint32_t* b_idx, const void* eq, const uint64_t alpha[2], const uint64_t beta[2],
                          int pin, void* comb, cudaStream_t st);
 int flock_launch_lc_quirky_eq(const void* lag, const void* x_rest, int n_rest, void* out, cudaStream_t st);
-int flock_launch_lc_round(void* c, void* z, size_t n, int bind, const uint64_t r[2], int emit, void* out,
-                          cudaStream_t st);
 
-int flock_launch_s_hat_v(const void* z, size_t n, const void* t_lo, const void* t_hi, int lo_bits, void* partials,
-                         int grid, cudaStream_t st);
-int flock_s_hat_v_warps(int grid);
 int flock_launch_shv_from_zvec(const void* zvec, const void* eq_tail, void* out, cudaStream_t st);
 int flock_launch_combined_basis(size_t n, const void* t0_lo, const void* t0_hi, const void* t1_lo,
                                 const void* t1_hi, int lo_bits, const void* tables, void* b, cudaStream_t st);

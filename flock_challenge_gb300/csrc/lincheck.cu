@@ -6,8 +6,8 @@
 //    (lincheck.rs:655-720);
 //  * comb: alpha * A0^T eq_inner + B0^T eq_inner (+ beta at the constant
 //    column) gathered column-wise from a CSC copy of the base matrices;
-//  * product sumcheck rounds over (comb, z_vec), binding the top variable
-//    (lincheck.rs:1242-1300), in one CTA per round.
+//  (the product sumcheck rounds over (comb, z_vec), binding the top variable
+//  (lincheck.rs:1242-1300), run on flock_launch_chain_round).
 #include "flock_internal.h"
 #include "gf128.cuh"
 
@@ -126,49 +126,6 @@ __global__ void lc_quirky_eq_kernel(const gf128* __restrict__ lag, const gf128* 
   out[i] = gf_mul(lag[s], e);
 }
 
-// One product-sumcheck round on (c, z) of length n (top-variable split), with
-// the previous round's top bind fused in when bind != 0:
-//   bind: v[i] <- v[i] + r (v[i + n] + v[i]) for the incoming length 2n
-//   msg:  e1 = sum c_hi z_hi, einf = sum (c_hi + c_lo)(z_hi + z_lo)
-// Single CTA; msg written to out[0..2].
-constexpr int LR_THREADS = 1024;
-__global__ void __launch_bounds__(LR_THREADS)
-lc_round_kernel(gf128* __restrict__ c, gf128* __restrict__ z, size_t n, int bind, gf128 r, int emit,
-                gf128* __restrict__ out) {
-  if (bind) {
-    for (size_t i = threadIdx.x; i < n; i += LR_THREADS) {
-      gf128 c0 = c[i], c1 = c[i + n], z0 = z[i], z1 = z[i + n];
-      c[i] = gf_add(c0, gf_mul(r, gf_add(c1, c0)));
-      z[i] = gf_add(z0, gf_mul(r, gf_add(z1, z0)));
-    }
-    __syncthreads();
-  }
-  if (!emit) return;
-  size_t half = n / 2;
-  gf256 e1 = {{0, 0, 0, 0}}, ei = {{0, 0, 0, 0}};
-  for (size_t i = threadIdx.x; i < half; i += LR_THREADS) {
-    gf128 cl = c[i], ch = c[i + half], zl = z[i], zh = z[i + half];
-    gf256_acc(e1, gf_mul_wide(ch, zh));
-    gf256_acc(ei, gf_mul_wide(gf_add(ch, cl), gf_add(zh, zl)));
-  }
-  __shared__ gf256 red[2][LR_THREADS / 32];
-  for (int off = 16; off > 0; off >>= 1)
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      e1.r[k] ^= __shfl_xor_sync(0xffffffffu, e1.r[k], off);
-      ei.r[k] ^= __shfl_xor_sync(0xffffffffu, ei.r[k], off);
-    }
-  int w = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0) { red[0][w] = e1; red[1][w] = ei; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    gf256 s1 = {{0, 0, 0, 0}}, si = {{0, 0, 0, 0}};
-    for (int k = 0; k < LR_THREADS / 32; k++) { gf256_acc(s1, red[0][k]); gf256_acc(si, red[1][k]); }
-    out[0] = gf256_reduce(s1);
-    out[1] = gf256_reduce(si);
-  }
-}
-
 inline gf128 to_gf(const uint64_t v[2]) {
   gf128 r;
   r.w[0] = (uint32_t)v[0]; r.w[1] = (uint32_t)(v[0] >> 32); r.w[2] = (uint32_t)v[1]; r.w[3] = (uint32_t)(v[1] >> 32);
@@ -204,8 +161,3 @@ int flock_launch_lc_quirky_eq(const void* lag, const void* x_rest, int n_rest, v
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
-int flock_launch_lc_round(void* c, void* z, size_t n, int bind, const uint64_t r[2], int emit, void* out,
-                          cudaStream_t st) {
-  lc_round_kernel<<<1, LR_THREADS, 0, st>>>((gf128*)c, (gf128*)z, n, bind, to_gf(r), emit, (gf128*)out); flock_count_launch();
-  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
-}

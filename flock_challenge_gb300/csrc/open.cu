@@ -1,10 +1,7 @@
 // Ring-switch kernels of the PCS opening (crates/flock-core/src/pcs/ring_switch.rs).
 //
-//  * s_hat_v[b] = sum_pos bit_b(z[pos]) t(pos), t = eq(suffix) (ring_switch.rs:1568-1620):
-//    t(pos) = t_lo[pos & lo_mask] * t_hi[pos >> lo_bits]; each warp handles
-//    whole hi blocks, folding eight positions at a time through a 256-entry
-//    subset-sum table of t_lo, and multiplies its 128 accumulators by t_hi once
-//    per block. Lane l owns bits 4l..4l+3.
+//  * s_hat_v of the ab claim from lincheck's z_vec (ring_switch.rs:1275-1325);
+//    the c claim's comes out of zerocheck round 1, so z is never re-read;
 //  * combined basis b[pos] = sum_k gamma_k sum_b bit_b(t_k(pos)) eq(r''_k)[b]
 //    (ring_switch.rs:1720-1760, pcs.rs:1080-1110), t_k = eq tensor of the
 //    claim's suffix: per high index, byte tables of the linear map
@@ -13,59 +10,6 @@
 #include "gf128.cuh"
 
 namespace {
-
-constexpr int SH_THREADS = 256;
-
-__global__ void __launch_bounds__(SH_THREADS)
-s_hat_v_kernel(const gf128* __restrict__ z, size_t n, const gf128* __restrict__ t_lo,
-               const gf128* __restrict__ t_hi, int lo_bits, gf128* __restrict__ partials) {
-  __shared__ gf128 tabs[SH_THREADS / 32][256];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  gf128* tab = tabs[warp];
-  const size_t lo_n = (size_t)1 << lo_bits;
-  const size_t n_hi = n >> lo_bits;
-  gf128 tot[4];
-#pragma unroll
-  for (int q = 0; q < 4; q++) tot[q] = gf_zero();
-  const size_t gw = (size_t)blockIdx.x * (SH_THREADS / 32) + warp;
-  const size_t nw = (size_t)gridDim.x * (SH_THREADS / 32);
-  const int word = lane >> 3, shift = (lane & 7) * 4;  // bits 4*lane .. 4*lane+3
-  for (size_t h = gw; h < n_hi; h += nw) {
-    gf128 acc[4];
-#pragma unroll
-    for (int q = 0; q < 4; q++) acc[q] = gf_zero();
-    for (size_t g = 0; g < lo_n; g += 8) {
-      // subset-sum table of t_lo[g..g+8): 8 entries per lane
-      __syncwarp();
-#pragma unroll
-      for (int k = 0; k < 8; k++) {
-        int v = lane * 8 + k;
-        gf128 s = gf_zero();
-#pragma unroll
-        for (int r = 0; r < 8; r++)
-          if ((v >> r) & 1) s = gf_add(s, t_lo[g + r]);
-        tab[v] = s;
-      }
-      __syncwarp();
-      uint32_t nib[8];
-#pragma unroll
-      for (int r = 0; r < 8; r++) nib[r] = (reinterpret_cast<const uint32_t*>(&z[h * lo_n + g + r])[word] >> shift) & 15;
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        uint32_t byte = 0;
-#pragma unroll
-        for (int r = 0; r < 8; r++) byte |= ((nib[r] >> q) & 1) << r;
-        if (byte) acc[q] = gf_add(acc[q], tab[byte]);
-      }
-    }
-    gf128 e = t_hi[h];
-#pragma unroll
-    for (int q = 0; q < 4; q++) tot[q] = gf_add(tot[q], gf_mul(acc[q], e));
-  }
-  gf128* out = partials + gw * 128 + 4 * lane;
-#pragma unroll
-  for (int q = 0; q < 4; q++) out[q] = tot[q];
-}
 
 constexpr int CB_THREADS = 256;
 constexpr size_t CB_SMEM = (size_t)2 * 16 * 256 * 16 + 2 * 128 * 16;
@@ -171,13 +115,6 @@ int flock_launch_shv_from_zvec(const void* zvec, const void* eq_tail, void* out,
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
-int flock_launch_s_hat_v(const void* z, size_t n, const void* t_lo, const void* t_hi, int lo_bits, void* partials,
-                         int grid, cudaStream_t st) {
-  s_hat_v_kernel<<<grid, SH_THREADS, 0, st>>>((const gf128*)z, n, (const gf128*)t_lo, (const gf128*)t_hi, lo_bits,
-                                              (gf128*)partials); flock_count_launch();
-  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
-}
-int flock_s_hat_v_warps(int grid) { return grid * (SH_THREADS / 32); }
 
 int flock_launch_combined_basis(size_t n, const void* t0_lo, const void* t0_hi, const void* t1_lo, const void* t1_hi,
                                 int lo_bits, const void* w, void* b, cudaStream_t st) {

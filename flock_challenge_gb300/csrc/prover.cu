@@ -281,7 +281,7 @@ struct ProverState {
   cudaStream_t st = nullptr;
   ZcRound1Tables* d_r1t = nullptr;
   DBuf in, z, a, b, stripe, cw, tree, A0, B0, A1, B1, eqlo, eqhi, eqout, rdev, part, red, lag, small, eqin, comb,
-      zvec, zvec0, lcmsg, tlo0, thi0, tlo1, thi1, tables, bc, f1, b1, W, LO, HI, basis, qbuf, abuf, rows, nidx, nodes,
+      zvec, zvec0, tlo0, thi0, tlo1, thi1, tables, bc, f1, b1, W, LO, HI, basis, qbuf, abuf, rows, nidx, nodes,
       grind, lvl_cw[2], lvl_tree[2], chW, chG;
   DBuf csc_ap, csc_ai, csc_bp, csc_bi;
   bool csc_ready = false;
@@ -294,7 +294,7 @@ struct ProverState {
 
   std::vector<DBuf*> bufs() {
     return {&in, &z, &a, &b, &stripe, &cw, &tree, &A0, &B0, &A1, &B1, &eqlo, &eqhi, &eqout, &rdev, &part, &red,
-            &lag, &small, &eqin, &comb, &zvec, &zvec0, &lcmsg, &tlo0, &thi0, &tlo1, &thi1, &tables, &bc, &f1, &b1,
+            &lag, &small, &eqin, &comb, &zvec, &zvec0, &tlo0, &thi0, &tlo1, &thi1, &tables, &bc, &f1, &b1,
             &W, &LO, &HI, &basis, &qbuf, &abuf, &rows, &nidx, &nodes, &grind, &lvl_cw[0], &lvl_cw[1],
             &lvl_tree[0], &lvl_tree[1], &chW, &chG, &csc_ap, &csc_ai, &csc_bp, &csc_bi};
   }
