@@ -368,12 +368,9 @@ int launch_tab2(gf128* dst, const gf128* src, size_t mask, const gf128* tw, int 
   // CTAs per block (one resident CTA per SM): minimise waves x per-CTA time,
   // a CTA costing its table build (about 700 products) plus its share of the
   // block's 4 products per quad-lane, with at least one item per thread
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 152;
-  }
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 152;
   size_t cph = 1;
   double best = 1e300;
   for (size_t c : {1, 2, 4, 8, 16, 19, 32, 38, 64, 76, 128, 152, 256, 304, 512}) {
