@@ -370,8 +370,8 @@ def run_gpu(args):
         if args.forms and ws == 1:
             from flock_challenge_gb300 import forms
             plain = forms.PlainProver()
-            line["forms"] = {"batched": forms.run_batched(64, 3, plain=plain),
-                             "serving": forms.run_serving((8.0, 24.0, 40.0), 60, 3, plain=plain)}
+            line["forms"] = {"batched": forms.run_batched(64, 4, plain=plain),
+                             "serving": forms.run_serving((8.0, 24.0, 40.0), 60, 4, plain=plain)}
         print(json.dumps(line))
     if ws > 1:
         torch.distributed.destroy_process_group()

@@ -1,6 +1,6 @@
 """Batched and served proving measured against the plain GPU path.
 
-python -m flock_challenge_gb300.forms [--batch 64] [--requests 60] [--rates 4,8] [--workers 3]
+python -m flock_challenge_gb300.forms [--batch 64] [--requests 60] [--rates 4,8] [--workers 4]
 
 Batched form: `count` proofs whose sizes are drawn log-uniformly from
 2^12..2^18 compressions (seeds 0..count-1) go through one server with
@@ -43,7 +43,7 @@ class PlainProver:
         return self.setups[log2].prove_seed(seed)
 
 
-def run_batched(count=64, workers=3, seed=20260, plain=None):
+def run_batched(count=64, workers=4, seed=20260, plain=None):
     sizes = log_uniform_sizes(count, 12, 18, seed)
     seeds = list(range(count))
     total = sum(1 << l for l in sizes)
@@ -66,7 +66,7 @@ def run_batched(count=64, workers=3, seed=20260, plain=None):
             "all_verified": verified}
 
 
-def run_serving(rates=(4.0, 8.0), requests=60, workers=3, budget_gb=120, seed=777, plain=None):
+def run_serving(rates=(4.0, 8.0), requests=60, workers=4, budget_gb=120, seed=777, plain=None):
     budget = int(budget_gb * (1 << 30))
     out = []
     plain = plain or PlainProver()
@@ -130,7 +130,7 @@ def main(argv=None):
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--requests", type=int, default=60)
     ap.add_argument("--rates", default="4,8")
-    ap.add_argument("--workers", type=int, default=3)
+    ap.add_argument("--workers", type=int, default=4)
     a = ap.parse_args(argv)
     plain = PlainProver()
     res = {"batched": run_batched(a.batch, a.workers, plain=plain),
