@@ -4,10 +4,9 @@
 // table entries, one per byte of y, with no carry-less multiply. Worth it when
 // one CTA multiplies many elements by the same t (NTT twiddles of the upper
 // layers, a sumcheck round's binding challenge). Slot (v << 4) + k lies in
-// bank group k mod 8 and a thread with rotation rot visits byte positions
-// rot, rot + 1, ... (mod 16), so eight consecutive threads with distinct rot
-// mod 8 read eight distinct bank groups: the random lookups are
-// conflict-free.
+// bank group k mod 8 and a thread visits the byte positions in an order
+// XORed with its index mod 8, so eight consecutive threads read eight
+// distinct bank groups: the random lookups are conflict-free.
 #pragma once
 #include "gf128.cuh"
 
@@ -26,21 +25,31 @@ __device__ __forceinline__ uint32_t gf_sel_word(const gf128& y, uint32_t j) {
   return (j & 2) ? ((j & 1) ? y.w[3] : y.w[2]) : ((j & 1) ? y.w[1] : y.w[0]);
 }
 
-// t * y from t's byte tables T.
+// t * y from t's byte tables T. The thread visits byte position k = st ^ rot at
+// step st (rot = thread index mod 8), so at every step eight consecutive
+// threads read eight distinct bank groups (k mod 8 = (st mod 8) ^ rot). The
+// bytes of y are permuted once to that order (a word swap for rot's bit 2, a
+// byte permutation for its bits 0..1), after which each step is a byte move,
+// one logic op for the slot offset, the load and the XOR.
 __device__ __forceinline__ gf128 gf_mul_tab(const uint4* __restrict__ T, const gf128& y, uint32_t rot) {
-  const uint32_t wr = rot >> 2, br = (rot & 3) * 8;
-  uint32_t q[5];
+  rot &= 7;
+  // permuted byte st of yp = byte st ^ rot of y
+  const bool sw = rot & 4;
+  uint32_t yp[4] = {sw ? y.w[1] : y.w[0], sw ? y.w[0] : y.w[1], sw ? y.w[3] : y.w[2], sw ? y.w[2] : y.w[3]};
+  const uint32_t x3 = rot & 3;
+  const uint32_t perm = x3 == 0 ? 0x3210u : x3 == 1 ? 0x2301u : x3 == 2 ? 0x1032u : 0x0123u;
 #pragma unroll
-  for (int i = 0; i < 4; i++) q[i] = gf_sel_word(y, (wr + i) & 3);
-  q[4] = q[0];
-  uint32_t r[4];  // byte s of r = byte (rot + s) mod 16 of y
-#pragma unroll
-  for (int i = 0; i < 4; i++) r[i] = __funnelshift_r(q[i], q[i + 1], br);
+  for (int i = 0; i < 4; i++) yp[i] = __byte_perm(yp[i], 0, perm);
+  const uint32_t xk = rot << 4;  // byte offset of the position XOR
+  const char* base = reinterpret_cast<const char*>(T);
   uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
 #pragma unroll
   for (int st = 0; st < 16; st++) {
-    const uint32_t b = (r[st >> 2] >> (8 * (st & 3))) & 255;
-    const uint4 v = T[(b << 4) | ((rot + st) & 15)];
+    // byte st of yp placed at bits 8..15 = v << 8; slot (v << 4) | (st ^ rot) is
+    // byte offset (v << 8) | ((st ^ rot) << 4)
+    const uint32_t vb = __byte_perm(yp[st >> 2], 0, 0x4404u | ((uint32_t)(st & 3) << 4));
+    const uint32_t off = (vb | ((uint32_t)st << 4)) ^ xk;
+    const uint4 v = *reinterpret_cast<const uint4*>(base + off);
     a0 ^= v.x; a1 ^= v.y; a2 ^= v.z; a3 ^= v.w;
   }
   gf128 o;
