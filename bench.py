@@ -222,7 +222,7 @@ def kernel_roofline(F, ctx_handle, stream_ptr, log2, peaks, torch, dev):
     achieved = alg / (ms * 1e-3) / 1e9
     muls = (log_d - 1) * (1 << (log_d - 1)) * 64
     return {"kernel": f"L0 commit NTT (layers 1..{log_d - 1}: {tab_passes} two-layer table passes, then "
-                      f"{passes - tab_passes} multiply passes of <= {max_f} layers)",
+                      f"{passes - tab_passes} multiply pass(es) of <= {max_f} layers)",
             "bound": "hbm",
             "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
             "traffic": (passes * NTT_TRAFFIC_PER_PASS[log_d]) if log_d in NTT_TRAFFIC_PER_PASS else None,
