@@ -282,7 +282,7 @@ struct ProverState {
   ZcRound1Tables* d_r1t = nullptr;
   DBuf in, z, a, b, stripe, cw, tree, A0, B0, A1, B1, eqlo, eqhi, eqout, rdev, part, red, lag, small, eqin, comb,
       zvec, zvec0, tlo0, thi0, tlo1, thi1, tables, bc, f1, b1, W, LO, HI, basis, qbuf, abuf, rows, nidx, nodes,
-      grind, lvl_cw[2], lvl_tree[2], chW, chG;
+      grind, lvl_cw[2], lvl_tree[2], chW, chG, eqlo2, eqhi2;
   DBuf csc_ap, csc_ai, csc_bp, csc_bi;
   bool csc_ready = false;
   FlockPhaseTimes times;
@@ -291,12 +291,16 @@ struct ProverState {
   // copies asynchronous); device->host reads go through the last kPinD2H bytes.
   uint8_t* pin = nullptr;
   size_t pin_off = 0;
+  // Mapped pinned area for round partials: kernels write them straight into
+  // host memory, so reading a round's message needs only the stream sync.
+  uint8_t* mapped = nullptr;
+  void* mapped_dev = nullptr;
 
   std::vector<DBuf*> bufs() {
     return {&in, &z, &a, &b, &stripe, &cw, &tree, &A0, &B0, &A1, &B1, &eqlo, &eqhi, &eqout, &rdev, &part, &red,
             &lag, &small, &eqin, &comb, &zvec, &zvec0, &tlo0, &thi0, &tlo1, &thi1, &tables, &bc, &f1, &b1,
             &W, &LO, &HI, &basis, &qbuf, &abuf, &rows, &nidx, &nodes, &grind, &lvl_cw[0], &lvl_cw[1],
-            &lvl_tree[0], &lvl_tree[1], &chW, &chG, &csc_ap, &csc_ai, &csc_bp, &csc_bi};
+            &lvl_tree[0], &lvl_tree[1], &chW, &chG, &eqlo2, &eqhi2, &csc_ap, &csc_ai, &csc_bp, &csc_bi};
   }
   std::vector<const DBuf*> bufs() const {
     auto v = const_cast<ProverState*>(this)->bufs();
@@ -306,7 +310,7 @@ struct ProverState {
 
 namespace {
 
-constexpr size_t kPinH2D = (size_t)4 << 20, kPinD2H = (size_t)1 << 20;
+constexpr size_t kPinH2D = (size_t)4 << 20, kPinD2H = (size_t)1 << 20, kMapped = (size_t)256 << 10;
 
 void h2d(ProverState& S, void* d, const void* h, size_t n) {
   if (n == 0) return;
@@ -391,6 +395,13 @@ void write_open(Wire& w, const Open& o) {
 // ones are reduced on the device first.
 std::vector<F> reduce_partials(ProverState& S, const void* part, size_t count, int width) {
   std::vector<F> out(width);
+  if (S.mapped && part == S.mapped_dev) {  // written by the kernel into host memory
+    CK(cudaStreamSynchronize(S.st));
+    const F* rows = reinterpret_cast<const F*>(S.mapped);
+    for (size_t c = 0; c < count; c++)
+      for (int k = 0; k < width; k++) out[k] += rows[c * width + k];
+    return out;
+  }
   if (count * (size_t)width <= 4096) {
     std::vector<F> rows(count * (size_t)width);
     d2h(S, rows.data(), part, rows.size() * 16);
@@ -402,6 +413,13 @@ std::vector<F> reduce_partials(ProverState& S, const void* part, size_t count, i
   FK(flock_launch_reduce_rows(part, count, width, r, S.st));
   d2h(S, out.data(), r, (size_t)width * 16);
   return out;
+}
+
+// Partials buffer of a round: the mapped host area when it fits (one round
+// at a time: reduce_partials reads it before the next round is launched).
+void* part_buf(ProverState& S, size_t bytes) {
+  if (S.mapped && bytes <= kMapped) return S.mapped_dev;
+  return S.part.get(bytes);
 }
 
 void eq_split_dev(ProverState& S, const std::vector<F>& r, int lo_bits, DBuf& lo, DBuf& hi) {
@@ -424,6 +442,12 @@ ProverState* flock_prover_create(int device) {
   void* pin = nullptr;
   if (cudaMallocHost(&pin, kPinH2D + kPinD2H) == cudaSuccess) S->pin = (uint8_t*)pin;
   else cudaGetLastError();
+  void* m = nullptr;
+  if (cudaHostAlloc(&m, kMapped, cudaHostAllocMapped) == cudaSuccess) {
+    if (cudaHostGetDevicePointer(&S->mapped_dev, m, 0) == cudaSuccess) S->mapped = (uint8_t*)m;
+    else cudaFreeHost(m);
+  }
+  cudaGetLastError();
   return S;
 }
 
@@ -433,6 +457,7 @@ void flock_prover_destroy(ProverState* S) {
   if (S->d_r1t) cudaFree(S->d_r1t);
   if (S->st) cudaStreamDestroy(S->st);
   if (S->pin) cudaFreeHost(S->pin);
+  if (S->mapped) cudaFreeHost(S->mapped);
   delete S;
 }
 
@@ -604,47 +629,67 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     void *curA = dA0, *curB = dB0, *nxtA = dA1, *nxtB = dB1;
     // r[9..12] = g / (1 + g), g = x^(2^(k-9)): eq(r_k, b) = (1 + r_k) x^(b 2^(k-9))
     auto shift_var = [&](int k) { return (F::one() + r[k]) * F(1ULL << (1 << (k - 9)), 0) == r[k]; };
-    for (int i = 0; i < n_mlv; i++) {
-      size_t n_pairs = rows0 >> (i + 1);  // pairs of the round-i table
+    // Per-round eq layout. The tables depend on r only, so round i + 1's are
+    // launched right after round i's kernel and build while the host waits
+    // for round i's message (two buffer pairs, alternating).
+    struct RoundEq {
+      bool grp;
+      int a_bits, m_bits, f0, lob;
+      F dinv;
+    };
+    DBuf* eqbuf[2][2] = {{&S->eqlo, &S->eqhi}, {&S->eqlo2, &S->eqhi2}};
+    auto round_eq = [&](int i, bool launch) {
       std::vector<F> rr(r.begin() + 6 + i + 1, r.end());
-      int nv = (int)rr.size();
-      uint64_t rp[2] = {0, 0};
-      if (i > 0) u2(rho.back(), rp);
+      const int nv = (int)rr.size();
       // lowest variables of rr that are fixed challenges: phi8 ones (r7, r8)
       // and shift ones (r9..r12); rounds 0..5 factor their eq weight
-      const int a_bits = std::max(0, 2 - i), f0 = std::max(9, 7 + i), m_bits = std::max(0, 13 - f0);
-      bool grp = m_bits > 0 && nv > a_bits + m_bits;
-      for (int k = f0; grp && k < 13; k++) grp = shift_var(k);
-      std::vector<F> g;
-      if (grp) {
-        F dinv = F::one();
-        for (int k = f0; k < 13; k++) dinv = dinv * (F::one() + r[k]);
-        std::vector<F> rg(rr.begin(), rr.begin() + a_bits);
-        rg.insert(rg.end(), rr.begin() + a_bits + m_bits, rr.end());
-        const int lob = std::min(nv - m_bits, 8);
-        eq_split_dev(*S, rg, lob, S->eqlo, S->eqhi);
-        int grid = (int)std::min<size_t>(n_pairs >> (lob + m_bits), 152 * 4);
-        void* dpart = S->part.get((size_t)grid * 2 * 16);
-        FK(flock_launch_zc_round_grp(i == 0 ? da : curA, i == 0 ? db : curB, n_pairs, i == 0, rp, dlag,
-                                     i == 0 ? dA0 : nxtA, i == 0 ? dB0 : nxtB, S->eqlo.p, S->eqhi.p, lob, a_bits,
-                                     m_bits, 1 << (f0 - 9), dpart, grid, st));
-        g = reduce_partials(*S, dpart, grid, 2);
-        g[0] = g[0] * dinv;
-        g[1] = g[1] * dinv;
+      RoundEq q;
+      q.a_bits = std::max(0, 2 - i);
+      q.f0 = std::max(9, 7 + i);
+      q.m_bits = std::max(0, 13 - q.f0);
+      q.grp = q.m_bits > 0 && nv > q.a_bits + q.m_bits;
+      for (int k = q.f0; q.grp && k < 13; k++) q.grp = shift_var(k);
+      q.dinv = F::one();
+      if (q.grp) {
+        for (int k = q.f0; k < 13; k++) q.dinv = q.dinv * (F::one() + r[k]);
+        std::vector<F> rg(rr.begin(), rr.begin() + q.a_bits);
+        rg.insert(rg.end(), rr.begin() + q.a_bits + q.m_bits, rr.end());
+        q.lob = std::min(nv - q.m_bits, 8);
+        if (launch) eq_split_dev(*S, rg, q.lob, *eqbuf[i & 1][0], *eqbuf[i & 1][1]);
       } else {
-        int lob = std::min(nv, 12);
-        eq_split_dev(*S, rr, lob, S->eqlo, S->eqhi);
-        int grid = (int)std::min<size_t>(((n_pairs >> lob) + 0), 152 * 4);
-        if (grid < 1) grid = 1;
-        void* dpart = S->part.get((size_t)grid * 2 * 16);
-        if (i == 0)  // skip fold (multilinear.rs:598-630) fused into round 0
-          FK(flock_launch_zc_round0_skip(da, db, n_pairs, dlag, dA0, dB0, S->eqlo.p, S->eqhi.p, lob, dpart, grid,
-                                         st));
-        else
-          FK(flock_launch_zc_round(curA, curB, n_pairs, 1, rp, nxtA, nxtB, S->eqlo.p, S->eqhi.p, lob, dpart, grid,
-                                   st));
-        g = reduce_partials(*S, dpart, grid, 2);
+        q.lob = std::min(nv, 12);
+        if (launch) eq_split_dev(*S, rr, q.lob, *eqbuf[i & 1][0], *eqbuf[i & 1][1]);
       }
+      return q;
+    };
+    RoundEq qn = round_eq(0, true);
+    for (int i = 0; i < n_mlv; i++) {
+      const size_t n_pairs = rows0 >> (i + 1);  // pairs of the round-i table
+      const RoundEq q = qn;
+      const void* elo = eqbuf[i & 1][0]->p;
+      const void* ehi = eqbuf[i & 1][1]->p;
+      uint64_t rp[2] = {0, 0};
+      if (i > 0) u2(rho.back(), rp);
+      int grid;
+      void* dpart;
+      if (q.grp) {
+        grid = (int)std::min<size_t>(n_pairs >> (q.lob + q.m_bits), 152 * 4);
+        dpart = part_buf(*S, (size_t)grid * 2 * 16);
+        FK(flock_launch_zc_round_grp(i == 0 ? da : curA, i == 0 ? db : curB, n_pairs, i == 0, rp, dlag,
+                                     i == 0 ? dA0 : nxtA, i == 0 ? dB0 : nxtB, elo, ehi, q.lob, q.a_bits, q.m_bits,
+                                     1 << (q.f0 - 9), dpart, grid, st));
+      } else {
+        grid = (int)std::max<size_t>(std::min<size_t>(n_pairs >> q.lob, 152 * 4), 1);
+        dpart = part_buf(*S, (size_t)grid * 2 * 16);
+        if (i == 0)  // skip fold (multilinear.rs:598-630) fused into round 0
+          FK(flock_launch_zc_round0_skip(da, db, n_pairs, dlag, dA0, dB0, elo, ehi, q.lob, dpart, grid, st));
+        else
+          FK(flock_launch_zc_round(curA, curB, n_pairs, 1, rp, nxtA, nxtB, elo, ehi, q.lob, dpart, grid, st));
+      }
+      if (i + 1 < n_mlv) qn = round_eq(i + 1, true);
+      auto g = reduce_partials(*S, dpart, grid, 2);
+      g[0] = g[0] * q.dinv;
+      g[1] = g[1] * q.dinv;
       if (i > 0) {
         std::swap(curA, nxtA);
         std::swap(curB, nxtB);
@@ -709,7 +754,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
         if (t > 0) u2(lc_rr.back(), rp);
         if (t > 0) len /= 2;
         const int grid = flock_chain_round_grid(len);
-        void* dpart = S->part.get((size_t)grid * 2 * 16);
+        void* dpart = part_buf(*S, (size_t)grid * 2 * 16);
         FK(flock_launch_chain_round(dcomb, dzv, len, t > 0, rp, dpart, grid, st));
         auto msg = reduce_partials(*S, dpart, grid, 2);
         tr.observe(msg[0]);
@@ -721,7 +766,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       u2(lc_rr.back(), rp);
       {  // final bind to the 64 entries of z_partial (its message is not used)
         const int grid = flock_chain_round_grid(len / 2);
-        void* dpart = S->part.get((size_t)grid * 2 * 16);
+        void* dpart = part_buf(*S, (size_t)grid * 2 * 16);
         FK(flock_launch_chain_round(dcomb, dzv, len / 2, 1, rp, dpart, grid, st));
       }
       d2h(*S, z_partial.data(), dzv, 64 * 16);
@@ -763,7 +808,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       for (int k = 0; k <= n_log; k++) {
         const size_t h = (2 * N) >> k;
         int grid = flock_chain_round_grid(h);
-        void* dpart = S->part.get((size_t)grid * 2 * 16);
+        void* dpart = part_buf(*S, (size_t)grid * 2 * 16);
         uint64_t rp[2] = {0, 0};
         if (k > 0) u2(rs.back(), rp);
         FK(flock_launch_chain_round(dW, dg, h, k > 0, rp, dpart, grid, st));
@@ -875,7 +920,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     auto run_msg = [&](int fold, F rr) {
       size_t n_out = fold ? len / 2 : len;
       int grid = flock_lig_grid(n_out / 2);
-      void* dpart = S->part.get((size_t)grid * 3 * 16);
+      void* dpart = part_buf(*S, (size_t)grid * 3 * 16);
       uint64_t rp[2];
       u2(rr, rp);
       if (fold) {
@@ -893,7 +938,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     };
     auto introduce = [&](const void* dbasis) {
       int grid = flock_lig_grid(len / 2);
-      void* dpart = S->part.get((size_t)grid * 3 * 16);
+      void* dpart = part_buf(*S, (size_t)grid * 3 * 16);
       uint64_t rp[2] = {0, 0};
       FK(flock_launch_lig_fold_msg(fcur, dbasis, len, 0, rp, nullptr, nullptr, dpart, grid, st));
       auto s = reduce_partials(*S, dpart, grid, 3);
@@ -912,7 +957,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
         int lob = std::min(nv, 12);
         eq_split_dev(*S, zp, lob, S->eqlo, S->eqhi);
         int grid = flock_lig_grid(len / 2);
-        void* dpart = S->part.get((size_t)grid * 3 * 16);
+        void* dpart = part_buf(*S, (size_t)grid * 3 * 16);
         FK(flock_launch_lig_intro_eq(fcur, len, S->eqlo.p, S->eqhi.p, lob, dpart, grid, st));
         auto s = reduce_partials(*S, dpart, grid, 3);
         tr.observe(s[2]);
