@@ -371,10 +371,13 @@ int launch_tab2(gf128* dst, const gf128* src, size_t mask, const gf128* tw, int 
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 152;
+  // (at least two waves where the block sizes allow: measured faster than one
+  // wave of twice-as-long CTAs)
   size_t cph = 1;
   double best = 1e300;
   for (size_t c : {1, 2, 4, 8, 16, 19, 32, 38, 64, 76, 128, 152, 256, 304, 512}) {
     if (c > 1 && items / c < TAB_THREADS) continue;
+    if (n_hi * c < 2 * (size_t)sms && items / (2 * c) >= TAB_THREADS) continue;
     const double waves = (double)((n_hi * c + sms - 1) / sms);
     const double t = waves * (700.0 + 4.0 * (double)items / (double)c);
     if (t < best) {

@@ -1,0 +1,80 @@
+"""Index arithmetic of the shared-memory table lookups (CPU): every lookup
+visits each byte position once with its own byte, and at every step eight
+consecutive threads read eight distinct bank groups (a 16-byte slot's bank
+group is its index mod 8), which is what makes the random lookups
+conflict-free. The formulas restate those of csrc/gf_tab.cuh (gf_mul_tab),
+csrc/open.cu (combined basis), csrc/zerocheck.cu (round-1 extension tables,
+phi8 replicas, skip tables) and csrc/lincheck.cu (stripe fold)."""
+
+
+def byte_perm(x, y, s):
+    """__byte_perm(x, y, s): result byte i = byte (s >> 4i) & 7 of {y:x}."""
+    b = [(x >> (8 * i)) & 255 for i in range(4)] + [(y >> (8 * i)) & 255 for i in range(4)]
+    return sum(b[(s >> (4 * i)) & 7] << (8 * i) for i in range(4))
+
+
+def gf_tab_offsets(y_bytes, lane):
+    """Byte offsets into the 64 KiB byte tables that gf_mul_tab reads, in step order."""
+    w = [sum(y_bytes[4 * j + i] << (8 * i) for i in range(4)) for j in range(4)]
+    rot = lane & 7
+    sw = bool(rot & 4)
+    yp = [w[1], w[0], w[3], w[2]] if sw else list(w)
+    perm = [0x3210, 0x2301, 0x1032, 0x0123][rot & 3]
+    yp = [byte_perm(v, 0, perm) for v in yp]
+    xk = rot << 4
+    out = []
+    for st in range(16):
+        vb = byte_perm(yp[st >> 2], 0, 0x4404 | ((st & 3) << 4))
+        out.append((vb | (st << 4)) ^ xk)
+    return out
+
+
+def test_gf_tab_visits_each_position_with_its_byte():
+    y = list(range(100, 116))  # byte k of y = 100 + k
+    for lane in range(32):
+        offs = gf_tab_offsets(y, lane)
+        slots = [o >> 4 for o in offs]
+        pos = sorted(s & 15 for s in slots)
+        assert pos == list(range(16)), lane
+        for s in slots:
+            assert s >> 4 == y[s & 15], (lane, s)  # table row = byte of that position
+
+
+def test_gf_tab_bank_groups_distinct():
+    y = [7] * 16  # worst case for value-dependent layouts: all bytes equal
+    for st in range(16):
+        for l0 in range(0, 32, 8):
+            groups = {(gf_tab_offsets(y, l)[st] >> 4) % 8 for l in range(l0, l0 + 8)}
+            assert len(groups) == 8, (st, l0)
+
+
+def test_combined_basis_rotation():
+    # lane rotation rot = thread & 15 visits q = (rot + t) & 15; slot (v << 4) + q
+    for t in range(16):
+        for l0 in range(0, 32, 8):
+            groups = {(((9 << 4) + ((l & 15) + t & 15)) % 8) for l in range(l0, l0 + 8)}
+            assert len(groups) == 8
+    for rot in range(16):
+        assert sorted((rot + t) & 15 for t in range(16)) == list(range(16))
+
+
+def test_zc_round1_extension_and_phi_layouts():
+    # extension table: entry (q, v, c) at slot ((q * 256 + v) << 3) + c, lane l reads c = (l + k) & 7
+    for k in range(8):
+        for l0 in range(0, 32, 8):
+            groups = {(((3 * 256 + 200) << 3) + ((l + k) & 7)) % 8 for l in range(l0, l0 + 8)}
+            assert len(groups) == 8
+    # phi8 replicas: value v of replica r at slot 8 v + r, lane l reads replica l & 7
+    for l0 in range(0, 32, 8):
+        assert len({(8 * 77 + (l & 7)) % 8 for l in range(l0, l0 + 8)}) == 8
+    # skip-fold tables of the grouped round 0: entry (v, c) at slot (v << 3) + c
+    for k in range(8):
+        assert len({((33 << 3) + ((l & 7) + k & 7)) % 8 for l in range(8)}) == 8
+
+
+def test_lincheck_stripe_rotation():
+    # t8[v][q] at slot v * 8 + q, lane reads stripe q = (lane8 + st) & 7
+    for st in range(8):
+        assert len({(5 * 8 + ((l + st) & 7)) % 8 for l in range(8)}) == 8
+    for l in range(8):
+        assert sorted((l + st) & 7 for st in range(8)) == list(range(8))
