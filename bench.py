@@ -54,6 +54,11 @@ PUBLISHED = 483866.0  # README.md:110-116, unmodified reference, Apple M4 Pro ru
 # five L0 passes in profiles/ntt_pass_l0_2e16.md), times 4 for 4x the positions.
 NTT_TRAFFIC_PER_PASS = {20: 4 * 486.5e6}
 NTT_MAX_LAYERS = {0: 4, 1: 6, 2: 8}  # layers per pass of the autotuner's pass shapes
+# Thread instructions per GF(2^128) product in the table passes and per
+# butterfly in the multiply passes, measured by ncu on the 2^18-position L0
+# transform (profiles/ntt_instructions_2e18pos.md).
+NTT_INSTR_PER_TABLE_PRODUCT = 152
+NTT_INSTR_PER_MULTIPLY_BUTTERFLY = 437
 
 
 def load_peaks():
@@ -183,7 +188,7 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def kernel_roofline(F, ctx_handle, stream_ptr, log2, peaks, torch, dev):
+def kernel_roofline(F, ctx_handle, stream_ptr, log2, peaks, torch, dev, clock_mhz=None):
     """Times the dominant kernel family (the L0 commit NTT) alone with CUDA events."""
     m = 14 + log2
     log_d = m - 7 - 6 + 1
@@ -221,6 +226,14 @@ def kernel_roofline(F, ctx_handle, stream_ptr, log2, peaks, torch, dev):
     alg = cw // 2 + cw + (passes - 1) * 2 * cw
     achieved = alg / (ms * 1e-3) / 1e9
     muls = (log_d - 1) * (1 << (log_d - 1)) * 64
+    # integer roofline: instruction counts (per product, from ncu) over the
+    # live time, against the SM issue peak (SMs x 4 sub-partitions x 32 lanes)
+    def products(l):  # butterflies of layer l with a product (block 0 skips it)
+        return ((1 << (log_d - 1)) - (1 << (log_d - l - 1))) * 64
+    ins = (sum(products(l) for l in range(1, tab_end)) * NTT_INSTR_PER_TABLE_PRODUCT
+           + sum(products(l) for l in range(tab_end, log_d)) * NTT_INSTR_PER_MULTIPLY_BUTTERFLY)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    issue_peak = sms * 4 * 32 * (clock_mhz or 2070.0) * 1e6
     return {"kernel": f"L0 commit NTT (layers 1..{log_d - 1}: {tab_passes} two-layer table passes, then "
                       f"{passes - tab_passes} multiply pass(es) of <= {max_f} layers)",
             "bound": "hbm",
@@ -228,6 +241,10 @@ def kernel_roofline(F, ctx_handle, stream_ptr, log2, peaks, torch, dev):
             "traffic": (passes * NTT_TRAFFIC_PER_PASS[log_d]) if log_d in NTT_TRAFFIC_PER_PASS else None,
             "algorithmic_bytes_per_set": alg, "pass_shape": variant,
             "ms_per_launch_set": ms, "gf128_muls_per_s": muls / (ms * 1e-3),
+            "integer": {"achieved": ins / (ms * 1e-3) / 1e12, "peak": issue_peak / 1e12, "unit": "T thread-instr/s",
+                        "frac": ins / (ms * 1e-3) / issue_peak, "instructions_per_set": ins,
+                        "note": "instructions per product from ncu (profiles/ntt_instructions_2e18pos.md) times "
+                                "the set's products, over the live time; peak = SMs x 4 x 32 lanes x SM clock"},
             "note": "the passes are bound by the integer pipes (byte-table lookups in the upper layers, "
                     "carry-less multiplies below), not HBM: see profiles/ntt_pass_l0_2e16.md and "
                     "profiles/ntt_tab_pass_l0_2e16.md"}
@@ -336,7 +353,7 @@ def run_gpu(args):
     if not verified:
         raise SystemExit("a timed proof was rejected by flock_verify")
     peaks, src = load_peaks()
-    roof = kernel_roofline(F, setup.ctx.handle, None, log2, peaks, torch, dev)
+    roof = kernel_roofline(F, setup.ctx.handle, None, log2, peaks, torch, dev, clk.summary().get("sm_mhz"))
     roof["peak_source"] = src
     dev_ms, e2e_ms, seed_ms = max_over_ranks([dev_ms, e2e_ms, seed_ms], ws, device=dev)
     if rank == 0:
