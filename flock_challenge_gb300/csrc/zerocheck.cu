@@ -119,18 +119,26 @@ __device__ __forceinline__ void acc_shift_xor_v(Acc5& a, const uint4 v, uint32_t
 //        step k lane l looks up byte position (l + k) mod 8, so any eight
 //        consecutive lanes hit eight distinct bank groups and the random
 //        lookups are conflict-free;
-//   phi  [256 v][8 replicas] of 16 B: lane l reads replica l mod 8, which
-//        lies in bank group l mod 8, so the lookups are conflict-free;
+//   LH   per warp, per half (one outer block xo): the eq-weighted phi8 nibble
+//        tables L[j] = phi8(j) e and H[g] = phi8(16 g) e, e = eq_out(xo), four
+//        replicas each (entry j of replica r at slot 4 j + r, lane l reads
+//        replica l mod 4, so at most two lanes of a quarter warp share a
+//        bank group): phi8(v) e = L[v & 15] + H[v >> 4], because phi8 is
+//        additive, so the block's values come out already weighted and need
+//        no GF(2^128) product (eight per block build the tables instead of
+//        twelve per lane);
+//   P    per warp, per half: phi8(2^k) e for k < 8, the tables' basis;
 //   xch  per warp, per half: [16 xm] rows of 20 words (64 bytes used; the
 //        odd 80-byte row pitch makes the 16-byte stores conflict-free), one
 //        plane set at a time, halves 336 words apart (16 mod 32 banks) so both
 //        halves' reads of one row index hit disjoint banks.
-// Measured against three-set exchange areas (which leave no room for the
-// phi replicas at 12 warps) and a two-stage exchange, the one-set exchange
-// with 12 warps is fastest despite its register spills.
+// Measured against three-set exchange areas and a two-stage exchange, the
+// one-set exchange with 12 warps is fastest despite its register spills.
 constexpr int R1_ROW = 20;
 constexpr int R1_HALF = 16 * R1_ROW + 16;
-constexpr size_t R1_SMEM = (size_t)8 * 4 * 256 * 16 + 8 * 256 * 16 + (size_t)(R1_THREADS / 32) * 2 * R1_HALF * 4;
+constexpr int R1_WARPS = R1_THREADS / 32;
+constexpr size_t R1_SMEM = (size_t)8 * 4 * 256 * 16 + (size_t)R1_WARPS * 2 * 128 * 16 + (size_t)R1_WARPS * 2 * 8 * 16 +
+                           128 + (size_t)R1_WARPS * 2 * R1_HALF * 4;
 static_assert(R1_SMEM <= 232448, "round-1 shared memory above the 227 KB per-block limit");
 
 // grid: each warp walks pairs of outer blocks; lane: xm = lane & 15, xo half = lane >> 4.
@@ -139,16 +147,18 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
                  size_t n_outer, const gf128* __restrict__ eq_out, const ZcRound1Tables* __restrict__ T,
                  gf128* __restrict__ partials) {
   extern __shared__ uint4 sm[];
-  uint4* ext = sm;                                                   // [8][4][256]
-  uint4* phi = sm + 8 * 4 * 256;                                     // [256][8]
-  uint32_t* xch = reinterpret_cast<uint32_t*>(phi + 8 * 256);        // per warp [2][R1_HALF]
+  uint4* ext = sm;                                                   // [4][256][8]
+  uint4* lh = ext + 8 * 4 * 256;                                     // per warp, half [L, H][16][4]
+  uint4* pb = lh + R1_WARPS * 2 * 128;                               // per warp, half [8]
+  uint4* phik = pb + R1_WARPS * 2 * 8;                               // phi8(2^k), k < 8
+  uint32_t* xch = reinterpret_cast<uint32_t*>(phik + 8);             // per warp [2][R1_HALF]
   const uint64_t* ext_src = &T->ext[0][0][0];
   for (int i = threadIdx.x; i < 8 * 4 * 256; i += R1_THREADS) {
     const int q = i >> 11, v = (i >> 3) & 255, c = i & 7;
     const uint64_t* e = ext_src + ((size_t)(c * 256 + v) << 3) + 2 * q;
     ext[i] = make_uint4((uint32_t)e[0], (uint32_t)(e[0] >> 32), (uint32_t)e[1], (uint32_t)(e[1] >> 32));
   }
-  for (int i = threadIdx.x; i < 8 * 256; i += R1_THREADS) phi[i] = reinterpret_cast<const uint4*>(T->phi8)[i >> 3];
+  if (threadIdx.x < 8) phik[threadIdx.x] = reinterpret_cast<const uint4*>(T->phi8)[1 << threadIdx.x];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int xm = lane & 15, half = lane >> 4;
@@ -223,10 +233,35 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
     // bytes: the lane of point quad xm reads word xm of every producer row,
     // and handles points / skip positions 4*xm .. 4*xm+3 of its half (and
     // both parities t of the c statistic).
-    const gf128 e = live ? gf_load(&eq_out[xo]) : gf_zero();
-    const uint4* my_phi = phi + (lane & 7);
-    // one plane set per iteration (not unrolled: the body holds four GF
-    // products, which keeps the loop inside the instruction cache)
+    // eq-weighted phi8 nibble tables of this block (see the layout above)
+    uint4* my_lh = lh + (warp * 2 + half) * 128;
+    uint4* my_p = pb + (warp * 2 + half) * 8;
+    if (xm < 8) {
+      const gf128 e = live ? gf_load(&eq_out[xo]) : gf_zero();
+      const uint4 f = phik[xm];
+      const gf128 pk = gf_mul(gf128{{f.x, f.y, f.z, f.w}}, e);
+      my_p[xm] = make_uint4(pk.w[0], pk.w[1], pk.w[2], pk.w[3]);
+    }
+    __syncwarp();
+    {
+      uint4 lo = make_uint4(0, 0, 0, 0), hi = lo;
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        if ((xm >> k) & 1) {
+          const uint4 a = my_p[k], b = my_p[4 + k];
+          lo.x ^= a.x; lo.y ^= a.y; lo.z ^= a.z; lo.w ^= a.w;
+          hi.x ^= b.x; hi.y ^= b.y; hi.z ^= b.z; hi.w ^= b.w;
+        }
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        my_lh[4 * xm + r] = lo;
+        my_lh[64 + 4 * xm + r] = hi;
+      }
+    }
+    const uint4* my_l = my_lh + (lane & 3);
+    const uint4* my_h = my_lh + 64 + (lane & 3);
+    // one plane set per iteration (not unrolled, which keeps the loop inside
+    // the instruction cache)
 #pragma unroll 1
     for (int set = 0; set < 3; set++) {
       uint64_t pl[8];
@@ -245,11 +280,15 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
         for (int mm2 = 0; mm2 < 16; mm2++) {
           const uint32_t bw = my_x[mm2 * R1_ROW + xm];
 #pragma unroll
-          for (int q = 0; q < 4; q++) acc_shift_xor_v(v[q], my_phi[((bw >> (8 * q)) & 255) << 3], (uint32_t)mm2);
+          for (int q = 0; q < 4; q++) {
+            const uint32_t v8 = (bw >> (8 * q)) & 255;
+            const uint4 a = my_l[(v8 & 15) << 2], b = my_h[(v8 >> 4) << 2];
+            acc_shift_xor_v(v[q], make_uint4(a.x ^ b.x, a.y ^ b.y, a.z ^ b.z, a.w ^ b.w), (uint32_t)mm2);
+          }
         }
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-          const gf128 p = gf_mul(acc_reduce(v[q]), e);
+          const gf128 p = acc_reduce(v[q]);
           if (set == 0) sum_ab[q] = gf_add(sum_ab[q], p);
           else if (set == 1) sum_c[q] = gf_add(sum_c[q], p);
           else sum_c[4 + q] = gf_add(sum_c[4 + q], p);

@@ -4,7 +4,7 @@ consecutive threads read eight distinct bank groups (a 16-byte slot's bank
 group is its index mod 8), which is what makes the random lookups
 conflict-free. The formulas restate those of csrc/gf_tab.cuh (gf_mul_tab),
 csrc/open.cu (combined basis), csrc/zerocheck.cu (round-1 extension tables,
-phi8 replicas, skip tables) and csrc/lincheck.cu (stripe fold)."""
+phi8 nibble tables, skip tables) and csrc/lincheck.cu (stripe fold)."""
 
 
 def byte_perm(x, y, s):
@@ -64,9 +64,18 @@ def test_zc_round1_extension_and_phi_layouts():
         for l0 in range(0, 32, 8):
             groups = {(((3 * 256 + 200) << 3) + ((l + k) & 7)) % 8 for l in range(l0, l0 + 8)}
             assert len(groups) == 8
-    # phi8 replicas: value v of replica r at slot 8 v + r, lane l reads replica l & 7
-    for l0 in range(0, 32, 8):
-        assert len({(8 * 77 + (l & 7)) % 8 for l in range(l0, l0 + 8)}) == 8
+    # eq-weighted phi8 nibble tables: L[j] of replica r at slot 4 j + r, H[g]
+    # at 64 + 4 g + r, lane l reads replica l & 3; every (table, entry,
+    # replica) has its own slot and a quarter warp puts at most two lanes in
+    # one bank group for any nibbles it reads
+    slots = {4 * j + r for j in range(16) for r in range(4)} | {64 + 4 * j + r for j in range(16) for r in range(4)}
+    assert slots == set(range(128))
+    import random
+    rng = random.Random(3)
+    for _ in range(200):
+        nib = [rng.randrange(16) for _ in range(8)]
+        groups = [(64 + 4 * nib[l] + (l & 3)) % 8 for l in range(8)]
+        assert max(groups.count(g) for g in groups) <= 2
     # skip-fold tables of the grouped round 0: entry (v, c) at slot (v << 3) + c
     for k in range(8):
         assert len({((33 << 3) + ((l & 7) + k & 7)) % 8 for l in range(8)}) == 8
@@ -78,3 +87,23 @@ def test_lincheck_stripe_rotation():
         assert len({(5 * 8 + ((l + st) & 7)) % 8 for l in range(8)}) == 8
     for l in range(8):
         assert sorted((l + st) & 7 for st in range(8)) == list(range(8))
+
+
+def test_phi8_nibble_tables_weight_by_eq():
+    # phi8(v) e = L[v & 15] + H[v >> 4] with L[j] = sum_{k<4, bit k of j} phi8(2^k) e
+    # and H[g] = sum_{k<4, bit k of g} phi8(2^(k+4)) e (phi8 is additive)
+    import oracle_lib as O
+    e = (0x0123456789ABCDEF, 0xF0E1D2C3B4A59687)
+    P = [O.gf_mul(O.phi8(1 << k), e) for k in range(8)]
+
+    def combo(j, base):
+        acc = (0, 0)
+        for k in range(4):
+            if (j >> k) & 1:
+                acc = (acc[0] ^ P[base + k][0], acc[1] ^ P[base + k][1])
+        return acc
+    L = [combo(j, 0) for j in range(16)]
+    H = [combo(g, 4) for g in range(16)]
+    for v in range(256):
+        lo, hi = L[v & 15], H[v >> 4]
+        assert (lo[0] ^ hi[0], lo[1] ^ hi[1]) == O.gf_mul(O.phi8(v), e), v
