@@ -53,6 +53,8 @@ int flock_launch_lig_intro_eq(const void* f, size_t n, const void* lo, const voi
 int flock_launch_glue_eq(void* b, size_t n, const void* lo, const void* hi, int lo_bits, const uint64_t beta[2],
                          cudaStream_t st);
 int flock_launch_glue(void* b, const void* add, size_t n, const uint64_t beta[2], cudaStream_t st);
+// LO holds nq << flock_induce_basis_lo_bits(n) entries, HI nq << (n - that).
+int flock_induce_basis_lo_bits(int n);
 int flock_launch_induce_basis(const uint32_t* d_queries, int nq, int n, const void* sks, const void* inv_sks,
                               const void* alpha_w, void* W, void* LO, void* HI, void* basis, cudaStream_t st);
 int flock_launch_gather_rows(const void* mat, const uint32_t* rows, int n_rows, int width, void* out,

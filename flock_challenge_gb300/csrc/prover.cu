@@ -984,7 +984,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       h2d(*S, dq, q.data(), q.size() * 4);
       void* dal = S->abuf.get(q.size() * 16);
       h2d(*S, dal, aw.data(), q.size() * 16);
-      int lo_bits = (nvars + 1) / 2, hi_bits = nvars - lo_bits;
+      int lo_bits = flock_induce_basis_lo_bits(nvars), hi_bits = nvars - lo_bits;
       void* dW = S->W.get(q.size() * nvars * 16);
       void* dLO = S->LO.get((q.size() << lo_bits) * 16);
       void* dHI = S->HI.get((q.size() << hi_bits) * 16);
