@@ -301,8 +301,8 @@ constexpr size_t TAB_SMEM = (size_t)3 * TAB_ENTRIES * 16 + (size_t)3 * GF_TAB_NI
 __device__ void build_tabs3(const gf128 t[3], uint4* __restrict__ T, uint4* __restrict__ LH) {
   if (threadIdx.x < 96) gf_tab_nibbles(t[threadIdx.x >> 5], LH + (threadIdx.x >> 5) * 512, threadIdx.x & 31);
   __syncthreads();
-  for (int e = threadIdx.x; e < 3 * TAB_ENTRIES; e += blockDim.x)
-    T[e] = gf_tab_entry(LH + (e / TAB_ENTRIES) * 512, e % TAB_ENTRIES);
+  for (int it = threadIdx.x; it < 3 * 512; it += blockDim.x)
+    gf_tab_rows<2>(LH + (it >> 9) * 512, T + (it >> 9) * TAB_ENTRIES, it & 511);
 }
 
 // Layers l, l + 1 of the transform for block hi of layer l (blockIdx.x / cph)

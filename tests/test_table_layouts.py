@@ -107,3 +107,29 @@ def test_phi8_nibble_tables_weight_by_eq():
     for v in range(256):
         lo, hi = L[v & 15], H[v >> 4]
         assert (lo[0] ^ hi[0], lo[1] ^ hi[1]) == O.gf_mul(O.phi8(v), e), v
+
+
+def gf_tab_rows_slots(item, split):
+    """(read L slot, read H slot, written T slot) triples of gf_tab_rows<split>(item)."""
+    J = 16 // split
+    s, g, k = item >> 8, (item >> 4) & 15, item & 15
+    return [(j * 16 + k, 256 + g * 16 + k, ((16 * g + j) << 4) + k) for j in range(s * J, (s + 1) * J)]
+
+
+def test_gf_tab_rows_cover_every_slot_once():
+    for split in (1, 2):
+        written = [t for it in range(256 * split) for (_, _, t) in gf_tab_rows_slots(it, split)]
+        assert sorted(written) == list(range(4096)), split
+        for it in range(256 * split):
+            for l, h, t in gf_tab_rows_slots(it, split):
+                v, k = t >> 4, t & 15
+                assert l == (v & 15) * 16 + k and h == 256 + (v >> 4) * 16 + k  # L[v & 15][k] + H[v >> 4][k]
+
+
+def test_gf_tab_rows_bank_groups_distinct():
+    for split in (1, 2):
+        for base in range(0, 256 * split, 8):
+            steps = [gf_tab_rows_slots(it, split) for it in range(base, base + 8)]
+            for st in range(16 // split):
+                for which in range(3):
+                    assert len({steps[q][st][which] % 8 for q in range(8)}) == 8
