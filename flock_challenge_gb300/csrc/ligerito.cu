@@ -153,37 +153,37 @@ basis_kernel(const gf128* __restrict__ LO, const gf128* __restrict__ HI, int nq,
   }
 }
 
-// The same basis through byte tables, for large bases (lo_bits = 10): CTA h
-// owns the 2^10 entries of high index h and walks the queries; per query it
-// builds the byte tables of HI[i][h] and adds HI[i][h] LO[i][jl] for its
-// entries (four per thread) as 16 table lookups each instead of a carry-less
-// multiply. The two barriers inside each table build order a query's lookups
-// before the next query's writes, so one table set suffices; three CTAs per
-// SM overlap one CTA's build with the others' lookups.
+// The same basis through byte tables, for large bases (LO_BITS = 10 or 11):
+// CTA h owns the 2^LO_BITS entries of high index h and walks the queries; per
+// query it builds the byte tables of HI[i][h] and adds HI[i][h] LO[i][jl] for
+// its entries (four or eight per thread) as 16 table lookups each instead of
+// a carry-less multiply. The two barriers inside each table build order a
+// query's lookups before the next query's writes, so one table set suffices;
+// three CTAs per SM overlap one CTA's build with the others' lookups.
 constexpr int BT_THREADS = 256;
-constexpr int BT_LO_BITS = 10;
-constexpr int BT_PER_THREAD = (1 << BT_LO_BITS) / BT_THREADS;
 constexpr size_t BT_SMEM = (size_t)(GF_TAB_ENTRIES + GF_TAB_NIBBLE_SLOTS) * 16;
 
+template <int LO_BITS>
 __global__ void __launch_bounds__(BT_THREADS, 3)
 basis_tab_kernel(const gf128* __restrict__ LO, const gf128* __restrict__ HI, int nq, int hi_bits,
                  gf128* __restrict__ basis) {
+  constexpr int PER_THREAD = (1 << LO_BITS) / BT_THREADS;
   extern __shared__ uint4 btab[];
-  const size_t lo_n = (size_t)1 << BT_LO_BITS, hi_n = (size_t)1 << hi_bits;
+  const size_t lo_n = (size_t)1 << LO_BITS, hi_n = (size_t)1 << hi_bits;
   const uint32_t rot = threadIdx.x & 7;
   for (size_t h = blockIdx.x; h < hi_n; h += gridDim.x) {
-    gf128 acc[BT_PER_THREAD];
+    gf128 acc[PER_THREAD];
 #pragma unroll
-    for (int k = 0; k < BT_PER_THREAD; k++) acc[k] = gf_zero();
+    for (int k = 0; k < PER_THREAD; k++) acc[k] = gf_zero();
     for (int i = 0; i < nq; i++) {
       gf_tab_build(HI[(size_t)i * hi_n + h], btab, btab + GF_TAB_ENTRIES);
       const gf128* lo = LO + (size_t)i * lo_n + threadIdx.x;
 #pragma unroll
-      for (int k = 0; k < BT_PER_THREAD; k++) acc[k] = gf_add(acc[k], gf_mul_tab(btab, lo[k * BT_THREADS], rot));
+      for (int k = 0; k < PER_THREAD; k++) acc[k] = gf_add(acc[k], gf_mul_tab(btab, lo[k * BT_THREADS], rot));
     }
-    gf128* out = basis + (h << BT_LO_BITS) + threadIdx.x;
+    gf128* out = basis + (h << LO_BITS) + threadIdx.x;
 #pragma unroll
-    for (int k = 0; k < BT_PER_THREAD; k++) out[k * BT_THREADS] = acc[k];
+    for (int k = 0; k < PER_THREAD; k++) out[k * BT_THREADS] = acc[k];
   }
 }
 
@@ -259,28 +259,35 @@ int flock_launch_glue(void* b, const void* add, size_t n, const uint64_t beta[2]
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
-// byte-table path from 2^18 entries (at least 256 CTAs of 2^10 entries)
+// byte-table path from 2^18 entries: CTAs of 2^10 entries at 2^18, of 2^11
+// above (at least 256 CTAs; 2^11 measured faster than 2^10 and 2^9 at 2^19)
 constexpr int kBasisTabMinBits = 18;
 
-int flock_induce_basis_lo_bits(int n) { return n >= kBasisTabMinBits ? BT_LO_BITS : (n + 1) / 2; }
+int flock_induce_basis_lo_bits(int n) { return n >= kBasisTabMinBits ? (n == kBasisTabMinBits ? 10 : 11) : (n + 1) / 2; }
 
 int flock_launch_induce_basis(const uint32_t* d_queries, int nq, int n, const void* sks, const void* inv_sks,
                               const void* alpha_w, void* W, void* LO, void* HI, void* basis, cudaStream_t st) {
   what_kernel<<<(nq + 127) / 128, 128, 0, st>>>(d_queries, nq, n, (const gf128*)sks, (const gf128*)inv_sks,
                                                 (gf128*)W); flock_count_launch();
   const int lo_bits = flock_induce_basis_lo_bits(n), hi_bits = n - lo_bits;
-  const bool tab = lo_bits == BT_LO_BITS && n >= kBasisTabMinBits;
+  const bool tab = n >= kBasisTabMinBits;
   size_t nlo = (size_t)nq << lo_bits, nhi = (size_t)nq << hi_bits;
   tensor_kernel<<<grid_for(nlo, 256, 1u << 30), 256, 0, st>>>((const gf128*)W, nq, n, 0, lo_bits,
                                                                (const gf128*)alpha_w, (gf128*)LO); flock_count_launch();
   tensor_kernel<<<grid_for(nhi, 256, 1u << 30), 256, 0, st>>>((const gf128*)W, nq, n, lo_bits, hi_bits, nullptr,
                                                                (gf128*)HI); flock_count_launch();
   if (tab) {
-    flock_once_per_device((const void*)basis_tab_kernel, [] {
-      cudaFuncSetAttribute(basis_tab_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BT_SMEM);
+    flock_once_per_device((const void*)basis_tab_kernel<10>, [] {
+      cudaFuncSetAttribute(basis_tab_kernel<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BT_SMEM);
+      cudaFuncSetAttribute(basis_tab_kernel<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BT_SMEM);
     });
-    basis_tab_kernel<<<(unsigned)((size_t)1 << hi_bits), BT_THREADS, BT_SMEM, st>>>(
-        (const gf128*)LO, (const gf128*)HI, nq, hi_bits, (gf128*)basis);
+    const unsigned grid = (unsigned)((size_t)1 << hi_bits);
+    if (lo_bits == 10)
+      basis_tab_kernel<10><<<grid, BT_THREADS, BT_SMEM, st>>>((const gf128*)LO, (const gf128*)HI, nq, hi_bits,
+                                                              (gf128*)basis);
+    else
+      basis_tab_kernel<11><<<grid, BT_THREADS, BT_SMEM, st>>>((const gf128*)LO, (const gf128*)HI, nq, hi_bits,
+                                                              (gf128*)basis);
   } else {
     basis_kernel<<<grid_for((size_t)1 << n, 256, 152 * 8), 256, 0, st>>>((const gf128*)LO, (const gf128*)HI, nq,
                                                                          lo_bits, hi_bits, (gf128*)basis);

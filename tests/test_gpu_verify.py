@@ -71,6 +71,9 @@ def test_every_supported_size_proves_and_verifies(cuda_device):
         p = F.Blake3Setup(1 << log2).prove_seed(1000 + log2)
         assert F.verify(p), log2
         assert len(p) < 500_000
+        if log2 in (17, 19):  # both byte-table splits of the Ligerito basis, checked by the oracle verifier
+            ok, why = O.verify(p, 14 + log2)
+            assert ok, (log2, why)
 
 
 def test_ragged_large_input_verifies(cuda_device):
