@@ -314,6 +314,9 @@ def run_gpu(args):
         prove_dev(d_ins[i % 2])
     first = prove_dev(d_ins[0])
     second = prove_dev(d_ins[1])
+    # the host-buffer and seed paths warm up too (their staging buffers)
+    prove_host(host[0])
+    setup.prove_seed(999_999)
     torch.cuda.synchronize()
     if ws > 1:
         torch.distributed.barrier()

@@ -95,6 +95,37 @@ __device__ __forceinline__ void gf_tab_rows(const uint4* __restrict__ LH, uint4*
   }
 }
 
+// One row of the byte table computed directly, without nibble tables or a
+// barrier: item = g << 4 | k (g, k < 16) writes the 16 slots (v << 4) + k of
+// v = 16 g + j, j < 16, i.e. t v x^(8k) = L_k(j) + H_k(g) with L_k(j) the sum
+// of t x^(8k+b) over the bits b of j and H_k(g) that of t x^(8k+4+b) over the
+// bits of g. The eight images t x^(8k+b) come from one shift and seven
+// doublings; j walks the Gray code, one XOR per slot. Suits tables rebuilt
+// often (one multiplier after another): every thread works, nothing waits on
+// a serial nibble phase. Eight consecutive items have eight consecutive k,
+// so their writes hit distinct bank groups.
+__device__ __forceinline__ void gf_tab_row_direct(gf128 t, uint4* __restrict__ T, int item) {
+  const int g = (item >> 4) & 15, k = item & 15;
+  gf128 B[8];
+  B[0] = gf_mul_xpow_small(t, 8 * k);
+#pragma unroll
+  for (int b = 1; b < 8; b++) B[b] = gf_mul_x(B[b - 1]);
+  gf128 v = gf_zero();
+#pragma unroll
+  for (int b = 0; b < 4; b++) {
+    const uint32_t m = 0u - (uint32_t)((g >> b) & 1);
+#pragma unroll
+    for (int w = 0; w < 4; w++) v.w[w] ^= B[4 + b].w[w] & m;
+  }
+  uint4* row = T + (g << 8) + k;
+#pragma unroll
+  for (int jj = 0; jj < 16; jj++) {
+    if (jj) v = gf_add(v, B[gf_tab_ctz4(jj)]);
+    const int j = jj ^ (jj >> 1);
+    row[j << 4] = make_uint4(v.w[0], v.w[1], v.w[2], v.w[3]);
+  }
+}
+
 // Byte tables of one multiplier t into T (GF_TAB_ENTRIES slots), using LH
 // (GF_TAB_NIBBLE_SLOTS slots) as scratch. All threads of the CTA call it; it
 // ends with a barrier, after which T is ready.

@@ -155,13 +155,15 @@ basis_kernel(const gf128* __restrict__ LO, const gf128* __restrict__ HI, int nq,
 
 // The same basis through byte tables, for large bases (LO_BITS = 10 or 11):
 // CTA h owns the 2^LO_BITS entries of high index h and walks the queries; per
-// query it builds the byte tables of HI[i][h] and adds HI[i][h] LO[i][jl] for
-// its entries (four or eight per thread) as 16 table lookups each instead of
-// a carry-less multiply. The two barriers inside each table build order a
-// query's lookups before the next query's writes, so one table set suffices;
-// three CTAs per SM overlap one CTA's build with the others' lookups.
+// query it builds the byte tables of HI[i][h] (one row per thread, computed
+// directly) and adds HI[i][h] LO[i][jl] for its entries (four or eight per
+// thread) as 16 table lookups each instead of a carry-less multiply. A barrier
+// before each build orders the previous query's lookups before the new
+// writes, so one table suffices; three CTAs per SM overlap one CTA's build
+// with the others' lookups.
 constexpr int BT_THREADS = 256;
-constexpr size_t BT_SMEM = (size_t)(GF_TAB_ENTRIES + GF_TAB_NIBBLE_SLOTS) * 16;
+constexpr size_t BT_SMEM = (size_t)GF_TAB_ENTRIES * 16;
+static_assert(BT_THREADS == 256, "one byte-table row per thread");
 
 template <int LO_BITS>
 __global__ void __launch_bounds__(BT_THREADS, 3)
@@ -176,7 +178,9 @@ basis_tab_kernel(const gf128* __restrict__ LO, const gf128* __restrict__ HI, int
 #pragma unroll
     for (int k = 0; k < PER_THREAD; k++) acc[k] = gf_zero();
     for (int i = 0; i < nq; i++) {
-      gf_tab_build(HI[(size_t)i * hi_n + h], btab, btab + GF_TAB_ENTRIES);
+      __syncthreads();
+      gf_tab_row_direct(HI[(size_t)i * hi_n + h], btab, threadIdx.x);
+      __syncthreads();
       const gf128* lo = LO + (size_t)i * lo_n + threadIdx.x;
 #pragma unroll
       for (int k = 0; k < PER_THREAD; k++) acc[k] = gf_add(acc[k], gf_mul_tab(btab, lo[k * BT_THREADS], rot));

@@ -133,3 +133,49 @@ def test_gf_tab_rows_bank_groups_distinct():
             for st in range(16 // split):
                 for which in range(3):
                     assert len({steps[q][st][which] % 8 for q in range(8)}) == 8
+
+
+def test_gf_tab_row_direct_gray_walk():
+    # gf_tab_row_direct: slot of step jj is (g << 8) + (j << 4) + k with j = jj ^ (jj >> 1),
+    # reached from the previous step by one XOR of image ctz(jj); all 4096 slots once
+    def ctz4(j):
+        return 0 if j & 1 else 1 if j & 2 else 2 if j & 4 else 3
+    written = []
+    for item in range(256):
+        g, k = item >> 4, item & 15
+        prev = 0
+        for jj in range(16):
+            j = jj ^ (jj >> 1)
+            if jj:
+                assert prev ^ j == 1 << ctz4(jj)  # the Gray step flips bit ctz(jj) of j
+            prev = j
+            slot = (g << 8) + (j << 4) + k
+            assert slot == ((16 * g + j) << 4) + k
+            written.append(slot)
+    assert sorted(written) == list(range(4096))
+    for base in range(0, 256, 8):  # eight consecutive items: distinct bank groups at every step
+        for jj in range(16):
+            j = jj ^ (jj >> 1)
+            assert len({(((base + q) >> 4 << 8) + (j << 4) + ((base + q) & 15)) % 8 for q in range(8)}) == 8
+
+
+def test_gf_tab_row_direct_values():
+    # the row formula: t v x^(8k) = sum_{bits b of j} t x^(8k+b) + sum_{bits b of g} t x^(8k+4+b), v = 16 g + j
+    import oracle_lib as O
+    t = (0x243F6A8885A308D3, 0x13198A2E03707344)
+
+    def xpow(i):
+        return (1 << i, 0) if i < 64 else (0, 1 << (i - 64))
+
+    for k in (0, 5, 15):
+        B = [O.gf_mul(t, xpow(8 * k + b)) for b in range(8)]
+        for v in (0, 1, 0x5A, 0xFF, 0x80):
+            g, j = v >> 4, v & 15
+            acc = (0, 0)
+            for b in range(4):
+                if (j >> b) & 1:
+                    acc = (acc[0] ^ B[b][0], acc[1] ^ B[b][1])
+                if (g >> b) & 1:
+                    acc = (acc[0] ^ B[4 + b][0], acc[1] ^ B[4 + b][1])
+            want = O.gf_mul(t, O.gf_mul((v, 0), xpow(8 * k)))
+            assert acc == want, (k, v)
