@@ -11,7 +11,6 @@
 #include "gf128.cuh"
 
 constexpr int GF_TAB_ENTRIES = 16 * 256;      // slots of one byte-table set
-constexpr int GF_TAB_NIBBLE_SLOTS = 2 * 256;  // slots of its nibble tables
 
 // t * x^i for 0 <= i < 128: shift into 256 bits, then reduce.
 __device__ __forceinline__ gf128 gf_mul_xpow_small(gf128 h, int i) {
@@ -59,51 +58,16 @@ __device__ __forceinline__ gf128 gf_mul_tab(const uint4* __restrict__ T, const g
 
 __host__ __device__ constexpr int gf_tab_ctz4(int j) { return (j & 1) ? 0 : (j & 2) ? 1 : (j & 4) ? 2 : 3; }
 
-// Nibble tables of t into LH (GF_TAB_NIBBLE_SLOTS slots): L[j][k] = t j x^(8k)
-// at j * 16 + k and H[g][k] = t g x^(8k + 4) at 256 + g * 16 + k, for nibbles
-// j, g < 16. Called by 32 threads, part = 0..31 (k = part & 15, L or H by
-// part >> 4), each with a Gray-code walk over four images t x^i.
-__device__ __forceinline__ void gf_tab_nibbles(gf128 t, uint4* __restrict__ LH, int part) {
-  const int half = part >> 4, k = part & 15;
-  gf128 B[4];
-#pragma unroll
-  for (int b = 0; b < 4; b++) B[b] = gf_mul_xpow_small(t, 8 * k + 4 * half + b);
-  gf128 v[16];
-  v[0] = gf_zero();
-#pragma unroll
-  for (int j = 1; j < 16; j++) v[j] = gf_add(v[j & (j - 1)], B[gf_tab_ctz4(j)]);
-  uint4* out = LH + half * 256;
-#pragma unroll
-  for (int j = 0; j < 16; j++) out[j * 16 + k] = make_uint4(v[j].w[0], v[j].w[1], v[j].w[2], v[j].w[3]);
-}
-
-// Part of the byte table from the nibble tables, by rows: item = s * 256 +
-// (g << 4 | k) writes the 16 / SPLIT slots (v << 4) + k of v = 16 g + j, j in
-// part s of 0..15, as L[j][k] + H[g][k] with H[g][k] read once (a third fewer
-// shared-memory accesses than entry by entry). Eight consecutive items have
-// eight consecutive k, so their reads and writes hit distinct bank groups.
-template <int SPLIT>
-__device__ __forceinline__ void gf_tab_rows(const uint4* __restrict__ LH, uint4* __restrict__ T, int item) {
-  constexpr int J = 16 / SPLIT;
-  const int s = item >> 8, g = (item >> 4) & 15, k = item & 15;
-  const uint4 h = LH[256 + g * 16 + k];
-#pragma unroll
-  for (int jj = 0; jj < J; jj++) {
-    const int j = s * J + jj;
-    const uint4 l = LH[j * 16 + k];
-    T[((16 * g + j) << 4) + k] = make_uint4(l.x ^ h.x, l.y ^ h.y, l.z ^ h.z, l.w ^ h.w);
-  }
-}
-
 // One row of the byte table computed directly, without nibble tables or a
 // barrier: item = g << 4 | k (g, k < 16) writes the 16 slots (v << 4) + k of
 // v = 16 g + j, j < 16, i.e. t v x^(8k) = L_k(j) + H_k(g) with L_k(j) the sum
 // of t x^(8k+b) over the bits b of j and H_k(g) that of t x^(8k+4+b) over the
 // bits of g. The eight images t x^(8k+b) come from one shift and seven
-// doublings; j walks the Gray code, one XOR per slot. Suits tables rebuilt
-// often (one multiplier after another): every thread works, nothing waits on
-// a serial nibble phase. Eight consecutive items have eight consecutive k,
-// so their writes hit distinct bank groups.
+// doublings; j walks the Gray code, one XOR per slot. Every thread works from
+// the start (measured faster than building 16-entry nibble tables first, whose
+// serial phase leaves most warps waiting, and with 16 B fewer shared-memory
+// reads per slot). Eight consecutive items have eight consecutive k, so their
+// writes hit distinct bank groups.
 __device__ __forceinline__ void gf_tab_row_direct(gf128 t, uint4* __restrict__ T, int item) {
   const int g = (item >> 4) & 15, k = item & 15;
   gf128 B[8];
@@ -126,12 +90,10 @@ __device__ __forceinline__ void gf_tab_row_direct(gf128 t, uint4* __restrict__ T
   }
 }
 
-// Byte tables of one multiplier t into T (GF_TAB_ENTRIES slots), using LH
-// (GF_TAB_NIBBLE_SLOTS slots) as scratch. All threads of the CTA call it; it
-// ends with a barrier, after which T is ready.
-__device__ __forceinline__ void gf_tab_build(gf128 t, uint4* __restrict__ T, uint4* __restrict__ LH) {
-  if (threadIdx.x < 32) gf_tab_nibbles(t, LH, threadIdx.x);
-  __syncthreads();
-  for (int it = threadIdx.x; it < 256; it += blockDim.x) gf_tab_rows<1>(LH, T, it);
+// Byte tables of one multiplier t into T (GF_TAB_ENTRIES slots): all threads
+// of the CTA call it (any block size); it ends with a barrier, after which T
+// is ready.
+__device__ __forceinline__ void gf_tab_build(gf128 t, uint4* __restrict__ T) {
+  for (int it = threadIdx.x; it < 256; it += blockDim.x) gf_tab_row_direct(t, T, it);
   __syncthreads();
 }

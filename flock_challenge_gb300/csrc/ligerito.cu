@@ -49,7 +49,7 @@ lig_fold_msg_kernel(const gf128* __restrict__ f, const gf128* __restrict__ b, si
                     gf128* __restrict__ fo, gf128* __restrict__ bo, gf128* __restrict__ partials) {
   extern __shared__ uint4 rtab[];
   const uint32_t rot = threadIdx.x & 15;
-  if (use_tab) gf_tab_build(r_plain, rtab, rtab + GF_TAB_ENTRIES);
+  if (use_tab) gf_tab_build(r_plain, rtab);
   gf256 u0 = {{0, 0, 0, 0}}, u2 = u0, zz = u0;
   size_t pairs = n_out / 2;
   for (size_t j = (size_t)blockIdx.x * LG_THREADS + threadIdx.x; j < pairs; j += (size_t)gridDim.x * LG_THREADS) {
@@ -232,7 +232,7 @@ int flock_lig_grid(size_t n_pairs) { return (int)grid_for(n_pairs, LG_THREADS, 1
 
 int flock_launch_lig_fold_msg(const void* f, const void* b, size_t n_out, int fold, const uint64_t r[2], void* fo,
                               void* bo, void* partials, int grid, cudaStream_t st) {
-  constexpr size_t kTabSmem = (size_t)(GF_TAB_ENTRIES + GF_TAB_NIBBLE_SLOTS) * 16;
+  constexpr size_t kTabSmem = (size_t)GF_TAB_ENTRIES * 16;
   flock_once_per_device((const void*)lig_fold_msg_kernel, [] {
     cudaFuncSetAttribute(lig_fold_msg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTabSmem);
   });

@@ -294,15 +294,16 @@ constexpr int kMaxPassLayers = variant_max_layers(kDefaultVariant);
 // positions of one lane.
 constexpr int TAB_THREADS = 512;
 constexpr int TAB_ENTRIES = GF_TAB_ENTRIES;
-constexpr size_t TAB_SMEM = (size_t)3 * TAB_ENTRIES * 16 + (size_t)3 * GF_TAB_NIBBLE_SLOTS * 16;
+constexpr size_t TAB_SMEM = (size_t)3 * TAB_ENTRIES * 16;
 
 // Byte tables of the three twiddles t[0..2] into T (3 x TAB_ENTRIES slots),
-// through their nibble tables in LH (3 x 512 slots). All threads take part.
-__device__ void build_tabs3(const gf128 t[3], uint4* __restrict__ T, uint4* __restrict__ LH) {
-  if (threadIdx.x < 96) gf_tab_nibbles(t[threadIdx.x >> 5], LH + (threadIdx.x >> 5) * 512, threadIdx.x & 31);
-  __syncthreads();
-  for (int it = threadIdx.x; it < 3 * 512; it += blockDim.x)
-    gf_tab_rows<2>(LH + (it >> 9) * 512, T + (it >> 9) * TAB_ENTRIES, it & 511);
+// one row (256 per table) per item, computed directly (gf_tab_row_direct):
+// every thread works from the start, with no serial nibble phase.
+__device__ void build_tabs3(const gf128 t[3], uint4* __restrict__ T) {
+  for (int it = threadIdx.x; it < 3 * 256; it += blockDim.x) {
+    const int w = it >> 8;
+    gf_tab_row_direct(w == 0 ? t[0] : w == 1 ? t[1] : t[2], T + w * TAB_ENTRIES, it & 255);
+  }
 }
 
 // Layers l, l + 1 of the transform for block hi of layer l (blockIdx.x / cph)
@@ -311,12 +312,12 @@ __device__ void build_tabs3(const gf128 t[3], uint4* __restrict__ T, uint4* __re
 __global__ void __launch_bounds__(TAB_THREADS, 1)
 ntt_tab2_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t src_pos_mask,
                 const gf128* __restrict__ tw, int log_d, int log_lanes, int l, int cph) {
-  extern __shared__ uint4 tabs[];  // [3][TAB_ENTRIES], then the nibble tables [3][2][16][16]
+  extern __shared__ uint4 tabs[];  // [3][TAB_ENTRIES]
   const size_t hi = blockIdx.x / cph;
   const int part = blockIdx.x % cph;
   const gf128 t3[3] = {tw[((size_t)1 << l) - 1 + hi], tw[((size_t)1 << (l + 1)) - 1 + 2 * hi],
                        tw[((size_t)1 << (l + 1)) - 1 + 2 * hi + 1]};
-  build_tabs3(t3, tabs, tabs + 3 * TAB_ENTRIES);
+  build_tabs3(t3, tabs);
   __syncthreads();
   // block 0 of every layer has twiddle 0: its butterflies need no product
   const bool za = hi == 0, zb = hi == 0;

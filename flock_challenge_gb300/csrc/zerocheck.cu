@@ -409,7 +409,7 @@ zc_round_kernel(const gf128* __restrict__ A, const gf128* __restrict__ B, size_t
                 int lo_bits, gf128* __restrict__ partials) {
   extern __shared__ uint4 rtab[];
   const uint32_t rot = threadIdx.x & 15;
-  if (use_tab) gf_tab_build(rho_plain, rtab, rtab + GF_TAB_ENTRIES);
+  if (use_tab) gf_tab_build(rho_plain, rtab);
   // grid-stride over hi blocks: each CTA handles whole hi indices
   const size_t lo_n = (size_t)1 << lo_bits;
   const size_t n_hi = (n_pairs + lo_n - 1) / lo_n;
@@ -579,7 +579,7 @@ zc_round_grp_kernel(const void* __restrict__ in0, const void* __restrict__ in1, 
   extern __shared__ gf128 tab[];
   uint4* rtab = reinterpret_cast<uint4*>(tab);
   const uint32_t rot = threadIdx.x & 15;
-  if constexpr (!SKIP) gf_tab_build(rho, rtab, rtab + GF_TAB_ENTRIES);
+  if constexpr (!SKIP) gf_tab_build(rho, rtab);
   if constexpr (SKIP) {
     for (int e = threadIdx.x; e < 8 * 256; e += blockDim.x) {
       const int v = e >> 3, c = e & 7;
@@ -694,7 +694,7 @@ int flock_launch_zc_round(const void* A, const void* B, size_t n_pairs, int bind
                           int grid, cudaStream_t st) {
   gf128 r;
   r.w[0] = (uint32_t)rho[0]; r.w[1] = (uint32_t)(rho[0] >> 32); r.w[2] = (uint32_t)rho[1]; r.w[3] = (uint32_t)(rho[1] >> 32);
-  constexpr size_t kTabSmem = (size_t)(GF_TAB_ENTRIES + GF_TAB_NIBBLE_SLOTS) * 16;
+  constexpr size_t kTabSmem = (size_t)GF_TAB_ENTRIES * 16;
   flock_once_per_device((const void*)zc_round_kernel, [] {
     cudaFuncSetAttribute(zc_round_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTabSmem);
   });
@@ -728,7 +728,7 @@ int flock_launch_zc_round_grp(const void* in0, const void* in1, size_t n_pairs, 
   if (n_pairs % per_h != 0 || grid < 1) return FLOCK_ERR_SHAPE;
   gf128 r;
   r.w[0] = (uint32_t)rho[0]; r.w[1] = (uint32_t)(rho[0] >> 32); r.w[2] = (uint32_t)rho[1]; r.w[3] = (uint32_t)(rho[1] >> 32);
-  constexpr size_t kTabSmem = (size_t)(GF_TAB_ENTRIES + GF_TAB_NIBBLE_SLOTS) * 16;
+  constexpr size_t kTabSmem = (size_t)GF_TAB_ENTRIES * 16;
   flock_once_per_device((const void*)zc_round_grp_kernel<false>, [] {
     cudaFuncSetAttribute(zc_round_grp_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTabSmem);
   });

@@ -2,7 +2,8 @@
 visits each byte position once with its own byte, and at every step eight
 consecutive threads read eight distinct bank groups (a 16-byte slot's bank
 group is its index mod 8), which is what makes the random lookups
-conflict-free. The formulas restate those of csrc/gf_tab.cuh (gf_mul_tab),
+conflict-free. The formulas restate those of csrc/gf_tab.cuh (gf_mul_tab and
+the byte-table rows of gf_tab_row_direct),
 csrc/open.cu (combined basis), csrc/zerocheck.cu (round-1 extension tables,
 phi8 nibble tables, skip tables) and csrc/lincheck.cu (stripe fold)."""
 
@@ -107,32 +108,6 @@ def test_phi8_nibble_tables_weight_by_eq():
     for v in range(256):
         lo, hi = L[v & 15], H[v >> 4]
         assert (lo[0] ^ hi[0], lo[1] ^ hi[1]) == O.gf_mul(O.phi8(v), e), v
-
-
-def gf_tab_rows_slots(item, split):
-    """(read L slot, read H slot, written T slot) triples of gf_tab_rows<split>(item)."""
-    J = 16 // split
-    s, g, k = item >> 8, (item >> 4) & 15, item & 15
-    return [(j * 16 + k, 256 + g * 16 + k, ((16 * g + j) << 4) + k) for j in range(s * J, (s + 1) * J)]
-
-
-def test_gf_tab_rows_cover_every_slot_once():
-    for split in (1, 2):
-        written = [t for it in range(256 * split) for (_, _, t) in gf_tab_rows_slots(it, split)]
-        assert sorted(written) == list(range(4096)), split
-        for it in range(256 * split):
-            for l, h, t in gf_tab_rows_slots(it, split):
-                v, k = t >> 4, t & 15
-                assert l == (v & 15) * 16 + k and h == 256 + (v >> 4) * 16 + k  # L[v & 15][k] + H[v >> 4][k]
-
-
-def test_gf_tab_rows_bank_groups_distinct():
-    for split in (1, 2):
-        for base in range(0, 256 * split, 8):
-            steps = [gf_tab_rows_slots(it, split) for it in range(base, base + 8)]
-            for st in range(16 // split):
-                for which in range(3):
-                    assert len({steps[q][st][which] % 8 for q in range(8)}) == 8
 
 
 def test_gf_tab_row_direct_gray_walk():
