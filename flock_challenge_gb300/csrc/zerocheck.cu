@@ -80,27 +80,28 @@ __device__ __forceinline__ uint64_t transpose8x8(uint64_t x) {
   return x;
 }
 
-// Eight 64-bit planes -> 64 bytes (byte i = sum_j bit i of p[j] << j), as 16
-// words in dst (word k holds bytes 4k .. 4k+3), written with 16-byte stores.
-__device__ __forceinline__ void planes_to_bytes(const uint64_t p[8], uint32_t* dst) {
-  uint32_t o[16];
+// Eight 64-bit planes -> bytes 32 h .. 32 h + 31 of the 64 (byte i = sum_j
+// bit i of p[j] << j), as words 8 h .. 8 h + 7 of dst (word k holds bytes
+// 4k .. 4k+3), written with two 16-byte stores: the two half-warps holding
+// the same planes produce one half of the bytes each.
+__device__ __forceinline__ void planes_to_bytes_half(const uint64_t p[8], uint32_t* dst, int h) {
+  uint32_t q[8];
 #pragma unroll
-  for (int g = 0; g < 8; g++) {
-    const int hw = g >> 2, b = g & 3;
-    uint32_t q[8];
+  for (int j = 0; j < 8; j++) q[j] = h ? (uint32_t)(p[j] >> 32) : (uint32_t)p[j];
+  uint32_t o[8];
 #pragma unroll
-    for (int j = 0; j < 8; j++) q[j] = hw ? (uint32_t)(p[j] >> 32) : (uint32_t)p[j];
-    // byte j of x = byte g of p[j]
+  for (int b = 0; b < 4; b++) {
+    // byte j of x = byte b of q[j]
     const uint32_t sel = (uint32_t)b | ((uint32_t)(b + 4) << 4);
     const uint32_t lo = __byte_perm(__byte_perm(q[0], q[1], sel), __byte_perm(q[2], q[3], sel), 0x5410);
     const uint32_t hi = __byte_perm(__byte_perm(q[4], q[5], sel), __byte_perm(q[6], q[7], sel), 0x5410);
     const uint64_t y = transpose8x8(((uint64_t)hi << 32) | lo);
-    o[2 * g] = (uint32_t)y;
-    o[2 * g + 1] = (uint32_t)(y >> 32);
+    o[2 * b] = (uint32_t)y;
+    o[2 * b + 1] = (uint32_t)(y >> 32);
   }
-#pragma unroll
-  for (int k = 0; k < 4; k++)
-    reinterpret_cast<uint4*>(dst)[k] = make_uint4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
+  uint4* d = reinterpret_cast<uint4*>(dst + 8 * h);
+  d[0] = make_uint4(o[0], o[1], o[2], o[3]);
+  d[1] = make_uint4(o[4], o[5], o[6], o[7]);
 }
 
 // a ^= v << sh for 0 <= sh < 16, branch-free.
@@ -112,6 +113,12 @@ __device__ __forceinline__ void acc_shift_xor_v(Acc5& a, const uint4 v, uint32_t
   a.w[4] ^= __funnelshift_l(v.w, 0u, sh);
 }
 
+__device__ __forceinline__ uint64_t shfl_xor64(uint64_t v, int m) {
+  const uint32_t lo = __shfl_xor_sync(0xffffffffu, (uint32_t)v, m);
+  const uint32_t hi = __shfl_xor_sync(0xffffffffu, (uint32_t)(v >> 32), m);
+  return ((uint64_t)hi << 32) | lo;
+}
+
 // Shared memory of the round-1 kernel (32-bit words):
 //   ext  [4 quarters q][256 values v][8 byte positions c] of 16 B (a value's
 //        eight 64-bit planes, quarter q = planes 2q, 2q+1): the table of byte
@@ -119,39 +126,44 @@ __device__ __forceinline__ void acc_shift_xor_v(Acc5& a, const uint4 v, uint32_t
 //        step k lane l looks up byte position (l + k) mod 8, so any eight
 //        consecutive lanes hit eight distinct bank groups and the random
 //        lookups are conflict-free;
-//   LH   per warp, per half (one outer block xo): the eq-weighted phi8 nibble
-//        tables L[j] = phi8(j) e and H[g] = phi8(16 g) e, e = eq_out(xo), four
-//        replicas each (entry j of replica r at slot 4 j + r, lane l reads
-//        replica l mod 4, so at most two lanes of a quarter warp share a
-//        bank group): phi8(v) e = L[v & 15] + H[v >> 4], because phi8 is
-//        additive, so the block's values come out already weighted and need
-//        no GF(2^128) product (eight per block build the tables instead of
-//        twelve per lane);
-//   P    per warp, per half: phi8(2^k) e for k < 8, the tables' basis;
-//   xch  per warp, per half: [16 xm] rows of 20 words (64 bytes used; the
-//        odd 80-byte row pitch makes the 16-byte stores conflict-free), one
-//        plane set at a time, halves 336 words apart (16 mod 32 banks) so both
-//        halves' reads of one row index hit disjoint banks.
-// Measured against three-set exchange areas and a two-stage exchange, the
-// one-set exchange with 12 warps is fastest despite its register spills.
+//   LH   per warp (one outer block xo per warp at a time): the eq-weighted
+//        phi8 nibble tables L[j] = phi8(j) e and H[g] = phi8(16 g) e,
+//        e = eq_out(xo), eight replicas each (entry j of replica r at slot
+//        8 j + r, H 128 slots after L; lane l reads replica l mod 8, so the
+//        lookups are conflict-free): phi8(v) e = L[v & 15] + H[v >> 4],
+//        because phi8 is additive, so the block's values come out already
+//        weighted and need no GF(2^128) product (eight per block build the
+//        tables instead of twelve per lane);
+//   P    per warp: phi8(2^k) e for k < 8, the tables' basis;
+//   xch  per warp: [16 producer rows] of 20 words (64 bytes used; the odd
+//        80-byte row pitch makes the 16-byte stores conflict-free), one plane
+//        set at a time.
+// The two half-warps share the outer block: each sums half of its rows, the
+// halves add their planes with one exchange of registers, each converts half
+// of the points to bytes, and each lane then handles two of the 64 points.
+// One block per warp (instead of one per half-warp) halves the nibble tables
+// per warp, which makes room for the eight replicas: with four, two lanes of
+// a quarter warp shared a bank group and nine quarter-warp lookups in ten
+// took two wavefronts.
 constexpr int R1_ROW = 20;
-constexpr int R1_HALF = 16 * R1_ROW + 16;
+constexpr int R1_XCH = 16 * R1_ROW;
 constexpr int R1_WARPS = R1_THREADS / 32;
-constexpr size_t R1_SMEM = (size_t)8 * 4 * 256 * 16 + (size_t)R1_WARPS * 2 * 128 * 16 + (size_t)R1_WARPS * 2 * 8 * 16 +
-                           128 + (size_t)R1_WARPS * 2 * R1_HALF * 4;
+constexpr size_t R1_SMEM = (size_t)8 * 4 * 256 * 16 + (size_t)R1_WARPS * 256 * 16 + (size_t)R1_WARPS * 8 * 16 + 128 +
+                           (size_t)R1_WARPS * R1_XCH * 4;
 static_assert(R1_SMEM <= 232448, "round-1 shared memory above the 227 KB per-block limit");
 
-// grid: each warp walks pairs of outer blocks; lane: xm = lane & 15, xo half = lane >> 4.
+// grid: each warp walks outer blocks; lane: xm = lane & 15 (producer row
+// group, then point quad), h = lane >> 4 (row half, then point pair).
 __global__ void __launch_bounds__(R1_THREADS, 1)
 zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B, const uint64_t* __restrict__ C,
                  size_t n_outer, const gf128* __restrict__ eq_out, const ZcRound1Tables* __restrict__ T,
                  gf128* __restrict__ partials) {
   extern __shared__ uint4 sm[];
   uint4* ext = sm;                                                   // [4][256][8]
-  uint4* lh = ext + 8 * 4 * 256;                                     // per warp, half [L, H][16][4]
-  uint4* pb = lh + R1_WARPS * 2 * 128;                               // per warp, half [8]
-  uint4* phik = pb + R1_WARPS * 2 * 8;                               // phi8(2^k), k < 8
-  uint32_t* xch = reinterpret_cast<uint32_t*>(phik + 8);             // per warp [2][R1_HALF]
+  uint4* lh = ext + 8 * 4 * 256;                                     // per warp [L, H][16][8]
+  uint4* pk_s = lh + R1_WARPS * 256;                                 // per warp [8]
+  uint4* phik = pk_s + R1_WARPS * 8;                                 // phi8(2^k), k < 8
+  uint32_t* xch = reinterpret_cast<uint32_t*>(phik + 8);             // per warp [R1_XCH]
   const uint64_t* ext_src = &T->ext[0][0][0];
   for (int i = threadIdx.x; i < 8 * 4 * 256; i += R1_THREADS) {
     const int q = i >> 11, v = (i >> 3) & 255, c = i & 7;
@@ -161,33 +173,33 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
   if (threadIdx.x < 8) phik[threadIdx.x] = reinterpret_cast<const uint4*>(T->phi8)[1 << threadIdx.x];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int xm = lane & 15, half = lane >> 4;
-  uint32_t* my_x = xch + warp * (2 * R1_HALF) + half * R1_HALF;
-  gf128 sum_ab[4], sum_c[8];
+  const int xm = lane & 15, h = lane >> 4;
+  uint32_t* my_x = xch + warp * R1_XCH;
+  uint4* my_lh = lh + warp * 256;
+  uint4* my_p = pk_s + warp * 8;
+  const uint4* my_l = my_lh + (lane & 7);
+  const uint4* my_h = my_lh + 128 + (lane & 7);
+  // points 4 xm + 2 h + {0, 1}: a b sums, then c sums of parity 0 and 1
+  gf128 sum_ab[2], sum_c[4];
 #pragma unroll
-  for (int q = 0; q < 4; q++) sum_ab[q] = gf_zero();
+  for (int q = 0; q < 2; q++) sum_ab[q] = gf_zero();
 #pragma unroll
-  for (int q = 0; q < 8; q++) sum_c[q] = gf_zero();
+  for (int q = 0; q < 4; q++) sum_c[q] = gf_zero();
 
-  const size_t total_warps = (size_t)gridDim.x * (R1_THREADS / 32);
-  const size_t gwarp = (size_t)blockIdx.x * (R1_THREADS / 32) + warp;
-  for (size_t pair = gwarp; 2 * pair < n_outer; pair += total_warps) {
-    const size_t xo = 2 * pair + half;
-    const bool live = xo < n_outer;
+  const size_t total_warps = (size_t)gridDim.x * R1_WARPS;
+  for (size_t xo = (size_t)blockIdx.x * R1_WARPS + warp; xo < n_outer; xo += total_warps) {
     uint64_t w[8], t[16];
 #pragma unroll
     for (int j = 0; j < 8; j++) w[j] = 0;
 #pragma unroll
     for (int j = 0; j < 16; j++) t[j] = 0;
-    if (live) {
-      const size_t row0 = xo * 128 + (size_t)xm * 8;
-
+    const size_t row0 = xo * 128 + (size_t)xm * 8 + 4 * h;
 #pragma unroll 1
-      for (int xs2 = 0; xs2 < 4; xs2++)
+    for (int xs2 = 0; xs2 < 2; xs2++)
 #pragma unroll kZc1ParUnroll
       for (int par = 0; par < 2; par++) {
-        const int xs = 2 * xs2 + par;
-        uint64_t ra = A[row0 + xs], rb = B[row0 + xs], rc = C[row0 + xs];
+        const int xs = 4 * h + 2 * xs2 + par;
+        const uint64_t ra = A[row0 + 2 * xs2 + par], rb = B[row0 + 2 * xs2 + par], rc = C[row0 + 2 * xs2 + par];
         uint64_t ea[8], eb[8];
 #pragma unroll
         for (int j = 0; j < 8; j++) { ea[j] = 0; eb[j] = 0; }
@@ -228,101 +240,88 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
           }
         }
       }
-    }
-    // Hand the three plane sets, one at a time, to the lanes of this half as
-    // bytes: the lane of point quad xm reads word xm of every producer row,
-    // and handles points / skip positions 4*xm .. 4*xm+3 of its half (and
-    // both parities t of the c statistic).
+    // the two halves' row sums of producer group xm: add them
+#pragma unroll
+    for (int j = 0; j < 8; j++) w[j] ^= shfl_xor64(w[j], 16);
+#pragma unroll
+    for (int j = 0; j < 16; j++) t[j] ^= shfl_xor64(t[j], 16);
     // eq-weighted phi8 nibble tables of this block (see the layout above)
-    uint4* my_lh = lh + (warp * 2 + half) * 128;
-    uint4* my_p = pb + (warp * 2 + half) * 8;
-    if (xm < 8) {
-      const gf128 e = live ? gf_load(&eq_out[xo]) : gf_zero();
-      const uint4 f = phik[xm];
-      const gf128 pk = gf_mul(gf128{{f.x, f.y, f.z, f.w}}, e);
-      my_p[xm] = make_uint4(pk.w[0], pk.w[1], pk.w[2], pk.w[3]);
+    if (lane < 8) {
+      const gf128 e = gf_load(&eq_out[xo]);
+      const uint4 f = phik[lane];
+      const gf128 p = gf_mul(gf128{{f.x, f.y, f.z, f.w}}, e);
+      my_p[lane] = make_uint4(p.w[0], p.w[1], p.w[2], p.w[3]);
     }
     __syncwarp();
     {
-      uint4 lo = make_uint4(0, 0, 0, 0), hi = lo;
+      // half 0 builds L[xm], half 1 H[xm]; replica (r + xm) mod 8 at step r
+      // keeps the eight stores of a quarter warp in distinct bank groups
+      const uint4* src = my_p + 4 * h;
+      uint4 val = make_uint4(0, 0, 0, 0);
 #pragma unroll
       for (int k = 0; k < 4; k++)
         if ((xm >> k) & 1) {
-          const uint4 a = my_p[k], b = my_p[4 + k];
-          lo.x ^= a.x; lo.y ^= a.y; lo.z ^= a.z; lo.w ^= a.w;
-          hi.x ^= b.x; hi.y ^= b.y; hi.z ^= b.z; hi.w ^= b.w;
+          const uint4 a = src[k];
+          val.x ^= a.x; val.y ^= a.y; val.z ^= a.z; val.w ^= a.w;
         }
+      uint4* dst = my_lh + 128 * h + 8 * xm;
 #pragma unroll
-      for (int r = 0; r < 4; r++) {
-        my_lh[4 * xm + r] = lo;
-        my_lh[64 + 4 * xm + r] = hi;
-      }
+      for (int r = 0; r < 8; r++) dst[(r + xm) & 7] = val;
     }
-    const uint4* my_l = my_lh + (lane & 3);
-    const uint4* my_h = my_lh + 64 + (lane & 3);
-    // one plane set per iteration (not unrolled, which keeps the loop inside
-    // the instruction cache)
+    // Hand the three plane sets, one at a time, to the lanes as bytes: the
+    // lanes of point quad xm read word xm of every producer row, half h
+    // taking points 4 xm + 2 h, 4 xm + 2 h + 1.
 #pragma unroll 1
     for (int set = 0; set < 3; set++) {
       uint64_t pl[8];
 #pragma unroll
       for (int j = 0; j < 8; j++) pl[j] = set == 0 ? w[j] : set == 1 ? t[j] : t[8 + j];
       __syncwarp();
-      planes_to_bytes(pl, my_x + xm * R1_ROW);
+      planes_to_bytes_half(pl, my_x + xm * R1_ROW, h);
       __syncwarp();
-      if (live) {
-        Acc5 v[4];
+      Acc5 v[2];
 #pragma unroll
-        for (int q = 0; q < 4; q++)
+      for (int q = 0; q < 2; q++)
 #pragma unroll
-          for (int k = 0; k < 5; k++) v[q].w[k] = 0;
+        for (int k = 0; k < 5; k++) v[q].w[k] = 0;
 #pragma unroll 4
-        for (int mm2 = 0; mm2 < 16; mm2++) {
-          const uint32_t bw = my_x[mm2 * R1_ROW + xm];
+      for (int mm2 = 0; mm2 < 16; mm2++) {
+        const uint32_t bw = my_x[mm2 * R1_ROW + xm] >> (16 * h);
 #pragma unroll
-          for (int q = 0; q < 4; q++) {
-            const uint32_t v8 = (bw >> (8 * q)) & 255;
-            const uint4 a = my_l[(v8 & 15) << 2], b = my_h[(v8 >> 4) << 2];
-            acc_shift_xor_v(v[q], make_uint4(a.x ^ b.x, a.y ^ b.y, a.z ^ b.z, a.w ^ b.w), (uint32_t)mm2);
-          }
+        for (int q = 0; q < 2; q++) {
+          const uint32_t v8 = (bw >> (8 * q)) & 255;
+          const uint4 a = my_l[(v8 & 15) << 3], b = my_h[(v8 >> 4) << 3];
+          acc_shift_xor_v(v[q], make_uint4(a.x ^ b.x, a.y ^ b.y, a.z ^ b.z, a.w ^ b.w), (uint32_t)mm2);
         }
+      }
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-          const gf128 p = acc_reduce(v[q]);
-          if (set == 0) sum_ab[q] = gf_add(sum_ab[q], p);
-          else if (set == 1) sum_c[q] = gf_add(sum_c[q], p);
-          else sum_c[4 + q] = gf_add(sum_c[4 + q], p);
-        }
+      for (int q = 0; q < 2; q++) {
+        const gf128 p = acc_reduce(v[q]);
+        if (set == 0) sum_ab[q] = gf_add(sum_ab[q], p);
+        else if (set == 1) sum_c[q] = gf_add(sum_c[q], p);
+        else sum_c[2 + q] = gf_add(sum_c[2 + q], p);
       }
     }
     __syncwarp();
   }
-  // lanes l and l + 16 hold the same points: combine; then reduce the warps
-  // of the block in shared memory (reusing the extension tables) and write one
-  // row of 192 partial sums per block: 64 P^AB values, then S[0..128).
-#pragma unroll
-  for (int q = 0; q < 4; q++)
-#pragma unroll
-    for (int k = 0; k < 4; k++) sum_ab[q].w[k] ^= __shfl_xor_sync(0xffffffffu, sum_ab[q].w[k], 16);
-#pragma unroll
-  for (int q = 0; q < 8; q++)
-#pragma unroll
-    for (int k = 0; k < 4; k++) sum_c[q].w[k] ^= __shfl_xor_sync(0xffffffffu, sum_c[q].w[k], 16);
+  // reduce the warps of the block in shared memory (reusing the extension
+  // tables) and write one row of 192 partial sums per block: 64 P^AB values,
+  // then S[0..128).
   __syncthreads();
   gf128* red = reinterpret_cast<gf128*>(ext);  // [warps][192], in the no longer needed extension tables
-  if (half == 0) {
-    gf128* o = red + warp * 192;
+  {
+    gf128* o = red + warp * 192 + 4 * xm + 2 * h;
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      o[4 * xm + q] = sum_ab[q];
-      o[64 + 4 * xm + q] = sum_c[q];
-      o[128 + 4 * xm + q] = sum_c[4 + q];
+    for (int q = 0; q < 2; q++) {
+      o[q] = sum_ab[q];
+      o[64 + q] = sum_c[q];
+      o[128 + q] = sum_c[2 + q];
     }
   }
   __syncthreads();
   for (int col = threadIdx.x; col < 192; col += R1_THREADS) {
     gf128 acc = gf_zero();
-    for (int w2 = 0; w2 < R1_THREADS / 32; w2++) acc = gf_add(acc, red[w2 * 192 + col]);
+    for (int w2 = 0; w2 < R1_WARPS; w2++) acc = gf_add(acc, red[w2 * 192 + col]);
     partials[(size_t)blockIdx.x * 192 + col] = acc;
   }
 }
