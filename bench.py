@@ -50,15 +50,16 @@ PUBLISHED = 483866.0  # README.md:110-116, unmodified reference, Apple M4 Pro ru
 # launch set, from ncu on a 2^18-position case scaled by positions (traffic
 # grows in proportion): profiles/ntt_pass_l0_2e16.md.
 # DRAM bytes (read + write) per NTT pass at the bench's shape (2^20 positions x
-# 64 lanes): 486.5 MB per pass measured by ncu at 2^18 positions (mean of the
-# five L0 passes in profiles/ntt_pass_l0_2e16.md), times 4 for 4x the positions.
-NTT_TRAFFIC_PER_PASS = {20: 4 * 486.5e6}
+# 64 lanes): 479.2 MB per pass measured by ncu at 2^18 positions (mean of the
+# eight L0 passes in profiles/ntt_instructions_2e18pos.md), times 4 for 4x the
+# positions.
+NTT_TRAFFIC_PER_PASS = {20: 4 * 479.2e6}
 NTT_MAX_LAYERS = {0: 4, 1: 6, 2: 8}  # layers per pass of the autotuner's pass shapes
 # Thread instructions per GF(2^128) product in the table passes and per
 # butterfly in the multiply passes, measured by ncu on the 2^18-position L0
 # transform (profiles/ntt_instructions_2e18pos.md).
-NTT_INSTR_PER_TABLE_PRODUCT = 152
-NTT_INSTR_PER_MULTIPLY_BUTTERFLY = 437
+NTT_INSTR_PER_TABLE_PRODUCT = 168
+NTT_INSTR_PER_MULTIPLY_BUTTERFLY = 433
 
 
 def load_peaks():
@@ -213,10 +214,10 @@ def kernel_roofline(F, ctx_handle, stream_ptr, log2, peaks, torch, dev, clock_mh
     F.lib().flock_ntt_tuned_variant.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     variant = F.lib().flock_ntt_tuned_variant(dev.index or 0, log_d, 6, 1)
     max_f = NTT_MAX_LAYERS.get(variant, 6)
-    # byte-table passes of two layers while a block holds >= 2^11 quad-lanes
+    # byte-table passes of two layers while a block holds >= 2^9 quad-lanes
     # (the library's rule), then multiply passes of <= max_f layers
     tab_end = 1
-    while tab_end + 1 < log_d and log_d - tab_end - 2 + 6 >= 11:
+    while tab_end + 1 < log_d and log_d - tab_end - 2 + 6 >= 9:
         tab_end += 2
     tab_passes = (tab_end - 1) // 2
     passes = tab_passes + (log_d - tab_end + max_f - 1) // max_f

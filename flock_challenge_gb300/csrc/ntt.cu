@@ -212,6 +212,20 @@ int launch_pass(gf128* dst, const gf128* src, size_t mask, const void* tw, int l
     return FLOCK_ERR_SHAPE;
   } else {
     size_t tiles = (size_t)1 << (log_d - F);
+    if constexpr (PassShape<F, 16, V>::THREADS < 32) {
+      // A pass no deeper than the shape's positions per thread needs one
+      // thread per lane: with 16 lanes a block would fill half a warp, so
+      // codes of 32 lanes or more take 32 lanes per block.
+      if (log_lanes >= 5) {
+        using S = PassShape<F, 32, V>;
+        static_assert(S::SMEM <= 48 * 1024, "one-stage passes use no tile");
+        size_t blocks = tiles * ((1 << log_lanes) / 32);
+        ntt_pass_kernel<F, 32, PREP, V>
+            <<<(unsigned)blocks, S::THREADS, S::SMEM, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
+        flock_count_launch();
+        return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+      }
+    }
     if (log_lanes >= 4) {
       using S = PassShape<F, 16, V>;
       size_t blocks = tiles * ((1 << log_lanes) / 16);
@@ -350,12 +364,15 @@ ntt_tab2_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t s
 }
 
 // Layers [start, end) handled by table passes: pairs of layers while a block
-// of the pass's first layer l holds at least 2^11 quad-lanes (its three tables
-// are then built for at least 8 K products; deeper blocks are left to the
-// multiply passes).
+// of the pass's first layer l holds at least 2^kTabMinLog quad-lanes (its three
+// tables are then built for at least 2 K products; deeper blocks are left to
+// the multiply passes). Measured at 2^20 positions x 64 lanes: 2^9 beats 2^11
+// by 0.3 ms (one more table pass, two layers fewer in the multiply pass), 2^8
+// ties and 2^7 (a lone last layer in the multiply pass) loses 2.2 ms.
+constexpr int kTabMinLog = 9;
 int tab_layers_end(int log_d, int log_lanes, int start) {
   int l = start;
-  while (l + 1 < log_d && log_d - l - 2 + log_lanes >= 11) l += 2;
+  while (l + 1 < log_d && log_d - l - 2 + log_lanes >= kTabMinLog) l += 2;
   return l;
 }
 

@@ -85,7 +85,7 @@ int flock_ntt(flock_ctx* ctx, void* d_data, int log_d, int log_num_ntts, int sta
  * yet. The first flock_ntt / commit / proof of a shape times the shapes on a
  * scratch buffer and keeps the fastest; FLOCK_NTT_TUNE=0 in the environment
  * disables tuning. The shape applies to the multiply passes: the upper
- * layers, whose blocks hold at least 2^11 position-quads x lanes, run as
+ * layers, whose blocks hold at least 2^9 position-quads x lanes, run as
  * byte-table passes of two layers. No reference counterpart. */
 int flock_ntt_tuned_variant(int device, int log_d, int log_lanes, int start_layer);
 

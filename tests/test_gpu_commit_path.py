@@ -42,10 +42,12 @@ def test_witness_z_only(cuda_device):
 
 
 # shapes whose upper layers run as byte-table passes (a block of the pass's
-# first layer holds >= 2^11 quad-lanes): (12, 6, 1), (13, 4, 3), (10, 6, 0),
-# (9, 7, 2), (16, 6, 1), (14, 3, 2)
+# first layer holds >= 2^9 quad-lanes): (7, 6, 1), (12, 6, 1), (13, 4, 3),
+# (10, 6, 0), (9, 7, 2), (16, 6, 1), (14, 3, 2); (8, 3, 0) and (11, 4, 4) sit
+# exactly at the cutoff (one table pass, then multiply passes)
 @pytest.mark.parametrize("log_d,log_lanes,start", [(1, 4, 0), (5, 4, 0), (7, 6, 1), (12, 6, 1), (13, 4, 3),
-                                                   (10, 6, 0), (9, 7, 2), (16, 6, 1), (14, 3, 2)])
+                                                   (10, 6, 0), (9, 7, 2), (16, 6, 1), (14, 3, 2), (8, 3, 0),
+                                                   (11, 4, 4)])
 def test_ntt_matches_oracle(ctx, log_d, log_lanes, start):
     rng = np.random.default_rng(log_d * 7 + start)
     data = rng.integers(0, 2**63, (1 << (log_d + log_lanes)) * 2, dtype=np.uint64)
@@ -113,3 +115,17 @@ def test_ntt_autotuner_records_a_shape_and_keeps_results(ctx, monkeypatch):
     F.ntt(ctx, d2, 14, 4, 1)
     assert L.flock_ntt_tuned_variant(0, 14, 4, 1) == -1
     assert np.array_equal(host(d2).view(np.uint64), O.ntt_interleaved(data2, 16, 1))
+
+
+@pytest.mark.parametrize("variant", ["0", "1", "2"])
+@pytest.mark.parametrize("log_d,log_lanes,start", [(13, 6, 2), (14, 5, 0), (15, 6, 1), (9, 7, 0)])
+def test_ntt_every_pass_shape_matches_oracle(ctx, monkeypatch, variant, log_d, log_lanes, start):
+    # each multiply-pass shape fixed in turn, on codes whose last pass is no
+    # deeper than the shape's positions per thread (one thread per lane, 32
+    # lanes per block) or deeper (two stages through the shared tile)
+    monkeypatch.setenv("FLOCK_NTT_VARIANT", variant)
+    rng = np.random.default_rng(log_d * 13 + log_lanes + int(variant))
+    data = rng.integers(0, 2**63, (1 << (log_d + log_lanes)) * 2, dtype=np.uint64)
+    d = to_dev(data)
+    F.ntt(ctx, d, log_d, log_lanes, start)
+    assert np.array_equal(host(d).view(np.uint64), O.ntt_interleaved(data, 1 << log_lanes, start))
