@@ -12,7 +12,6 @@ struct ZcRound1Tables {
   uint64_t ext[8][256][8];
   uint64_t phi8[256][2];  // phi8 embedding GF(2^8) -> GF(2^128), [lo, hi]
   uint8_t e8[8];          // GF(2^8) eq weight of the three fixed small challenges
-  uint8_t e8_mat[8][8];   // multiply-by-e8[xs] as plane masks: out_j = xor_k [bit k] y_k
   uint8_t e8c[4];         // GF(2^8) eq weight of the fixed challenges r7, r8 (c statistic)
 };
 
@@ -80,12 +79,6 @@ inline void build_round1_tables(ZcRound1Tables& T) {
   }
   for (int xs = 0; xs < 8; xs++) {
     T.e8[xs] = e8(xs);
-    for (int j = 0; j < 8; j++) T.e8_mat[xs][j] = 0;
-    for (int k = 0; k < 8; k++) {
-      uint8_t col = hf::f8_mul(T.e8[xs], (uint8_t)(1u << k));
-      for (int j = 0; j < 8; j++)
-        if ((col >> j) & 1) T.e8_mat[xs][j] |= (uint8_t)(1u << k);
-    }
   }
 }
 

@@ -71,6 +71,37 @@ __device__ __forceinline__ void f8_mul_planes(const uint64_t* a, const uint64_t*
   for (int k = 0; k < 8; k++) out[k] = p[k];
 }
 
+// GF(2^8) product (modulus x^8 + x^4 + x^3 + x + 1), usable in constant
+// expressions so that multiplications by the fixed challenges below fold into
+// compile-time XOR patterns.
+__host__ __device__ constexpr uint8_t f8_mul_c(uint8_t a, uint8_t b) {
+  unsigned acc = 0;
+  for (int i = 0; i < 8; i++)
+    if ((a >> i) & 1) acc ^= (unsigned)b << i;
+  for (int i = 14; i >= 8; i--)
+    if ((acc >> i) & 1) acc ^= 0x11Bu << (i - 8);
+  return (uint8_t)acc;
+}
+
+// eq factor of one fixed small challenge: bit ? C : 1 + C.
+__host__ __device__ constexpr uint8_t f8_eq_factor(int v, int bit) {
+  return bit ? zc::SMALL_CHAL[v] : (uint8_t)(1 ^ zc::SMALL_CHAL[v]);
+}
+
+// acc (+)= E * y on bit-sliced planes, E a compile-time GF(2^8) constant: plane
+// j takes y_k where bit j of E x^k is set (about half of the 64 pairs).
+template <uint8_t E, bool ADD>
+__device__ __forceinline__ void f8_mul_const_planes(const uint64_t y[8], uint64_t acc[8]) {
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    uint64_t s = ADD ? acc[j] : 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      if ((f8_mul_c(E, (uint8_t)(1u << k)) >> j) & 1) s ^= y[k];
+    acc[j] = s;
+  }
+}
+
 // 8x8 bit-matrix transpose: bit 8r + c <-> bit 8c + r.
 __device__ __forceinline__ uint64_t transpose8x8(uint64_t x) {
   uint64_t t;
@@ -219,27 +250,37 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
         }
         uint64_t y[8];
         f8_mul_planes(ea, eb, y);
-        // w += e8[xs] * y (constant multiply as an 8x8 plane matrix);
-        // t[xs & 1] += e8c[xs >> 1] * c_s (c_s in {0,1}: plane j takes c where
-        // bit j of the constant is set).
-        const uint8_t* mm = T->e8_mat[xs];
+        // w += e8[xs] * y with e8[xs] = f0(par) f1(xs2) f2(h): the row factor
+        // f0 f1 is one of four compile-time constants (xs2 and par are the
+        // same in every lane, so the switch does not diverge); f2(h) is
+        // applied once per block below. t[xs & 1] += e8c[xs >> 1] * c_s
+        // (c_s in {0,1}: plane j takes c where bit j of the constant is set).
+        switch (2 * xs2 + par) {
+          case 0: f8_mul_const_planes<f8_mul_c(f8_eq_factor(0, 0), f8_eq_factor(1, 0)), true>(y, w); break;
+          case 1: f8_mul_const_planes<f8_mul_c(f8_eq_factor(0, 1), f8_eq_factor(1, 0)), true>(y, w); break;
+          case 2: f8_mul_const_planes<f8_mul_c(f8_eq_factor(0, 0), f8_eq_factor(1, 1)), true>(y, w); break;
+          default: f8_mul_const_planes<f8_mul_c(f8_eq_factor(0, 1), f8_eq_factor(1, 1)), true>(y, w); break;
+        }
         const uint8_t e8c = T->e8c[xs >> 1];
         // c goes to the parity-par half of t; with the parity a runtime value
         // (one loop body for both parities) the halves take rc or 0
         const uint64_t c_even = par ? 0 : rc, c_odd = par ? rc : 0;
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-          uint64_t acc = 0;
-#pragma unroll
-          for (int k = 0; k < 8; k++)
-            if ((mm[j] >> k) & 1) acc ^= y[k];
-          w[j] ^= acc;
+        for (int j = 0; j < 8; j++)
           if ((e8c >> j) & 1) {
             t[j] ^= c_even;
             t[8 + j] ^= c_odd;
           }
-        }
       }
+    // the rows' common factor f2(h) (h differs between the half-warps: both
+    // compile-time products, then a select)
+    {
+      uint64_t w0[8], w1[8];
+      f8_mul_const_planes<f8_eq_factor(2, 0), false>(w, w0);
+      f8_mul_const_planes<f8_eq_factor(2, 1), false>(w, w1);
+#pragma unroll
+      for (int j = 0; j < 8; j++) w[j] = h ? w1[j] : w0[j];
+    }
     // the two halves' row sums of producer group xm: add them
 #pragma unroll
     for (int j = 0; j < 8; j++) w[j] ^= shfl_xor64(w[j], 16);

@@ -154,3 +154,25 @@ def test_gf_tab_row_direct_values():
                     acc = (acc[0] ^ B[4 + b][0], acc[1] ^ B[4 + b][1])
             want = O.gf_mul(t, O.gf_mul((v, 0), xpow(8 * k)))
             assert acc == want, (k, v)
+
+
+def test_zc_round1_eq_weight_factors():
+    # round 1 multiplies each row by f0(par) f1(xs2) (compile-time constants)
+    # and the block's sum by f2(h): e8(xs) = prod_v (bit v of xs ? C_v : 1 + C_v)
+    # with xs = 4 h + 2 xs2 + par, C = (0xF7, 0x53, 0xB5)
+    import oracle_lib as O
+    mul = O.lib().oracle_gf8_mul
+    C = (0xF7, 0x53, 0xB5)
+
+    def f(v, bit):
+        return C[v] if bit else 1 ^ C[v]
+
+    for xs in range(8):
+        e = 1
+        for v in range(3):
+            e = mul(e, f(v, (xs >> v) & 1))
+        par, xs2, h = xs & 1, (xs >> 1) & 1, xs >> 2
+        assert mul(mul(f(0, par), f(1, xs2)), f(2, h)) == e
+        # and multiplying planes by a constant is linear: (a + b) E = a E + b E
+        for y in (1, 0x53, 0xFF):
+            assert mul(y, e) == mul(mul(y, mul(f(0, par), f(1, xs2))), f(2, h))
