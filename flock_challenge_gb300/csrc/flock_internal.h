@@ -28,6 +28,15 @@ int flock_launch_zc_round1(const void* a, const void* b, const void* c, size_t n
                            const ZcRound1Tables* d_tables, void* partials, int grid, cudaStream_t st);
 int flock_launch_reduce_rows(const void* in, size_t count, int width, void* out, cudaStream_t st);
 int flock_launch_eq_split(const void* r, int lo_bits, int hi_bits, void* lo, void* hi, cudaStream_t st);
+// Several eq table pairs in one launch (device array of jobs; lo_bits and
+// hi_bits each at most 28; max_entries = the largest 2^lo_bits + 2^hi_bits).
+struct FlockEqJob {
+  const void* r;
+  void* lo;
+  void* hi;
+  int lo_bits, hi_bits;
+};
+int flock_launch_eq_split_multi(const FlockEqJob* d_jobs, int n_jobs, size_t max_entries, cudaStream_t st);
 int flock_launch_zc_round(const void* A, const void* B, size_t n_pairs, int bind, const uint64_t rho[2], void* Aout,
                           void* Bout, const void* eq_lo, const void* eq_hi, int lo_bits, void* partials, int grid,
                           cudaStream_t st);

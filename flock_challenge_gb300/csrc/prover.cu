@@ -282,7 +282,7 @@ struct ProverState {
   ZcRound1Tables* d_r1t = nullptr;
   DBuf in, z, a, b, stripe, cw, tree, A0, B0, A1, B1, eqlo, eqhi, eqout, rdev, part, red, lag, small, eqin, comb,
       zvec, zvec0, tlo0, thi0, tlo1, thi1, tables, bc, f1, b1, W, LO, HI, basis, qbuf, abuf, rows, nidx, nodes,
-      grind, lvl_cw[2], lvl_tree[2], chW, chG, eqlo2, eqhi2;
+      grind, lvl_cw[2], lvl_tree[2], chW, chG, zceq, zcr, zcjobs;
   DBuf csc_ap, csc_ai, csc_bp, csc_bi;
   bool csc_ready = false;
   FlockPhaseTimes times;
@@ -300,7 +300,7 @@ struct ProverState {
     return {&in, &z, &a, &b, &stripe, &cw, &tree, &A0, &B0, &A1, &B1, &eqlo, &eqhi, &eqout, &rdev, &part, &red,
             &lag, &small, &eqin, &comb, &zvec, &zvec0, &tlo0, &thi0, &tlo1, &thi1, &tables, &bc, &f1, &b1,
             &W, &LO, &HI, &basis, &qbuf, &abuf, &rows, &nidx, &nodes, &grind, &lvl_cw[0], &lvl_cw[1],
-            &lvl_tree[0], &lvl_tree[1], &chW, &chG, &eqlo2, &eqhi2, &csc_ap, &csc_ai, &csc_bp, &csc_bi};
+            &lvl_tree[0], &lvl_tree[1], &chW, &chG, &zceq, &zcr, &zcjobs, &csc_ap, &csc_ai, &csc_bp, &csc_bi};
   }
   std::vector<const DBuf*> bufs() const {
     auto v = const_cast<ProverState*>(this)->bufs();
@@ -629,16 +629,16 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     void *curA = dA0, *curB = dB0, *nxtA = dA1, *nxtB = dB1;
     // r[9..12] = g / (1 + g), g = x^(2^(k-9)): eq(r_k, b) = (1 + r_k) x^(b 2^(k-9))
     auto shift_var = [&](int k) { return (F::one() + r[k]) * F(1ULL << (1 << (k - 9)), 0) == r[k]; };
-    // Per-round eq layout. The tables depend on r only, so round i + 1's are
-    // launched right after round i's kernel and build while the host waits
-    // for round i's message (two buffer pairs, alternating).
+    // Per-round eq layout. The tables depend on r only, so all rounds' tables
+    // are built by one launch before the first round (no eq work between a
+    // round's kernel and the host's read of its message).
     struct RoundEq {
       bool grp;
       int a_bits, m_bits, f0, lob;
       F dinv;
+      std::vector<F> vars;  // the variables of the split tables
     };
-    DBuf* eqbuf[2][2] = {{&S->eqlo, &S->eqhi}, {&S->eqlo2, &S->eqhi2}};
-    auto round_eq = [&](int i, bool launch) {
+    auto round_eq = [&](int i) {
       std::vector<F> rr(r.begin() + 6 + i + 1, r.end());
       const int nv = (int)rr.size();
       // lowest variables of rr that are fixed challenges: phi8 ones (r7, r8)
@@ -655,19 +655,47 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
         std::vector<F> rg(rr.begin(), rr.begin() + q.a_bits);
         rg.insert(rg.end(), rr.begin() + q.a_bits + q.m_bits, rr.end());
         q.lob = std::min(nv - q.m_bits, 8);
-        if (launch) eq_split_dev(*S, rg, q.lob, *eqbuf[i & 1][0], *eqbuf[i & 1][1]);
+        q.vars = std::move(rg);
       } else {
         q.lob = std::min(nv, 12);
-        if (launch) eq_split_dev(*S, rr, q.lob, *eqbuf[i & 1][0], *eqbuf[i & 1][1]);
+        q.vars = std::move(rr);
       }
       return q;
     };
-    RoundEq qn = round_eq(0, true);
+    std::vector<RoundEq> qs;
+    std::vector<std::pair<size_t, size_t>> eq_off;  // (lo, hi) F128 offsets in zceq
+    {
+      std::vector<F> vars;
+      std::vector<size_t> var_off;
+      size_t tot = 0, max_entries = 0;
+      for (int i = 0; i < n_mlv; i++) {
+        qs.push_back(round_eq(i));
+        const RoundEq& q = qs.back();
+        const int hb = (int)q.vars.size() - q.lob;
+        if (q.lob > 28 || hb > 28) throw Fail(FLOCK_ERR_SHAPE, "eq split");
+        var_off.push_back(vars.size());
+        vars.insert(vars.end(), q.vars.begin(), q.vars.end());
+        eq_off.push_back({tot, tot + ((size_t)1 << q.lob)});
+        tot += ((size_t)1 << q.lob) + ((size_t)1 << hb);
+        max_entries = std::max(max_entries, ((size_t)1 << q.lob) + ((size_t)1 << hb));
+      }
+      F* dvars = (F*)S->zcr.get(vars.size() * 16 + 16);
+      h2d(*S, dvars, vars.data(), vars.size() * 16);
+      F* deq = (F*)S->zceq.get(tot * 16);
+      std::vector<FlockEqJob> jobs(n_mlv);
+      for (int i = 0; i < n_mlv; i++)
+        jobs[i] = {dvars + var_off[i], deq + eq_off[i].first, deq + eq_off[i].second, qs[i].lob,
+                   (int)qs[i].vars.size() - qs[i].lob};
+      auto* djobs = (FlockEqJob*)S->zcjobs.get(jobs.size() * sizeof(FlockEqJob));
+      h2d(*S, djobs, jobs.data(), jobs.size() * sizeof(FlockEqJob));
+      FK(flock_launch_eq_split_multi(djobs, n_mlv, max_entries, st));
+    }
     for (int i = 0; i < n_mlv; i++) {
       const size_t n_pairs = rows0 >> (i + 1);  // pairs of the round-i table
-      const RoundEq q = qn;
-      const void* elo = eqbuf[i & 1][0]->p;
-      const void* ehi = eqbuf[i & 1][1]->p;
+      const RoundEq& q = qs[i];
+      const F* deq = (const F*)S->zceq.p;
+      const void* elo = deq + eq_off[i].first;
+      const void* ehi = deq + eq_off[i].second;
       uint64_t rp[2] = {0, 0};
       if (i > 0) u2(rho.back(), rp);
       int grid;
@@ -686,7 +714,6 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
         else
           FK(flock_launch_zc_round(curA, curB, n_pairs, 1, rp, nxtA, nxtB, elo, ehi, q.lob, dpart, grid, st));
       }
-      if (i + 1 < n_mlv) qn = round_eq(i + 1, true);
       auto g = reduce_partials(*S, dpart, grid, 2);
       g[0] = g[0] * q.dinv;
       g[1] = g[1] * q.dinv;
@@ -772,14 +799,8 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       d2h(*S, z_partial.data(), dzv, 64 * 16);
     }
     tr.observe_slice(z_partial.data(), 64);
-    F r_inner_skip = tr.sample();
-    F lc_w;
-    {
-      auto l2 = LG.at(r_inner_skip, 0);
-      lc_w = dot(l2.data(), z_partial.data(), 64);
-    }
+    tr.sample();  // lincheck's skip challenge: only the verifier evaluates the claim at it
     std::vector<F> r_inner_rest(lc_rr.rbegin(), lc_rr.rend());
-    (void)lc_w;
     T.lincheck_ms = clk.lap();
     w.pv(lc_rounds);
     w.fv(z_partial);

@@ -391,9 +391,10 @@ reduce_rows_kernel(const gf128* __restrict__ in, size_t count, int width, gf128*
 // 4 x 128 entries per set), so an entry costs (chunks - 1) products instead
 // of one per variable.
 constexpr int EQ_CHUNK = 7, EQ_MAX_CHUNKS = 4;
-__global__ void __launch_bounds__(256)
-eq_split_kernel(const gf128* __restrict__ r, int lo_bits, int hi_bits, gf128* __restrict__ lo,
-                gf128* __restrict__ hi) {
+// One table pair, CTA `blk` of `nblk` (the calling kernel's grid slice).
+__device__ __forceinline__ void eq_split_body(const gf128* __restrict__ r, int lo_bits, int hi_bits,
+                                              gf128* __restrict__ lo, gf128* __restrict__ hi, size_t blk,
+                                              size_t nblk) {
   __shared__ gf128 t[2][EQ_MAX_CHUNKS][1 << EQ_CHUNK];
   for (int e = threadIdx.x; e < 2 * EQ_MAX_CHUNKS * (1 << EQ_CHUNK); e += blockDim.x) {
     const int set = e / (EQ_MAX_CHUNKS << EQ_CHUNK), c = (e >> EQ_CHUNK) % EQ_MAX_CHUNKS, v = e & ((1 << EQ_CHUNK) - 1);
@@ -411,7 +412,7 @@ eq_split_kernel(const gf128* __restrict__ r, int lo_bits, int hi_bits, gf128* __
   }
   __syncthreads();
   const size_t nlo = (size_t)1 << lo_bits, nhi = (size_t)1 << hi_bits;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < nlo + nhi; e += (size_t)gridDim.x * blockDim.x) {
+  for (size_t e = blk * blockDim.x + threadIdx.x; e < nlo + nhi; e += nblk * blockDim.x) {
     const bool is_lo = e < nlo;
     const size_t idx = is_lo ? e : e - nlo;
     const int set = is_lo ? 0 : 1, nb = is_lo ? lo_bits : hi_bits;
@@ -424,6 +425,20 @@ eq_split_kernel(const gf128* __restrict__ r, int lo_bits, int hi_bits, gf128* __
     if (is_lo) lo[idx] = acc;
     else hi[idx] = acc;
   }
+}
+
+__global__ void __launch_bounds__(256)
+eq_split_kernel(const gf128* __restrict__ r, int lo_bits, int hi_bits, gf128* __restrict__ lo,
+                gf128* __restrict__ hi) {
+  eq_split_body(r, lo_bits, hi_bits, lo, hi, blockIdx.x, gridDim.x);
+}
+
+// Many table pairs in one launch: job blockIdx.y, its tables split over the
+// x dimension.
+__global__ void __launch_bounds__(256)
+eq_split_multi_kernel(const FlockEqJob* __restrict__ jobs) {
+  const FlockEqJob j = jobs[blockIdx.y];
+  eq_split_body((const gf128*)j.r, j.lo_bits, j.hi_bits, (gf128*)j.lo, (gf128*)j.hi, blockIdx.x, gridDim.x);
 }
 
 // One multilinear round (zerocheck.rs:690-760, multilinear.rs:632-675), with
@@ -716,6 +731,16 @@ int flock_launch_zc_round1(const void* a, const void* b, const void* c, size_t n
 
 int flock_launch_reduce_rows(const void* in, size_t count, int width, void* out, cudaStream_t st) {
   reduce_rows_kernel<<<(width + 7) / 8, 256, 0, st>>>((const gf128*)in, count, width, (gf128*)out); flock_count_launch();
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_launch_eq_split_multi(const FlockEqJob* d_jobs, int n_jobs, size_t max_entries, cudaStream_t st) {
+  if (n_jobs <= 0) return FLOCK_OK;
+  if (n_jobs > 65535) return FLOCK_ERR_SHAPE;
+  size_t gx = (max_entries + 2047) / 2048;  // >= 8 entries per thread, as in flock_launch_eq_split
+  if (gx < 1) gx = 1;
+  if (gx > 152) gx = 152;
+  eq_split_multi_kernel<<<dim3((unsigned)gx, (unsigned)n_jobs), 256, 0, st>>>(d_jobs); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
