@@ -366,17 +366,19 @@ Open open_rows(ProverState& S, const void* cw, const void* tree, size_t block_le
   h2d(S, dq, q.data(), q.size() * 4);
   void* dr = S.rows.get(q.size() * width * 16);
   FK(flock_launch_gather_rows(cw, dq, (int)q.size(), width, dr, S.st));
-  o.rows.resize(q.size() * width);
-  d2h(S, o.rows.data(), dr, o.rows.size() * 16);
+  // both gathers are queued before the first read: one wait for the two
   auto idx = multiproof_nodes(block_len, q);
-  o.nodes.resize(idx.size() * 32);
+  void* dn = nullptr;
   if (!idx.empty()) {
     uint32_t* di = (uint32_t*)S.nidx.get(idx.size() * 4);
     h2d(S, di, idx.data(), idx.size() * 4);
-    void* dn = S.nodes.get(idx.size() * 32);
+    dn = S.nodes.get(idx.size() * 32);
     FK(flock_launch_gather_nodes(tree, di, (int)idx.size(), dn, S.st));
-    d2h(S, o.nodes.data(), dn, o.nodes.size());
   }
+  o.rows.resize(q.size() * width);
+  d2h(S, o.rows.data(), dr, o.rows.size() * 16);
+  o.nodes.resize(idx.size() * 32);
+  if (dn) d2h(S, o.nodes.data(), dn, o.nodes.size());
   return o;
 }
 
