@@ -144,6 +144,40 @@ __device__ __forceinline__ void acc_shift_xor_v(Acc5& a, const uint4 v, uint32_t
   a.w[4] ^= __funnelshift_l(v.w, 0u, sh);
 }
 
+// 288-bit accumulator of shifted unreduced products (a 256-bit carry-less
+// product shifted by < 16 bits): the reduction is paid once per sum.
+struct Acc9 {
+  uint32_t w[9];
+};
+
+__device__ __forceinline__ void acc9_shift_xor(Acc9& a, const gf256& v, uint32_t sh) {
+  uint32_t u[8];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    u[2 * k] = (uint32_t)v.r[k];
+    u[2 * k + 1] = (uint32_t)(v.r[k] >> 32);
+  }
+  a.w[0] ^= u[0] << sh;
+#pragma unroll
+  for (int k = 1; k < 8; k++) a.w[k] ^= __funnelshift_l(u[k - 1], u[k], sh);
+  a.w[8] ^= __funnelshift_l(u[7], 0u, sh);
+}
+
+// a mod x^128 + x^7 + x^2 + x + 1 for a below 2^272: the high part H (bits
+// 128 and up, below 2^144) folds in as H (1 + x + x^2 + x^7), whose bits
+// above 127 (fewer than 23) fold in once more.
+__device__ __forceinline__ gf128 acc9_reduce(const Acc9& a) {
+  const uint64_t l0 = a.w[0] | ((uint64_t)a.w[1] << 32), l1 = a.w[2] | ((uint64_t)a.w[3] << 32);
+  const uint64_t h0 = a.w[4] | ((uint64_t)a.w[5] << 32), h1 = a.w[6] | ((uint64_t)a.w[7] << 32), h2 = a.w[8];
+  const uint64_t t0 = h0 ^ (h0 << 1) ^ (h0 << 2) ^ (h0 << 7);
+  const uint64_t t1 = h1 ^ ((h1 << 1) | (h0 >> 63)) ^ ((h1 << 2) | (h0 >> 62)) ^ ((h1 << 7) | (h0 >> 57));
+  const uint64_t t2 = h2 ^ ((h2 << 1) | (h1 >> 63)) ^ ((h2 << 2) | (h1 >> 62)) ^ ((h2 << 7) | (h1 >> 57));
+  const uint64_t lo = l0 ^ t0 ^ t2 ^ (t2 << 1) ^ (t2 << 2) ^ (t2 << 7), hi = l1 ^ t1;
+  gf128 r;
+  r.w[0] = (uint32_t)lo; r.w[1] = (uint32_t)(lo >> 32); r.w[2] = (uint32_t)hi; r.w[3] = (uint32_t)(hi >> 32);
+  return r;
+}
+
 __device__ __forceinline__ uint64_t shfl_xor64(uint64_t v, int m) {
   const uint32_t lo = __shfl_xor_sync(0xffffffffu, (uint32_t)v, m);
   const uint32_t hi = __shfl_xor_sync(0xffffffffu, (uint32_t)(v >> 32), m);
@@ -666,9 +700,9 @@ zc_round_grp_kernel(const void* __restrict__ in0, const void* __restrict__ in1, 
     const size_t base = h * per_h;
     for (size_t it = threadIdx.x; it < items; it += RND_THREADS) {
       const size_t j0 = base + ((it >> a_bits) << s) + (it & amask);
-      Acc5 t1, ti;
+      Acc9 t1, ti;
 #pragma unroll
-      for (int k = 0; k < 5; k++) { t1.w[k] = 0; ti.w[k] = 0; }
+      for (int k = 0; k < 9; k++) { t1.w[k] = 0; ti.w[k] = 0; }
       for (int jm = 0; jm < (1 << m_bits); jm++) {
         const size_t j = j0 + ((size_t)jm << a_bits);
         gf128 a0, a1, b0, b1;
@@ -689,14 +723,13 @@ zc_round_grp_kernel(const void* __restrict__ in0, const void* __restrict__ in1, 
         }
         Aout[2 * j] = a0; Aout[2 * j + 1] = a1;
         Bout[2 * j] = b0; Bout[2 * j + 1] = b1;
-        const gf128 p1 = gf_mul(a1, b1), pi = gf_mul(gf_add(a0, a1), gf_add(b0, b1));
         const uint32_t sh = (uint32_t)(jm * m_mul);
-        acc_shift_xor_v(t1, make_uint4(p1.w[0], p1.w[1], p1.w[2], p1.w[3]), sh);
-        acc_shift_xor_v(ti, make_uint4(pi.w[0], pi.w[1], pi.w[2], pi.w[3]), sh);
+        acc9_shift_xor(t1, gf_mul_wide(a1, b1), sh);
+        acc9_shift_xor(ti, gf_mul_wide(gf_add(a0, a1), gf_add(b0, b1)), sh);
       }
       const gf128 e = eq_lo[it];
-      gf256_acc(l1, gf_mul_wide(e, acc_reduce(t1)));
-      gf256_acc(li, gf_mul_wide(e, acc_reduce(ti)));
+      gf256_acc(l1, gf_mul_wide(e, acc9_reduce(t1)));
+      gf256_acc(li, gf_mul_wide(e, acc9_reduce(ti)));
     }
     const gf128 eh = eq_hi[h];
     gf256_acc(g1, gf_mul_wide(eh, gf256_reduce(l1)));

@@ -176,3 +176,28 @@ def test_zc_round1_eq_weight_factors():
         # and multiplying planes by a constant is linear: (a + b) E = a E + b E
         for y in (1, 0x53, 0xFF):
             assert mul(y, e) == mul(mul(y, mul(f(0, par), f(1, xs2))), f(2, h))
+
+
+def test_acc9_reduce_formula():
+    # csrc/zerocheck.cu acc9_reduce: a < 2^272 folded as L + H (1 + x + x^2 + x^7),
+    # the bits of that above 127 folded once more; checked against long division
+    import random
+    M64 = (1 << 64) - 1
+    POLY = (1 << 128) | 0x87
+
+    def pmod(a):
+        while a.bit_length() > 128:
+            a ^= POLY << (a.bit_length() - 129)
+        return a
+
+    rng = random.Random(9)
+    for _ in range(300):
+        a = rng.getrandbits(255) << rng.randrange(16)  # a shifted 255-bit product
+        l0, l1 = a & M64, (a >> 64) & M64
+        h0, h1, h2 = (a >> 128) & M64, (a >> 192) & M64, a >> 256
+        t0 = (h0 ^ (h0 << 1) ^ (h0 << 2) ^ (h0 << 7)) & M64
+        t1 = (h1 ^ ((h1 << 1) | (h0 >> 63)) ^ ((h1 << 2) | (h0 >> 62)) ^ ((h1 << 7) | (h0 >> 57))) & M64
+        t2 = (h2 ^ ((h2 << 1) | (h1 >> 63)) ^ ((h2 << 2) | (h1 >> 62)) ^ ((h2 << 7) | (h1 >> 57))) & M64
+        lo = (l0 ^ t0 ^ t2 ^ (t2 << 1) ^ (t2 << 2) ^ (t2 << 7)) & M64
+        hi = l1 ^ t1
+        assert (hi << 64) | lo == pmod(a)
