@@ -308,7 +308,17 @@ constexpr int kMaxPassLayers = variant_max_layers(kDefaultVariant);
 // positions of one lane.
 constexpr int TAB_THREADS = 512;
 constexpr int TAB_ENTRIES = GF_TAB_ENTRIES;
-constexpr size_t TAB_SMEM = (size_t)3 * TAB_ENTRIES * 16;
+// three byte tables, then a prefetch slot of one quad (4 x 16 B) per thread
+constexpr size_t TAB_SMEM = (size_t)3 * TAB_ENTRIES * 16 + (size_t)4 * TAB_THREADS * 16;
+static_assert(TAB_SMEM <= 232448, "table pass shared memory above the 227 KB per-block limit");
+
+// 16-byte asynchronous global -> shared copy (cp.async, L2 only).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" :: "r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // Byte tables of the three twiddles t[0..2] into T (3 x TAB_ENTRIES slots),
 // one row (256 per table) per item, computed directly (gf_tab_row_direct):
@@ -326,7 +336,7 @@ __device__ void build_tabs3(const gf128 t[3], uint4* __restrict__ T) {
 __global__ void __launch_bounds__(TAB_THREADS, 1)
 ntt_tab2_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t src_pos_mask,
                 const gf128* __restrict__ tw, int log_d, int log_lanes, int l, int cph) {
-  extern __shared__ uint4 tabs[];  // [3][TAB_ENTRIES]
+  extern __shared__ uint4 tabs[];  // [3][TAB_ENTRIES], then the prefetch slots [4][TAB_THREADS]
   const size_t hi = blockIdx.x / cph;
   const int part = blockIdx.x % cph;
   const gf128 t3[3] = {tw[((size_t)1 << l) - 1 + hi], tw[((size_t)1 << (l + 1)) - 1 + 2 * hi],
@@ -339,13 +349,36 @@ ntt_tab2_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t s
   const size_t nl = (size_t)1 << log_lanes;
   const size_t items = ((size_t)1 << lo_bits) << log_lanes;
   const uint32_t rot = threadIdx.x & 15;
-  for (size_t it = (size_t)part * TAB_THREADS + threadIdx.x; it < items; it += (size_t)cph * TAB_THREADS) {
-    const size_t lane = it & (nl - 1), lo = it >> log_lanes;
-    const size_t p0 = (hi << (lo_bits + 2)) | lo;
-    gf128 y[4];
+  // The next quad is fetched into this thread's slot (cp.async) while the
+  // current one is computed: with three 64 KiB tables an SM holds 16 warps,
+  // too few to hide the global-load latency otherwise. Each quad is read and
+  // written by one thread only, so the prefetch is safe in place (dst == src).
+  // The slot's reads for the current quad are issued before the copies into
+  // it (the asm's memory clobber keeps that order), and a copy writes the
+  // slot only when its global read returns.
+  uint4* slot = tabs + 3 * TAB_ENTRIES + threadIdx.x;  // entry b at slot[b * TAB_THREADS]
+  auto prefetch = [&](size_t it2) {
+    const size_t lane2 = it2 & (nl - 1), lo2 = it2 >> log_lanes;
+    const size_t q0 = (hi << (lo_bits + 2)) | lo2;
 #pragma unroll
     for (int b = 0; b < 4; b++)
-      y[b] = gf_load(&src[((p0 | ((size_t)b << lo_bits)) & src_pos_mask) * nl + lane]);
+      cp_async16(slot + b * TAB_THREADS, &src[((q0 | ((size_t)b << lo_bits)) & src_pos_mask) * nl + lane2]);
+    cp_async_commit();
+  };
+  const size_t stride = (size_t)cph * TAB_THREADS;
+  size_t it = (size_t)part * TAB_THREADS + threadIdx.x;
+  if (it < items) prefetch(it);
+  for (; it < items; it += stride) {
+    const size_t lane = it & (nl - 1), lo = it >> log_lanes;
+    const size_t p0 = (hi << (lo_bits + 2)) | lo;
+    cp_async_wait_all();
+    gf128 y[4];
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      const uint4 v = slot[b * TAB_THREADS];
+      y[b] = gf128{{v.x, v.y, v.z, v.w}};
+    }
+    if (it + stride < items) prefetch(it + stride);
     // layer l: pairs (b, b + 2) with t_A
     if (!za) {
       y[0] = gf_add(y[0], gf_mul_tab(tabs, y[2], rot));
