@@ -29,6 +29,7 @@
 #include "flock_internal.h"
 #include "gf128.cuh"
 #include "gf_tab.cuh"
+#include "cp_async.cuh"
 #include "host_field.h"
 
 namespace {
@@ -312,13 +313,6 @@ constexpr int TAB_ENTRIES = GF_TAB_ENTRIES;
 constexpr size_t TAB_SMEM = (size_t)3 * TAB_ENTRIES * 16 + (size_t)4 * TAB_THREADS * 16;
 static_assert(TAB_SMEM <= 232448, "table pass shared memory above the 227 KB per-block limit");
 
-// 16-byte asynchronous global -> shared copy (cp.async, L2 only).
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" :: "r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // Byte tables of the three twiddles t[0..2] into T (3 x TAB_ENTRIES slots),
 // one row (256 per table) per item, computed directly (gf_tab_row_direct):

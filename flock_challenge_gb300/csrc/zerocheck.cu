@@ -664,7 +664,9 @@ zc_round_grp_kernel(const void* __restrict__ in0, const void* __restrict__ in1, 
   // SKIP: [256 v][8 c] subset sums of the Lagrange weights of byte position c;
   // entry (v, c) sits in bank group c and lane l starts at byte position l mod
   // 8, so eight consecutive lanes read eight distinct bank groups.
-  // Otherwise: rho's byte tables, then their nibble tables.
+  // Otherwise: rho's byte tables (a prefetch slot per thread for the next
+  // pair, as in the NTT table passes, measured slower here: these rounds are
+  // ALU-bound).
   extern __shared__ gf128 tab[];
   uint4* rtab = reinterpret_cast<uint4*>(tab);
   const uint32_t rot = threadIdx.x & 15;
