@@ -129,3 +129,26 @@ def test_ntt_every_pass_shape_matches_oracle(ctx, monkeypatch, variant, log_d, l
     d = to_dev(data)
     F.ntt(ctx, d, log_d, log_lanes, start)
     assert np.array_equal(host(d).view(np.uint64), O.ntt_interleaved(data, 1 << log_lanes, start))
+
+
+def test_rate_quarter_256_columns_2e16_rows(ctx):
+    """The kernel-microbench shape at its smallest stated size, 2^16 rows x 256
+    columns (rate 1/4: 2^18 codeword positions, 1 GiB): columns are independent
+    transforms, so three of them are checked against the oracle's one-column
+    commit; the whole tree (4 KiB leaves) against the oracle's Merkle tree of
+    the device codeword."""
+    rows_log, cols_log = 16, 8
+    m = 7 + cols_log + rows_log
+    rng = np.random.default_rng(2016)
+    z = rng.integers(0, 2**63, (1 << (m - 7)) * 2, dtype=np.uint64)
+    z |= rng.integers(0, 2, z.shape, dtype=np.uint64) << np.uint64(63)
+    root, cw, tree = F.commit(ctx, to_dev(z), m, log_inv_rate=2, log_batch_size=cols_log)
+    cwb = host(cw)
+    cwh = cwb.view(np.uint64).reshape(1 << (rows_log + 2), 1 << cols_log, 2)
+    zc = z.reshape(1 << rows_log, 1 << cols_log, 2)
+    for c in (0, 77, 255):
+        _, ocw, _ = O.commit(np.ascontiguousarray(zc[:, c, :]).reshape(-1), 7 + rows_log, 2, 0, want_codeword=True)
+        assert np.array_equal(np.ascontiguousarray(cwh[:, c, :]).reshape(-1), ocw), c
+    otree = O.merkle_tree(cwb, 1 << (rows_log + 2))
+    assert np.array_equal(host(tree).reshape(-1, 32), otree)
+    assert root == otree[-1].tobytes()
