@@ -189,6 +189,63 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def kernel_microbench(F, ctx_handle, peaks, torch, dev, rows_logs=(16, 18, 20), reps=3):
+    """The kernel microbench shape (no protocol): rows x 256 columns of uniform
+    F128, rate 1/4 (two replica layers, then the NTT), BLAKE3 Merkle over 4 KiB
+    leaves. flock_commit (NTT + tree) and flock_merkle_tree are timed alone with
+    CUDA events on their stream; the NTT time is their difference."""
+    out = []
+    s = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(s.cuda_stream)
+    for rl in rows_logs:
+        cols_log, rate = 8, 2
+        m = 7 + cols_log + rl
+        log_d = rl + rate
+        z = torch.randint(-2**62, 2**62, ((1 << (rl + cols_log)) * 2,), dtype=torch.int64, device=dev).view(torch.uint8)
+        cw = torch.empty((1 << (log_d + cols_log)) * 16, dtype=torch.uint8, device=dev)
+        tree = torch.empty((2 * (1 << log_d) - 1) * 32, dtype=torch.uint8, device=dev)
+        root = (ctypes.c_uint8 * 32)()
+        lib = F.lib()
+
+        def commit():
+            F.check(lib.flock_commit(ctx_handle, F._dptr(z), m, rate, cols_log, F._dptr(cw), F._dptr(tree), root, sp),
+                    "flock_commit")
+
+        def merkle():
+            F.check(lib.flock_merkle_tree(F._dptr(cw), 1 << log_d, 16 << cols_log, F._dptr(tree), sp),
+                    "flock_merkle_tree")
+
+        def timed(fn):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(s):
+                fn()
+                fn()
+                e0.record(s)
+                for _ in range(reps):
+                    fn()
+                e1.record(s)
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / reps
+
+        c_ms, m_ms = timed(commit), timed(merkle)
+        ntt_ms = max(c_ms - m_ms, 1e-6)
+        elems = (1 << (rl + cols_log))
+        alg = 16 * elems * (1 + (1 << rate))  # read the message once, write the codeword once
+        muls = (log_d - rate) * (1 << (log_d - 1)) * (1 << cols_log)
+        leaves = 1 << log_d
+        comp = leaves * ((16 << cols_log) // 64 + (16 << cols_log) // 1024 - 1) + leaves - 1
+        out.append({"rows": 1 << rl, "columns": 1 << cols_log, "rate": "1/4", "leaf_bytes": 16 << cols_log,
+                    "commit_ms": c_ms, "merkle_ms": m_ms, "ntt_ms": ntt_ms,
+                    "ntt_gbs": alg / (ntt_ms * 1e-3) / 1e9, "ntt_frac_of_hbm": alg / (ntt_ms * 1e-3) / 1e9 / peaks["hbm_gbs"],
+                    "ntt_gf128_muls_per_s": muls / (ntt_ms * 1e-3),
+                    "merkle_gbs": (16 * elems * (1 << rate)) / (m_ms * 1e-3) / 1e9,
+                    "merkle_compressions_per_s": comp / (m_ms * 1e-3)})
+        del z, cw, tree
+        torch.cuda.empty_cache()
+    return out
+
+
 def kernel_roofline(F, ctx_handle, stream_ptr, log2, peaks, torch, dev, clock_mhz=None):
     """Times the dominant kernel family (the L0 commit NTT) alone with CUDA events."""
     m = 14 + log2
@@ -387,6 +444,7 @@ def run_gpu(args):
         }
         if ws == 1:
             line["chain"] = run_chain(F, setup, log2)
+            line["kernel_microbench"] = kernel_microbench(F, setup.ctx.handle, peaks, torch, dev)
         line["cpu_baseline"] = oracle_baseline(budget_s=20.0, gpu_proof=first, gpu_m=14 + log2)
         if args.forms and ws == 1:
             from flock_challenge_gb300 import forms
