@@ -50,15 +50,15 @@ PUBLISHED = 483866.0  # README.md:110-116, unmodified reference, Apple M4 Pro ru
 # launch set, from ncu on a 2^18-position case scaled by positions (traffic
 # grows in proportion): profiles/ntt_pass_l0_2e16.md.
 # DRAM bytes (read + write) per NTT pass at the bench's shape (2^20 positions x
-# 64 lanes): 479.2 MB per pass measured by ncu at 2^18 positions (mean of the
+# 64 lanes): 478.8 MB per pass measured by ncu at 2^18 positions (mean of the
 # eight L0 passes in profiles/ntt_instructions_2e18pos.md), times 4 for 4x the
 # positions.
-NTT_TRAFFIC_PER_PASS = {20: 4 * 479.2e6}
+NTT_TRAFFIC_PER_PASS = {20: 4 * 478.8e6}
 NTT_MAX_LAYERS = {0: 4, 1: 6, 2: 8}  # layers per pass of the autotuner's pass shapes
 # Thread instructions per GF(2^128) product in the table passes and per
 # butterfly in the multiply passes, measured by ncu on the 2^18-position L0
 # transform (profiles/ntt_instructions_2e18pos.md).
-NTT_INSTR_PER_TABLE_PRODUCT = 168
+NTT_INSTR_PER_TABLE_PRODUCT = 179
 NTT_INSTR_PER_MULTIPLY_BUTTERFLY = 433
 
 
