@@ -659,7 +659,11 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
         q.lob = std::min(nv - q.m_bits, 8);
         q.vars = std::move(rg);
       } else {
-        q.lob = std::min(nv, 12);
+        // a CTA takes whole rows of 2^lob pairs: rows of 2^(nv - 10) pairs,
+        // at least 2^8 (one pair per thread) and at most 2^12, keep the grid
+        // near 608 CTAs while the round has pairs for it (rows of 2^12 left
+        // rounds 7..13 on 1..64 CTAs, ~90 us each)
+        q.lob = std::min(nv, std::max(8, std::min(12, nv - 10)));
         q.vars = std::move(rr);
       }
       return q;
