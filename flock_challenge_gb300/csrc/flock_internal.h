@@ -50,7 +50,8 @@ int flock_launch_lc_comb(const uint32_t* a_ptr, const uint32_t* a_idx, const uin
                          int pin, void* comb, cudaStream_t st);
 int flock_launch_lc_quirky_eq(const void* lag, const void* x_rest, int n_rest, void* out, cudaStream_t st);
 
-int flock_launch_shv_from_zvec(const void* zvec, const void* eq_tail, void* out, cudaStream_t st);
+// scratch: 32 x 128 F128 of partial sums
+int flock_launch_shv_from_zvec(const void* zvec, const void* eq_tail, void* scratch, void* out, cudaStream_t st);
 int flock_launch_combined_basis(size_t n, const void* t0_lo, const void* t0_hi, const void* t1_lo,
                                 const void* t1_hi, int lo_bits, const void* tables, void* b, cudaStream_t st);
 
@@ -64,8 +65,10 @@ int flock_launch_glue_eq(void* b, size_t n, const void* lo, const void* hi, int 
 int flock_launch_glue(void* b, const void* add, size_t n, const uint64_t beta[2], cudaStream_t st);
 // LO holds nq << flock_induce_basis_lo_bits(n) entries, HI nq << (n - that).
 int flock_induce_basis_lo_bits(int n);
-int flock_launch_induce_basis(const uint32_t* d_queries, int nq, int n, const void* sks, const void* inv_sks,
-                              const void* alpha_w, void* W, void* LO, void* HI, void* basis, cudaStream_t st);
+// what_lin: [n][32] F128, What_k(x^b) (the normalized subspace polynomials on
+// the index bits; What_k(q) is their XOR over the set bits of q).
+int flock_launch_induce_basis(const uint32_t* d_queries, int nq, int n, const void* what_lin, const void* alpha_w,
+                              void* W, void* LO, void* HI, void* basis, cudaStream_t st);
 int flock_launch_gather_rows(const void* mat, const uint32_t* rows, int n_rows, int width, void* out,
                              cudaStream_t st);
 int flock_launch_gather_nodes(const void* tree, const uint32_t* idx, int n, void* out, cudaStream_t st);

@@ -111,18 +111,22 @@ __global__ void glue_kernel(gf128* __restrict__ b, const gf128* __restrict__ add
     b[j] = gf_add(b[j], gf_mul(beta, add[j]));
 }
 
-// What_k(q_i) for k < n (ligerito.rs:1776-1824): s_0 = q, s_k = s^2 + s_{k-1}(v_{k-1}) s,
-// normalized by 1 / s_k(v_k).
-__global__ void what_kernel(const uint32_t* __restrict__ queries, int nq, int n, const gf128* __restrict__ sks,
-                            const gf128* __restrict__ inv_sks, gf128* __restrict__ W) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nq) return;
-  gf128 s = gf_zero();
-  s.w[0] = queries[i];
-  for (int k = 0; k < n; k++) {
-    if (k > 0) s = gf_add(gf_mul(s, s), gf_mul(sks[k - 1], s));
-    W[(size_t)i * n + k] = gf_mul(s, inv_sks[k]);
-  }
+// What_k(q_i) for k < n (ligerito.rs:1776-1824: s_0 = q, s_k = s^2 + s_{k-1}(v_{k-1}) s,
+// normalized by 1 / s_k(v_k)). Each s_k is GF(2)-linear in its argument (a
+// square plus a constant multiple of a linear map), so What_k(q) is the XOR,
+// over the set bits b of the 32-bit index q, of lin[k][b] = What_k(x^b): one
+// thread per (query, k), no product.
+__global__ void what_kernel(const uint32_t* __restrict__ queries, int nq, int n, const gf128* __restrict__ lin,
+                            gf128* __restrict__ W) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)nq * n) return;
+  const int i = (int)(e / n), k = (int)(e % n);
+  const uint32_t q = queries[i];
+  const gf128* row = lin + (size_t)k * 32;
+  gf128 acc = gf_zero();
+  for (int b = 0; b < 32; b++)
+    if ((q >> b) & 1) acc = gf_add(acc, row[b]);
+  W[e] = acc;
 }
 
 // T[i][j] = scale_i * prod_{k < bits, bit k of j} W[i][k0 + k]; scale_i = alpha_i or 1.
@@ -269,10 +273,10 @@ constexpr int kBasisTabMinBits = 18;
 
 int flock_induce_basis_lo_bits(int n) { return n >= kBasisTabMinBits ? (n == kBasisTabMinBits ? 10 : 11) : (n + 1) / 2; }
 
-int flock_launch_induce_basis(const uint32_t* d_queries, int nq, int n, const void* sks, const void* inv_sks,
-                              const void* alpha_w, void* W, void* LO, void* HI, void* basis, cudaStream_t st) {
-  what_kernel<<<(nq + 127) / 128, 128, 0, st>>>(d_queries, nq, n, (const gf128*)sks, (const gf128*)inv_sks,
-                                                (gf128*)W); flock_count_launch();
+int flock_launch_induce_basis(const uint32_t* d_queries, int nq, int n, const void* what_lin, const void* alpha_w,
+                              void* W, void* LO, void* HI, void* basis, cudaStream_t st) {
+  what_kernel<<<(unsigned)(((size_t)nq * n + 127) / 128), 128, 0, st>>>(d_queries, nq, n, (const gf128*)what_lin,
+                                                                          (gf128*)W); flock_count_launch();
   const int lo_bits = flock_induce_basis_lo_bits(n), hi_bits = n - lo_bits;
   const bool tab = n >= kBasisTabMinBits;
   size_t nlo = (size_t)nq << lo_bits, nhi = (size_t)nq << hi_bits;

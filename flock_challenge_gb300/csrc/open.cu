@@ -89,30 +89,33 @@ combined_basis_kernel(int lo_bits, int slices, const gf128* __restrict__ lo0, co
 // s_hat_v of the ab claim from lincheck's pre-sumcheck z_vec (ring_switch.rs:1275-1325):
 // packed word pos = outer * 128 + (i >> 7), bit b = i & 127, so
 // s_hat_v[b] = sum_{h < 128} eq_tail[h] * z_vec[h * 128 + b].
-// One CTA of 512 threads: thread (q, b) sums h in [32 q, 32 q + 32), then
-// the four partial sums of each b are XORed in shared memory.
+// SHV_CTAS CTAs of 512 threads, CTA g taking h in [4 g, 4 g + 4): thread
+// (q, b) forms one product, the four of each b are XORed in shared memory
+// into row g of the partials, which a row reduction then folds (one CTA
+// forming all 16 K products took 58 us, latency-bound on one SM).
+constexpr int SHV_CTAS = 32;
 __global__ void __launch_bounds__(512)
-shv_from_zvec_kernel(const gf128* __restrict__ zvec, const gf128* __restrict__ eq_tail, gf128* __restrict__ out) {
+shv_from_zvec_kernel(const gf128* __restrict__ zvec, const gf128* __restrict__ eq_tail, gf128* __restrict__ part) {
   __shared__ gf128 red[4][128];
   const int b = threadIdx.x & 127, q = threadIdx.x >> 7;
-  gf256 acc = {{0, 0, 0, 0}};
-#pragma unroll 2
-  for (int h = 32 * q; h < 32 * q + 32; h++) gf256_acc(acc, gf_mul_wide(eq_tail[h], zvec[h * 128 + b]));
-  red[q][b] = gf256_reduce(acc);
+  const int h = 4 * blockIdx.x + q;
+  red[q][b] = gf_mul(eq_tail[h], zvec[h * 128 + b]);
   __syncthreads();
   if (q == 0) {
     gf128 v = red[0][b];
     for (int k = 1; k < 4; k++) v = gf_add(v, red[k][b]);
-    out[b] = v;
+    part[(size_t)blockIdx.x * 128 + b] = v;
   }
 }
 
 }  // namespace
 
-int flock_launch_shv_from_zvec(const void* zvec, const void* eq_tail, void* out, cudaStream_t st) {
-  shv_from_zvec_kernel<<<1, 512, 0, st>>>((const gf128*)zvec, (const gf128*)eq_tail, (gf128*)out);
+int flock_launch_shv_from_zvec(const void* zvec, const void* eq_tail, void* scratch, void* out, cudaStream_t st) {
+  static_assert(SHV_CTAS * 4 == 128, "the CTAs cover the 128 high indices");
+  shv_from_zvec_kernel<<<SHV_CTAS, 512, 0, st>>>((const gf128*)zvec, (const gf128*)eq_tail, (gf128*)scratch);
   flock_count_launch();
-  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+  if (cudaGetLastError() != cudaSuccess) return FLOCK_ERR_CUDA;
+  return flock_launch_reduce_rows(scratch, SHV_CTAS, 128, out, st);
 }
 
 

@@ -185,6 +185,7 @@ std::vector<F> transpose128(const std::vector<F>& v) {
 // s_k(v_k) and inverses, ligerito.rs:1747-1774.
 struct Sks {
   std::vector<F> s, inv;
+  std::vector<F> lin;  // [n][32]: What_k(x^b) for the bits b of a 32-bit index
 };
 const Sks& sks_for(int n) {
   static std::vector<Sks> cache(64);
@@ -207,6 +208,15 @@ const Sks& sks_for(int n) {
       cur--;
     }
     for (auto& v : r.s) r.inv.push_back(v.zero() ? F() : hf::inv(v));
+    // s_k is GF(2)-linear: What_k(q) = sum over the set bits b of q of What_k(x^b)
+    r.lin.assign((size_t)n * 32, F());
+    for (int b = 0; b < 32; b++) {
+      F s(1ULL << b, 0);
+      for (int k = 0; k < n; k++) {
+        if (k > 0) s = s * s + r.s[k - 1] * s;
+        r.lin[(size_t)k * 32 + b] = s * r.inv[k];
+      }
+    }
     cache[n] = r;
     have[n] = true;
   }
@@ -874,7 +884,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       void* det = S->small.get(128 * 16);
       h2d(*S, det, eq_tail.data(), 128 * 16);
       void* dsh = S->red.get(128 * 16);
-      FK(flock_launch_shv_from_zvec(S->zvec0.p, det, dsh, st));
+      FK(flock_launch_shv_from_zvec(S->zvec0.p, det, S->part.get(32 * 128 * 16), dsh, st));
       s_hat[0].resize(128);
       d2h(*S, s_hat[0].data(), dsh, 128 * 16);
       s_hat[1] = shv_c;
@@ -1004,9 +1014,8 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       const Sks& sk = sks_for(nvars);
       auto aw = eq_table(alpha_v);
       aw.resize(q.size());
-      void* dsk = S->small.get((size_t)(2 * (nvars + 1)) * 16);
-      h2d(*S, dsk, sk.s.data(), (nvars + 1) * 16);
-      h2d(*S, (char*)dsk + (nvars + 1) * 16, sk.inv.data(), (nvars + 1) * 16);
+      void* dsk = S->small.get((size_t)nvars * 32 * 16);
+      h2d(*S, dsk, sk.lin.data(), (size_t)nvars * 32 * 16);
       uint32_t* dq = (uint32_t*)S->qbuf.get(q.size() * 4);
       h2d(*S, dq, q.data(), q.size() * 4);
       void* dal = S->abuf.get(q.size() * 16);
@@ -1016,7 +1025,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       void* dLO = S->LO.get((q.size() << lo_bits) * 16);
       void* dHI = S->HI.get((q.size() << hi_bits) * 16);
       void* dbs = S->basis.get(((size_t)16) << nvars);
-      FK(flock_launch_induce_basis(dq, (int)q.size(), nvars, dsk, (const char*)dsk + (nvars + 1) * 16, dal, dW, dLO,
+      FK(flock_launch_induce_basis(dq, (int)q.size(), nvars, dsk, dal, dW, dLO,
                                    dHI, dbs, st));
       return dbs;
     };
@@ -1348,10 +1357,9 @@ void bind_top(std::vector<F>& v, F r) {
 
 std::vector<F> what_at(int n, const Sks& sk, uint32_t q) {
   std::vector<F> w(n);
-  if (n == 0) return w;
-  w[0] = F(q, 0);
-  for (int i = 1; i < n; i++) w[i] = w[i - 1] * w[i - 1] + sk.s[i - 1] * w[i - 1];
-  for (int i = 0; i < n; i++) w[i] = w[i] * sk.inv[i];
+  for (int k = 0; k < n; k++)
+    for (int b = 0; b < 32; b++)
+      if ((q >> b) & 1) w[k] += sk.lin[(size_t)k * 32 + b];
   return w;
 }
 
