@@ -130,17 +130,38 @@ __global__ void what_kernel(const uint32_t* __restrict__ queries, int nq, int n,
 }
 
 // T[i][j] = scale_i * prod_{k < bits, bit k of j} W[i][k0 + k]; scale_i = alpha_i or 1.
-__global__ void tensor_kernel(const gf128* __restrict__ W, int nq, int n, int k0, int bits,
-                              const gf128* __restrict__ scale, gf128* __restrict__ T) {
-  size_t len = (size_t)1 << bits;
-  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (size_t)nq * len) return;
-  int i = (int)(e / len);
-  size_t j = e % len;
-  gf128 acc = scale ? scale[i] : gf_one();
-  for (int k = 0; k < bits; k++)
-    if ((j >> k) & 1) acc = gf_mul(acc, W[(size_t)i * n + k0 + k]);
-  T[e] = acc;
+// CTA (query i, chunk c) first builds the sub-tables of the low TB_LO bits
+// (scaled) and of the remaining high bits (at most TB_HI) in shared memory,
+// then forms its 256 entries with one product each (a chain of up to `bits`
+// dependent products per entry before).
+constexpr int TB_LO = 5, TB_HI = 7, TB_THREADS = 256;
+static_assert((1 << TB_LO) <= 32 && 32 + (1 << TB_HI) <= TB_THREADS, "sub-table builders fit the CTA");
+__global__ void __launch_bounds__(TB_THREADS)
+tensor_kernel(const gf128* __restrict__ W, int nq, int n, int k0, int bits, const gf128* __restrict__ scale,
+              gf128* __restrict__ T) {
+  __shared__ gf128 lo_t[1 << TB_LO], hi_t[1 << TB_HI];
+  const int lb = bits < TB_LO ? bits : TB_LO, hb = bits - lb;
+  const size_t len = (size_t)1 << bits;
+  const size_t chunks = (len + TB_THREADS - 1) / TB_THREADS;
+  const int i = (int)(blockIdx.x / chunks);
+  const size_t c = blockIdx.x % chunks;
+  const gf128* w = W + (size_t)i * n + k0;
+  const int t = threadIdx.x;
+  if (t < (1 << lb)) {
+    gf128 acc = scale ? scale[i] : gf_one();
+    for (int k = 0; k < lb; k++)
+      if ((t >> k) & 1) acc = gf_mul(acc, w[k]);
+    lo_t[t] = acc;
+  } else if (t >= 32 && t - 32 < (1 << hb)) {
+    const int u = t - 32;
+    gf128 acc = gf_one();
+    for (int k = 0; k < hb; k++)
+      if ((u >> k) & 1) acc = gf_mul(acc, w[lb + k]);
+    hi_t[u] = acc;
+  }
+  __syncthreads();
+  const size_t j = c * TB_THREADS + t;
+  if (j < len) T[(size_t)i * len + j] = gf_mul(lo_t[j & ((1 << lb) - 1)], hi_t[j >> lb]);
 }
 
 // basis[j] = sum_i LO[i][j & mask] * HI[i][j >> lo_bits]
@@ -279,11 +300,12 @@ int flock_launch_induce_basis(const uint32_t* d_queries, int nq, int n, const vo
                                                                           (gf128*)W); flock_count_launch();
   const int lo_bits = flock_induce_basis_lo_bits(n), hi_bits = n - lo_bits;
   const bool tab = n >= kBasisTabMinBits;
-  size_t nlo = (size_t)nq << lo_bits, nhi = (size_t)nq << hi_bits;
-  tensor_kernel<<<grid_for(nlo, 256, 1u << 30), 256, 0, st>>>((const gf128*)W, nq, n, 0, lo_bits,
-                                                               (const gf128*)alpha_w, (gf128*)LO); flock_count_launch();
-  tensor_kernel<<<grid_for(nhi, 256, 1u << 30), 256, 0, st>>>((const gf128*)W, nq, n, lo_bits, hi_bits, nullptr,
-                                                               (gf128*)HI); flock_count_launch();
+  if (lo_bits > TB_LO + TB_HI || hi_bits > TB_LO + TB_HI) return FLOCK_ERR_SHAPE;
+  auto tgrid = [&](int bits) { return (unsigned)((size_t)nq * ((((size_t)1 << bits) + TB_THREADS - 1) / TB_THREADS)); };
+  tensor_kernel<<<tgrid(lo_bits), TB_THREADS, 0, st>>>((const gf128*)W, nq, n, 0, lo_bits, (const gf128*)alpha_w,
+                                                       (gf128*)LO); flock_count_launch();
+  tensor_kernel<<<tgrid(hi_bits), TB_THREADS, 0, st>>>((const gf128*)W, nq, n, lo_bits, hi_bits, nullptr,
+                                                       (gf128*)HI); flock_count_launch();
   if (tab) {
     flock_once_per_device((const void*)basis_tab_kernel<10>, [] {
       cudaFuncSetAttribute(basis_tab_kernel<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BT_SMEM);
