@@ -67,8 +67,10 @@ int flock_launch_glue(void* b, const void* add, size_t n, const uint64_t beta[2]
 int flock_induce_basis_lo_bits(int n);
 // what_lin: [n][32] F128, What_k(x^b) (the normalized subspace polynomials on
 // the index bits; What_k(q) is their XOR over the set bits of q).
+// scratch: flock_induce_basis_scratch_bytes(n) bytes (slice partials of small bases)
+size_t flock_induce_basis_scratch_bytes(int n);
 int flock_launch_induce_basis(const uint32_t* d_queries, int nq, int n, const void* what_lin, const void* alpha_w,
-                              void* W, void* LO, void* HI, void* basis, cudaStream_t st);
+                              void* W, void* LO, void* HI, void* basis, void* scratch, cudaStream_t st);
 int flock_launch_gather_rows(const void* mat, const uint32_t* rows, int n_rows, int width, void* out,
                              cudaStream_t st);
 int flock_launch_gather_nodes(const void* tree, const uint32_t* idx, int n, void* out, cudaStream_t st);

@@ -164,17 +164,20 @@ tensor_kernel(const gf128* __restrict__ W, int nq, int n, int k0, int bits, cons
   if (j < len) T[(size_t)i * len + j] = gf_mul(lo_t[j & ((1 << lb) - 1)], hi_t[j >> lb]);
 }
 
-// basis[j] = sum_i LO[i][j & mask] * HI[i][j >> lo_bits]
+// basis[j] = sum_i LO[i][j & mask] * HI[i][j >> lo_bits]. Slice blockIdx.y
+// sums the queries [y q_per, (y + 1) q_per) into row y of out (the slices'
+// rows are then XOR-reduced), so small bases still fill the GPU.
 __global__ void __launch_bounds__(256)
 basis_kernel(const gf128* __restrict__ LO, const gf128* __restrict__ HI, int nq, int lo_bits, int hi_bits,
-             gf128* __restrict__ basis) {
+             int q_per, gf128* __restrict__ out) {
   size_t n = (size_t)1 << (lo_bits + hi_bits);
   size_t lo_n = (size_t)1 << lo_bits, hi_n = (size_t)1 << hi_bits;
+  const int i0 = blockIdx.y * q_per, i1 = i0 + q_per < nq ? i0 + q_per : nq;
   for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
     size_t jl = j & (lo_n - 1), jh = j >> lo_bits;
     gf256 acc = {{0, 0, 0, 0}};
-    for (int i = 0; i < nq; i++) gf256_acc(acc, gf_mul_wide(LO[(size_t)i * lo_n + jl], HI[(size_t)i * hi_n + jh]));
-    basis[j] = gf256_reduce(acc);
+    for (int i = i0; i < i1; i++) gf256_acc(acc, gf_mul_wide(LO[(size_t)i * lo_n + jl], HI[(size_t)i * hi_n + jh]));
+    out[(size_t)blockIdx.y * n + j] = gf256_reduce(acc);
   }
 }
 
@@ -291,11 +294,13 @@ int flock_launch_glue(void* b, const void* add, size_t n, const uint64_t beta[2]
 // byte-table path from 2^18 entries: CTAs of 2^10 entries at 2^18, of 2^11
 // above (at least 256 CTAs; 2^11 measured faster than 2^10 and 2^9 at 2^19)
 constexpr int kBasisTabMinBits = 18;
+constexpr int kBasisSlices = 8;
+size_t flock_induce_basis_scratch_bytes(int n) { return n >= kBasisTabMinBits ? 0 : ((size_t)kBasisSlices << n) * 16; }
 
 int flock_induce_basis_lo_bits(int n) { return n >= kBasisTabMinBits ? (n == kBasisTabMinBits ? 10 : 11) : (n + 1) / 2; }
 
 int flock_launch_induce_basis(const uint32_t* d_queries, int nq, int n, const void* what_lin, const void* alpha_w,
-                              void* W, void* LO, void* HI, void* basis, cudaStream_t st) {
+                              void* W, void* LO, void* HI, void* basis, void* scratch, cudaStream_t st) {
   what_kernel<<<(unsigned)(((size_t)nq * n + 127) / 128), 128, 0, st>>>(d_queries, nq, n, (const gf128*)what_lin,
                                                                           (gf128*)W); flock_count_launch();
   const int lo_bits = flock_induce_basis_lo_bits(n), hi_bits = n - lo_bits;
@@ -319,8 +324,18 @@ int flock_launch_induce_basis(const uint32_t* d_queries, int nq, int n, const vo
       basis_tab_kernel<11><<<grid, BT_THREADS, BT_SMEM, st>>>((const gf128*)LO, (const gf128*)HI, nq, hi_bits,
                                                               (gf128*)basis);
   } else {
-    basis_kernel<<<grid_for((size_t)1 << n, 256, 152 * 8), 256, 0, st>>>((const gf128*)LO, (const gf128*)HI, nq,
-                                                                         lo_bits, hi_bits, (gf128*)basis);
+    // slices of the query sum: about 2^18 threads in all, at most kBasisSlices
+    // (one thread per entry ran 106 dependent products at 2^16 entries)
+    int slices = 1;
+    while (slices < kBasisSlices && ((size_t)slices << n) < ((size_t)1 << 18) && slices < nq) slices *= 2;
+    const int q_per = (nq + slices - 1) / slices;
+    const dim3 grid(grid_for((size_t)1 << n, 256, 152 * 8), slices);
+    basis_kernel<<<grid, 256, 0, st>>>((const gf128*)LO, (const gf128*)HI, nq, lo_bits, hi_bits, q_per,
+                                       (gf128*)(slices > 1 ? scratch : basis));
+    flock_count_launch();
+    if (cudaGetLastError() != cudaSuccess) return FLOCK_ERR_CUDA;
+    if (slices > 1) return flock_launch_reduce_rows(scratch, slices, 1 << n, basis, st);
+    return FLOCK_OK;
   }
   flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;

@@ -1025,8 +1025,9 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       void* dLO = S->LO.get((q.size() << lo_bits) * 16);
       void* dHI = S->HI.get((q.size() << hi_bits) * 16);
       void* dbs = S->basis.get(((size_t)16) << nvars);
-      FK(flock_launch_induce_basis(dq, (int)q.size(), nvars, dsk, dal, dW, dLO,
-                                   dHI, dbs, st));
+      const size_t scr = flock_induce_basis_scratch_bytes(nvars);
+      FK(flock_launch_induce_basis(dq, (int)q.size(), nvars, dsk, dal, dW, dLO, dHI, dbs,
+                                   scr ? S->part.get(scr) : nullptr, st));
       return dbs;
     };
 
