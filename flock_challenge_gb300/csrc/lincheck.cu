@@ -54,13 +54,20 @@ lc_partial_fold_kernel(const uint8_t* __restrict__ stripe, size_t n_stripes, con
     for (int q = 0; q < PF_GROUP; q++)
       bytes[q] = *reinterpret_cast<const uint4*>(stripe + (s0 + q) * FLOCK_K + col0);
     __syncthreads();
-    for (int e = threadIdx.x; e < PF_GROUP * 256; e += PF_THREADS) {
-      const int v = e >> 3, q = e & 7;
+    // subset sums by a Gray walk: thread (c, q) owns t8[8c .. 8c+7][q], starts
+    // from the sum over the bits of 8c and adds one weight per entry
+    static_assert(PF_THREADS == 32 * PF_GROUP, "one thread per (8-entry run, stripe)");
+    {
+      const int q = threadIdx.x & 7, c = threadIdx.x >> 3;
       gf128 acc8 = gf_zero();
 #pragma unroll
-      for (int r = 0; r < 8; r++)
-        if ((v >> r) & 1) acc8 = gf_add(acc8, e8v[r][q]);
-      t8[v][q] = acc8;
+      for (int r = 3; r < 8; r++)
+        if ((c >> (r - 3)) & 1) acc8 = gf_add(acc8, e8v[r][q]);
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        if (i) acc8 = gf_add(acc8, e8v[(i & 1) ? 0 : (i & 2) ? 1 : 2][q]);
+        t8[8 * c + (i ^ (i >> 1))][q] = acc8;
+      }
     }
     __syncthreads();
 #pragma unroll

@@ -201,3 +201,29 @@ def test_acc9_reduce_formula():
         lo = (l0 ^ t0 ^ t2 ^ (t2 << 1) ^ (t2 << 2) ^ (t2 << 7)) & M64
         hi = l1 ^ t1
         assert (hi << 64) | lo == pmod(a)
+
+
+def test_lincheck_subset_sum_gray_walk():
+    # csrc/lincheck.cu: thread (c, q) writes t8[8c + (i ^ (i >> 1))][q] for i < 8,
+    # starting from the bits of 8c and adding weight ctz(i) at step i: every
+    # entry v gets the XOR of the weights of its set bits, all 256 once
+    import random
+    rng = random.Random(4)
+    w = [rng.getrandbits(128) for _ in range(8)]
+    seen = {}
+    for c in range(32):
+        acc = 0
+        for r in range(3, 8):
+            if (c >> (r - 3)) & 1:
+                acc ^= w[r]
+        for i in range(8):
+            if i:
+                acc ^= w[0 if i & 1 else 1 if i & 2 else 2]
+            seen[8 * c + (i ^ (i >> 1))] = acc
+    assert sorted(seen) == list(range(256))
+    for v, val in seen.items():
+        want = 0
+        for r in range(8):
+            if (v >> r) & 1:
+                want ^= w[r]
+        assert val == want, v
