@@ -53,14 +53,22 @@ combined_basis_kernel(int lo_bits, int slices, const gf128* __restrict__ lo0, co
     beta[k * 128 + (i & 7) * 16 + (i >> 3)] = acc;
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < 2 * 16 * 256; e += CB_THREADS) {
-    const int k = e >> 12, v = (e >> 4) & 255, q = e & 15;
+  // subset sums by a Gray walk: item (k, c, q) owns entries v = 8c .. 8c+7 of
+  // position q of claim k, starts from the sum over the bits of 8c and adds
+  // one image per entry (consecutive items: consecutive q, distinct banks)
+  for (int it = threadIdx.x; it < 2 * 32 * 16; it += CB_THREADS) {
+    const int q = it & 15, c = (it >> 4) & 31, k = it >> 9;
     const gf128* bq = beta + k * 128 + q;
     gf128 acc = gf_zero();
 #pragma unroll
-    for (int t = 0; t < 8; t++)
-      if ((v >> t) & 1) acc = gf_add(acc, bq[16 * t]);
-    tab[e] = acc;
+    for (int t = 3; t < 8; t++)
+      if ((c >> (t - 3)) & 1) acc = gf_add(acc, bq[16 * t]);
+    gf128* row = tab + k * 4096 + q;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      if (i) acc = gf_add(acc, bq[16 * ((i & 1) ? 0 : (i & 2) ? 1 : 2)]);
+      row[(8 * c + (i ^ (i >> 1))) << 4] = acc;
+    }
   }
   __syncthreads();
   const size_t lo_n = (size_t)1 << lo_bits;
