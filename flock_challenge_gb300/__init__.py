@@ -145,6 +145,8 @@ def _proto_lib():
         L.flock_setup.argtypes = [P, ctypes.c_size_t]
         L.flock_prove.argtypes = [P, P, ctypes.c_size_t, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
         L.flock_last_phase_times.argtypes = [P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+        L.flock_kernel_timing.argtypes = [P, ctypes.c_int]
+        L.flock_last_kernel_times.argtypes = [P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
         L.flock_prove_seed.argtypes = [P, ctypes.c_uint32, ctypes.c_uint64, P, ctypes.c_size_t,
                                        ctypes.POINTER(ctypes.c_size_t)]
         L.flock_prove_device.argtypes = [P, P, ctypes.c_size_t, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
@@ -172,9 +174,104 @@ def _proto_lib():
         L.flock_prove_chain.argtypes = [P, P, ctypes.c_size_t, ctypes.c_char_p, P, ctypes.c_size_t, szp]
         L.flock_verify_chain.argtypes = [P, P, ctypes.c_size_t, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
         L.flock_chain_inputs.argtypes = [ctypes.c_size_t, ctypes.c_uint64, P, P]
+        L.flock_transcript_create.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(P)]
+        L.flock_transcript_fork.argtypes = [P, ctypes.POINTER(P)]
+        L.flock_transcript_destroy.argtypes = [P]
+        L.flock_transcript_observe_label.argtypes = [P, ctypes.c_char_p, ctypes.c_size_t]
+        L.flock_transcript_observe_f128.argtypes = [P, u64p]
+        L.flock_transcript_observe_f128_slice.argtypes = [P, u64p, ctypes.c_size_t]
+        L.flock_transcript_observe_bytes.argtypes = [P, ctypes.c_char_p, ctypes.c_size_t]
+        L.flock_transcript_sample_f128.argtypes = [P, u64p]
+        L.flock_transcript_sample_f128_vec.argtypes = [P, ctypes.c_size_t, u64p]
+        L.flock_prove_challenger.argtypes = [P, P, ctypes.c_size_t, ctypes.c_int, P, P, ctypes.c_size_t, szp, P,
+                                             ctypes.POINTER(R1csClaim)]
+        L.flock_verify_challenger.argtypes = [P, P, ctypes.c_size_t, P, ctypes.POINTER(ctypes.c_int)]
         L._proto_ready = True
     return L
 
+
+CLAIM_MAX_OUTER = 24  # FLOCK_CLAIM_MAX_OUTER
+
+
+class ZClaim(ctypes.Structure):
+    """flock_zclaim: z_hat(point) = value with point (z_skip, x_inner_rest, x_outer)
+    (ZClaim / QuirkyPoint, crates/flock-core/src/proof.rs:26-29, lincheck.rs:418-426)."""
+    _fields_ = [("z_skip", ctypes.c_uint64 * 2), ("x_inner_rest", (ctypes.c_uint64 * 2) * 8),
+                ("x_outer", (ctypes.c_uint64 * 2) * CLAIM_MAX_OUTER), ("n_outer", ctypes.c_uint32),
+                ("value", ctypes.c_uint64 * 2)]
+
+    def as_dict(self):
+        f = lambda a: (int(a[0]), int(a[1]))  # noqa: E731
+        return {"z_skip": f(self.z_skip), "x_inner_rest": [f(x) for x in self.x_inner_rest],
+                "x_outer": [f(self.x_outer[i]) for i in range(self.n_outer)], "value": f(self.value)}
+
+
+class R1csClaim(ctypes.Structure):
+    """flock_r1cs_claim: R1csClaim { ab, c } (crates/flock-core/src/proof.rs:36-45)."""
+    _fields_ = [("ab", ZClaim), ("c", ZClaim)]
+
+
+class FsChallenger:
+    """Caller-owned Fiat-Shamir transcript (flock_transcript_*): the reference's
+    FsChallenger::with_hash(domain, HashKind::Blake3)
+    (crates/flock-core/src/challenger.rs:183-438). F128 values are (lo, hi) pairs."""
+
+    def __init__(self, domain=b"flock-bench-v0", _handle=None):
+        self._h = ctypes.c_void_p()
+        if _handle is not None:
+            self._h = _handle
+        else:
+            d = _domain_bytes(domain)
+            check(_proto_lib().flock_transcript_create(d, len(d), ctypes.byref(self._h)), "flock_transcript_create")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def fork(self):
+        h = ctypes.c_void_p()
+        check(_proto_lib().flock_transcript_fork(self._h, ctypes.byref(h)), "flock_transcript_fork")
+        return FsChallenger(_handle=h)
+
+    def observe_label(self, label):
+        b = _domain_bytes(label)
+        check(_proto_lib().flock_transcript_observe_label(self._h, b, len(b)), "observe_label")
+
+    def observe_f128(self, v):
+        a = (ctypes.c_uint64 * 2)(*v)
+        check(_proto_lib().flock_transcript_observe_f128(self._h, a), "observe_f128")
+
+    def observe_f128_slice(self, vs):
+        a = (ctypes.c_uint64 * (2 * max(len(vs), 1)))(*[w for v in vs for w in v])
+        check(_proto_lib().flock_transcript_observe_f128_slice(self._h, a, len(vs)), "observe_f128_slice")
+
+    def observe_bytes(self, b):
+        b = bytes(b)
+        check(_proto_lib().flock_transcript_observe_bytes(self._h, b, len(b)), "observe_bytes")
+
+    def sample_f128(self):
+        a = (ctypes.c_uint64 * 2)()
+        check(_proto_lib().flock_transcript_sample_f128(self._h, a), "sample_f128")
+        return int(a[0]), int(a[1])
+
+    def sample_f128_vec(self, n):
+        a = (ctypes.c_uint64 * (2 * max(n, 1)))()
+        check(_proto_lib().flock_transcript_sample_f128_vec(self._h, n, a), "sample_f128_vec")
+        return [(int(a[2 * i]), int(a[2 * i + 1])) for i in range(n)]
+
+    def close(self):
+        if self._h:
+            _proto_lib().flock_transcript_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+KERNEL_SPANS = ["witness", "l0_ntt", "l0_merkle", "zerocheck_round1"]
 
 PHASES = ["setup", "commit", "zerocheck_round1", "zerocheck_rounds", "lincheck", "ring_switch", "ligerito",
           "serialize"]
@@ -200,11 +297,22 @@ class Blake3Setup:
         check(_proto_lib().flock_setup(self.ctx.handle, n_blocks), "flock_setup")
         self._buf = np.zeros(1 << 20, np.uint8)
 
-    def prove_fast(self, blocks):
+    def prove_fast(self, blocks, challenger=None):
+        """Proof bundle bytes of `blocks` under a fresh "flock-bench-v0" transcript;
+        with `challenger` (an FsChallenger), the proof continues that transcript
+        and advances it, and the call returns (bundle bytes, commitment root,
+        R1csClaim as a dict), as the reference's prove_fast returns (proof,
+        commitment, claim) (blake3.rs:3405-3409)."""
         blocks = np.ascontiguousarray(blocks, dtype=COMPRESSION_DTYPE)
         if len(blocks) != self.n_blocks:
             raise ValueError(f"expected {self.n_blocks} blocks, got {len(blocks)}")
         L = _proto_lib()
+        if challenger is not None:
+            root = (ctypes.c_uint8 * 32)()
+            claim = R1csClaim()
+            proof = self._call(L.flock_prove_challenger, blocks.ctypes.data_as(ctypes.c_void_p), len(blocks), 0,
+                               challenger.handle, _tail=(root, ctypes.byref(claim)))
+            return proof, bytes(root), {"ab": claim.ab.as_dict(), "c": claim.c.as_dict()}
         ln = ctypes.c_size_t()
         rc = L.flock_prove(self.ctx.handle, blocks.ctypes.data_as(ctypes.c_void_p), len(blocks),
                            self._buf.ctypes.data_as(ctypes.c_void_p), self._buf.size, ctypes.byref(ln))
@@ -215,13 +323,14 @@ class Blake3Setup:
         check(rc, "flock_prove")
         return self._buf[:ln.value].tobytes()
 
-    def _call(self, fn, *args):
+    def _call(self, fn, *args, _tail=()):
         ln = ctypes.c_size_t()
-        rc = fn(self.ctx.handle, *args, self._buf.ctypes.data_as(ctypes.c_void_p), self._buf.size, ctypes.byref(ln))
+        rc = fn(self.ctx.handle, *args, self._buf.ctypes.data_as(ctypes.c_void_p), self._buf.size, ctypes.byref(ln),
+                *_tail)
         if rc == -5:
             self._buf = np.zeros(ln.value, np.uint8)
             rc = fn(self.ctx.handle, *args, self._buf.ctypes.data_as(ctypes.c_void_p), self._buf.size,
-                    ctypes.byref(ln))
+                    ctypes.byref(ln), *_tail)
         check(rc, fn.__name__)
         return self._buf[:ln.value].tobytes()
 
@@ -257,6 +366,16 @@ class Blake3Setup:
     def stream_handle(self):
         """cudaStream_t the prover launches on (for event timing)."""
         return _proto_lib().flock_stream(self.ctx.handle)
+
+    def set_kernel_timing(self, on=True):
+        """CUDA-event timing of the main kernels of each proof (flock_kernel_timing)."""
+        check(_proto_lib().flock_kernel_timing(self.ctx.handle, int(bool(on))), "flock_kernel_timing")
+
+    def kernel_times(self):
+        """Device ms of the last proof's main kernels (flock_last_kernel_times)."""
+        arr = (ctypes.c_double * len(KERNEL_SPANS))()
+        check(_proto_lib().flock_last_kernel_times(self.ctx.handle, arr, len(KERNEL_SPANS)), "flock_last_kernel_times")
+        return dict(zip(KERNEL_SPANS, list(arr)))
 
     def phase_times(self):
         arr = (ctypes.c_double * 8)()
@@ -377,19 +496,25 @@ class Server:
 _VERIFY_CTX = {}
 
 
-def verify(proof, ctx=None, device=0):
+def verify(proof, ctx=None, device=0, challenger=None):
     """flock_verify: True when the serialized proof bundle verifies.
 
     Mirrors verifier::verify_ligerito on R1csProofBundleLigerito::from_bytes
-    (crates/flock-core/src/verifier.rs, crates/flock-prover/src/proof_io.rs)."""
+    (crates/flock-core/src/verifier.rs, crates/flock-prover/src/proof_io.rs).
+    With `challenger` (an FsChallenger) the replay continues that transcript
+    (flock_verify_challenger), which advances only on acceptance."""
     if ctx is None:
         ctx = _VERIFY_CTX.get(device)
         if ctx is None:
             ctx = _VERIFY_CTX[device] = Context(device)
     buf = np.frombuffer(bytes(proof), np.uint8)
     ok = ctypes.c_int()
-    check(_proto_lib().flock_verify(ctx.handle, buf.ctypes.data_as(ctypes.c_void_p), buf.size, ctypes.byref(ok)),
-          "flock_verify")
+    if challenger is not None:
+        check(_proto_lib().flock_verify_challenger(ctx.handle, buf.ctypes.data_as(ctypes.c_void_p), buf.size,
+                                                   challenger.handle, ctypes.byref(ok)), "flock_verify_challenger")
+    else:
+        check(_proto_lib().flock_verify(ctx.handle, buf.ctypes.data_as(ctypes.c_void_p), buf.size,
+                                        ctypes.byref(ok)), "flock_verify")
     return bool(ok.value)
 
 

@@ -7,6 +7,7 @@
 #include "prover.h"
 #include "host_blake3.h"
 #include "r1cs_setup.h"
+#include "transcript.h"
 
 #include <atomic>
 #include <mutex>
@@ -24,6 +25,10 @@ void flock_once_per_device(const void* key, void (*fn)()) {
   // run under the lock: no thread launches the kernel before the work is done
   if (done.insert({dev, key}).second) fn();
 }
+
+struct flock_transcript {
+  fs::Transcript t;
+};
 
 struct flock_ctx {
   int device = 0;
@@ -179,6 +184,99 @@ int flock_verify_batch(flock_ctx* ctx, size_t count, const uint8_t* const* proof
   return FLOCK_OK;
 }
 
+int flock_transcript_create(const uint8_t* domain, size_t domain_len, flock_transcript** out) {
+  if (!out || (!domain && domain_len)) return FLOCK_ERR_ARG;
+  *out = new (std::nothrow) flock_transcript{fs::Transcript(std::string((const char*)domain, domain_len))};
+  return *out ? FLOCK_OK : FLOCK_ERR_OOM;
+}
+
+int flock_transcript_fork(const flock_transcript* t, flock_transcript** out) {
+  if (!t || !out) return FLOCK_ERR_ARG;
+  *out = new (std::nothrow) flock_transcript{t->t};
+  return *out ? FLOCK_OK : FLOCK_ERR_OOM;
+}
+
+void flock_transcript_destroy(flock_transcript* t) { delete t; }
+
+int flock_transcript_observe_label(flock_transcript* t, const uint8_t* label, size_t len) {
+  if (!t || (!label && len)) return FLOCK_ERR_ARG;
+  t->t.label(label, len);
+  return FLOCK_OK;
+}
+
+int flock_transcript_observe_f128(flock_transcript* t, const uint64_t value[2]) {
+  if (!t || !value) return FLOCK_ERR_ARG;
+  t->t.observe(hf::F(value[0], value[1]));
+  return FLOCK_OK;
+}
+
+int flock_transcript_observe_f128_slice(flock_transcript* t, const uint64_t* values, size_t n) {
+  if (!t || (!values && n)) return FLOCK_ERR_ARG;
+  std::vector<hf::F> v(n);
+  for (size_t i = 0; i < n; i++) v[i] = hf::F(values[2 * i], values[2 * i + 1]);
+  t->t.observe_slice(v.data(), n);
+  return FLOCK_OK;
+}
+
+int flock_transcript_observe_bytes(flock_transcript* t, const uint8_t* bytes, size_t len) {
+  if (!t || (!bytes && len)) return FLOCK_ERR_ARG;
+  t->t.observe_bytes(bytes, len);
+  return FLOCK_OK;
+}
+
+int flock_transcript_sample_f128(flock_transcript* t, uint64_t out[2]) {
+  if (!t || !out) return FLOCK_ERR_ARG;
+  hf::F v = t->t.sample();
+  out[0] = v.lo;
+  out[1] = v.hi;
+  return FLOCK_OK;
+}
+
+int flock_transcript_sample_f128_vec(flock_transcript* t, size_t n, uint64_t* out) {
+  if (!t || (!out && n)) return FLOCK_ERR_ARG;
+  auto v = t->t.sample_vec(n);
+  for (size_t i = 0; i < n; i++) {
+    out[2 * i] = v[i].lo;
+    out[2 * i + 1] = v[i].hi;
+  }
+  return FLOCK_OK;
+}
+
+int flock_prove_challenger(flock_ctx* ctx, const flock_compression* in, size_t n, int in_on_device,
+                           flock_transcript* tr, uint8_t* out, size_t cap, size_t* len, uint8_t root[32],
+                           flock_r1cs_claim* claim) {
+  if (!ctx || !len || !tr || (n && !in)) return FLOCK_ERR_ARG;
+  size_t nn = n < 8 ? 8 : n;
+  int n_log = 0;
+  while (((size_t)1 << n_log) < nn) n_log++;
+  if (ctx->hbm_budget && flock_footprint_bytes((uint32_t)n_log) > ctx->hbm_budget) return FLOCK_ERR_OOM;
+  if (!ctx->prover) {
+    ctx->prover = flock_prover_create(ctx->device);
+    if (!ctx->prover) return FLOCK_ERR_CUDA;
+  }
+  // the proof runs on a copy, so a too-small output buffer leaves `tr` as it was
+  fs::Transcript work = tr->t;
+  flock_r1cs_claim cl;
+  int rc = flock_prover_prove(ctx->prover, in, n, n_log, ctx->last_proof, in_on_device != 0, nullptr, &work, &cl);
+  if (rc != FLOCK_OK) return rc;
+  *len = ctx->last_proof.size();
+  if (!out || cap < ctx->last_proof.size()) return FLOCK_ERR_CAPACITY;
+  memcpy(out, ctx->last_proof.data(), ctx->last_proof.size());
+  if (root) memcpy(root, ctx->last_proof.data() + 7, 32);  // "FLOCK" 4 2, then Commitment.root
+  if (claim) *claim = cl;
+  tr->t = work;
+  return FLOCK_OK;
+}
+
+int flock_verify_challenger(flock_ctx* ctx, const uint8_t* proof, size_t len, flock_transcript* tr, int* accepted) {
+  if (!ctx || !tr || (!proof && len) || !accepted) return FLOCK_ERR_ARG;
+  if (!ctx->prover) {
+    ctx->prover = flock_prover_create(ctx->device);
+    if (!ctx->prover) return FLOCK_ERR_CUDA;
+  }
+  return flock_prover_verify(ctx->prover, proof, len, accepted, nullptr, &tr->t);
+}
+
 int flock_prove_chain(flock_ctx* ctx, const flock_compression* in, size_t n, const char* domain, uint8_t* out,
                       size_t cap, size_t* len) {
   if (!ctx || !len || !in) return FLOCK_ERR_ARG;
@@ -245,6 +343,20 @@ void* flock_stream(flock_ctx* ctx) {
   if (!ctx) return nullptr;
   if (!ctx->prover) ctx->prover = flock_prover_create(ctx->device);
   return ctx->prover ? (void*)flock_prover_stream(ctx->prover) : nullptr;
+}
+
+int flock_kernel_timing(flock_ctx* ctx, int enable) {
+  if (!ctx) return FLOCK_ERR_ARG;
+  if (!ctx->prover) {
+    ctx->prover = flock_prover_create(ctx->device);
+    if (!ctx->prover) return FLOCK_ERR_CUDA;
+  }
+  return flock_prover_set_timing(ctx->prover, enable != 0);
+}
+
+int flock_last_kernel_times(const flock_ctx* ctx, double* ms, int n) {
+  if (!ctx || !ctx->prover || !ms) return FLOCK_ERR_ARG;
+  return flock_prover_kernel_times(ctx->prover, ms, n);
 }
 
 int flock_last_phase_times(const flock_ctx* ctx, double* ms, int n) {

@@ -20,6 +20,8 @@
 // taking row p mod 2^(log_d - r), which is the replicated state after the r
 // copy layers (pcs/commit.rs:451-473).
 #include <cstdio>
+#include <cuda.h>
+
 #include <map>
 #include <cstdlib>
 #include <mutex>
@@ -635,14 +637,17 @@ int flock_launch_ntt(void* d_data, const void* d_src, int log_d, int log_lanes, 
 namespace {
 
 constexpr int kNoAllocMaxLogD = FLOCK_NTT_NOALLOC_MAX_LOG_D;
-constexpr int kMaxDevices = 64;
 
 // Twiddle table of one transform of up to 2^16 positions: 2^16 - 1 entries
 // of 16 bytes (1 MiB, the last entry unused).
 __device__ __align__(256) gf128 g_noalloc_twiddles[(size_t)1 << kNoAllocMaxLogD];
 
+// Device address of g_noalloc_twiddles per CUDA context, keyed by the
+// context's process-unique id (cuCtxGetId): a context that a host framework
+// destroys and creates again (cudaDeviceReset, a primary-context reset) gets a
+// new id, and its first call looks the address up again.
 std::mutex g_noalloc_mu;
-void* g_noalloc_addr[kMaxDevices];  // device address of g_noalloc_twiddles per device
+std::map<unsigned long long, void*> g_noalloc_addr;
 
 // Entry (layer, bit) of the breadth-first table's generators: for layer l the
 // table holds the 2^l subset sums of {row_l[bit] : bit < l}, at
@@ -688,19 +693,55 @@ void twiddle_generators(int d, TwiddleGenerators* gen) {
   }
 }
 
-// Device address of the scratch array on the current device, looked up once
-// per device (the first call on each device; later calls read the cache).
+// Id of the current CUDA context (0 when none is current or the driver entry
+// points are unavailable), through the runtime's driver entry points so the
+// library links no driver library.
+unsigned long long current_context_id() {
+  typedef int (*GetCurrentFn)(CUcontext*);
+  typedef int (*GetIdFn)(CUcontext, unsigned long long*);
+  static GetCurrentFn get_current = nullptr;
+  static GetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (GetCurrentFn)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (GetIdFn)f;
+    cudaGetLastError();
+  });
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&c) != 0 || !c || get_id(c, &id) != 0) return 0;
+  return id;
+}
+
+// Device address of the scratch array in the current context: looked up with
+// cudaGetSymbolAddress by the first call in each context (once per device
+// unless its context is reset), read from the cache afterwards. A failed
+// lookup clears the runtime's error state before it returns.
 int noalloc_scratch(gf128** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return FLOCK_ERR_CUDA;
-  if (dev < 0 || dev >= kMaxDevices) return FLOCK_ERR_ARG;
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_twiddles) != cudaSuccess || !p) return FLOCK_ERR_CUDA;
-    g_noalloc_addr[dev] = p;
+  unsigned long long id = current_context_id();
+  if (id) {
+    auto it = g_noalloc_addr.find(id);
+    if (it != g_noalloc_addr.end()) {
+      *out = (gf128*)it->second;
+      return FLOCK_OK;
+    }
   }
-  *out = (gf128*)g_noalloc_addr[dev];
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_twiddles) != cudaSuccess || !p) {
+    cudaGetLastError();
+    return FLOCK_ERR_CUDA;
+  }
+  id = current_context_id();  // the lookup made the device's context current if none was
+  if (id) g_noalloc_addr[id] = p;
+  *out = (gf128*)p;
   return FLOCK_OK;
 }
 

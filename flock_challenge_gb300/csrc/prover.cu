@@ -286,6 +286,8 @@ struct Open {
 }  // namespace
 
 // ============================================================================
+constexpr int kKernelSpans = 4;  // witness, L0 NTT, L0 Merkle tree, zerocheck round 1
+
 struct ProverState {
   int device = 0;
   cudaStream_t st = nullptr;
@@ -296,6 +298,14 @@ struct ProverState {
   DBuf csc_ap, csc_ai, csc_bp, csc_bi;
   bool csc_ready = false;
   FlockPhaseTimes times;
+  // Optional CUDA-event timing of the main kernels of a proof, on the
+  // prover's stream: pairs of events around each span of kKernelSpans.
+  bool timing = false;
+  cudaEvent_t tev[2 * kKernelSpans] = {};
+  float span_ms[kKernelSpans] = {};
+  void mark(int i) {
+    if (timing && tev[i]) cudaEventRecord(tev[i], st);
+  }
   // Pinned host staging: small host->device copies are bump-allocated in
   // [0, kPinH2D) for the duration of one proof (pinned sources keep the
   // copies asynchronous); device->host reads go through the last kPinD2H bytes.
@@ -466,6 +476,8 @@ ProverState* flock_prover_create(int device) {
 void flock_prover_destroy(ProverState* S) {
   if (!S) return;
   cudaSetDevice(S->device);
+  for (cudaEvent_t e : S->tev)
+    if (e) cudaEventDestroy(e);
   if (S->d_r1t) cudaFree(S->d_r1t);
   if (S->st) cudaStreamDestroy(S->st);
   if (S->pin) cudaFreeHost(S->pin);
@@ -487,6 +499,21 @@ void flock_prover_trim(ProverState* S) {
 }
 
 const FlockPhaseTimes& flock_prover_times(const ProverState* S) { return S->times; }
+
+int flock_prover_set_timing(ProverState* S, bool on) {
+  if (on) {
+    if (cudaSetDevice(S->device) != cudaSuccess) return FLOCK_ERR_CUDA;
+    for (cudaEvent_t& e : S->tev)
+      if (!e && cudaEventCreate(&e) != cudaSuccess) return FLOCK_ERR_CUDA;
+  }
+  S->timing = on;
+  return FLOCK_OK;
+}
+
+int flock_prover_kernel_times(const ProverState* S, double* ms, int n) {
+  for (int k = 0; k < n && k < kKernelSpans; k++) ms[k] = S->timing ? S->span_ms[k] : 0.0;
+  return FLOCK_OK;
+}
 cudaStream_t flock_prover_stream(const ProverState* S) { return S->st; }
 
 int flock_prover_prove_seed(ProverState* S, int log2, uint64_t seed, std::vector<uint8_t>& out) {
@@ -505,7 +532,7 @@ int flock_prover_prove_seed(ProverState* S, int log2, uint64_t seed, std::vector
 }
 
 int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, int n_log, std::vector<uint8_t>& out,
-                       bool input_on_device, const ChainReq* chain) {
+                       bool input_on_device, const ChainReq* chain, fs::Transcript* ext_tr, flock_r1cs_claim* claim) {
   try {
     CK(cudaSetDevice(S->device));
     CK(cudaStreamSynchronize(S->st));  // the staging area of the previous proof is free again
@@ -551,14 +578,20 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       d_in = buf;
     }
     void *dz = S->z.get(nbytes), *da = S->a.get(nbytes), *db = S->b.get(nbytes), *ds = S->stripe.get(nbytes);
+    S->mark(0);
     FK(flock_launch_witness((const flock_compression*)d_in, n, n_log, dz, da, db, ds, st));
+    S->mark(1);
     const int lbs = 6, rate0 = 1;
     const int log_d0 = m - 7 - lbs + rate0;
     const size_t block0 = (size_t)1 << log_d0;
     void* dcw = S->cw.get((n128 << rate0) * 16);
     void* dtree = S->tree.get((2 * block0 - 1) * 32);
+    S->mark(2);
     FK(flock_launch_ntt(dcw, dz, log_d0, lbs, rate0, st));
+    S->mark(3);
+    S->mark(4);
     FK(flock_launch_merkle(dcw, block0, (size_t)16 << lbs, dtree, st));
+    S->mark(5);
     uint8_t root0[32];
     d2h(*S, root0, (const uint8_t*)dtree + (2 * block0 - 2) * 32, 32);
     T.commit_ms = clk.lap();
@@ -575,7 +608,8 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     w.u32(0);  // LigeritoProfile::Fast
     w.u32(1);  // HashKind::Blake3
 
-    fs::Transcript tr(chain ? chain->domain : "flock-bench-v0");
+    // the caller's transcript is copied and written back only when the proof is made
+    fs::Transcript tr = ext_tr ? *ext_tr : fs::Transcript(chain ? chain->domain : "flock-bench-v0");
     // bind_statement (crates/flock-core/src/proof.rs:51-59)
     tr.label("flock-r1cs-v0");
     tr.observe_bytes(digest, 32);
@@ -606,7 +640,9 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       FK(flock_launch_eq_split(dr, nv, 0, deq, S->eqhi.get(16), st));
       const int grid = 152;
       void* dpart = S->part.get((size_t)grid * 192 * 16);
+      S->mark(6);
       FK(flock_launch_zc_round1(da, db, dz, n_outer, deq, S->d_r1t, dpart, grid, st));
+      S->mark(7);
       auto sums = reduce_partials(*S, dpart, grid, 192);
       F dinv = zc::medium_dinv();
       const std::vector<F>& PM = phi_ext_matrix();
@@ -815,8 +851,31 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       d2h(*S, z_partial.data(), dzv, 64 * 16);
     }
     tr.observe_slice(z_partial.data(), 64);
-    tr.sample();  // lincheck's skip challenge: only the verifier evaluates the claim at it
+    const F lc_skip = tr.sample();  // lincheck's skip challenge: the ab claim's z_skip
     std::vector<F> r_inner_rest(lc_rr.rbegin(), lc_rr.rend());
+    if (claim) {
+      // R1csClaim { ab, c } (crates/flock-prover/src/prover.rs:255-262), RowMajor
+      // points (crates/flock-core/src/r1cs.rs:289-334): ab = (skip, r_inner_rest,
+      // x_outer) with w = <Lagrange_S(skip), z_partial>; c = (zerocheck skip
+      // point, r[6..14), r[14..m)) with the extracted c evaluation.
+      std::memset(claim, 0, sizeof(*claim));
+      const int n_out = m - 14;
+      if (n_out > FLOCK_CLAIM_MAX_OUTER) throw Fail(FLOCK_ERR_SHAPE, "claim size");
+      auto wl = LG.at(lc_skip, 0);
+      u2(lc_skip, claim->ab.z_skip);
+      u2(dot(wl.data(), z_partial.data(), 64), claim->ab.value);
+      u2(zc_z, claim->c.z_skip);
+      u2(final_c, claim->c.value);
+      for (int i = 0; i < 8; i++) {
+        u2(r_inner_rest[i], claim->ab.x_inner_rest[i]);
+        u2(r[6 + i], claim->c.x_inner_rest[i]);
+      }
+      for (int i = 0; i < n_out; i++) {
+        u2(x_out[i], claim->ab.x_outer[i]);
+        u2(r[14 + i], claim->c.x_outer[i]);
+      }
+      claim->ab.n_outer = claim->c.n_outer = (uint32_t)n_out;
+    }
     T.lincheck_ms = clk.lap();
     w.pv(lc_rounds);
     w.fv(z_partial);
@@ -1129,6 +1188,15 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       }
     }
     out.swap(w.v);
+    if (ext_tr) *ext_tr = tr;
+    if (S->timing) {
+      for (int k = 0; k < kKernelSpans; k++) {
+        S->span_ms[k] = 0;
+        if (cudaEventSynchronize(S->tev[2 * k + 1]) == cudaSuccess)
+          cudaEventElapsedTime(&S->span_ms[k], S->tev[2 * k], S->tev[2 * k + 1]);
+      }
+      cudaGetLastError();
+    }
     T.serialize_ms = clk.lap();
     return FLOCK_OK;
   } catch (const Fail& f) {
@@ -1412,7 +1480,7 @@ F fold_phys(const std::vector<uint8_t>& bits, F tau) {
 
 // R1CS bundle (chain_domain == nullptr) or chain bundle under chain_domain.
 static int verify_impl(ProverState* S, const uint8_t* data, size_t len, const char* chain_domain, int* accepted,
-                std::string* why) {
+                std::string* why, fs::Transcript* ext_tr) {
   *accepted = 0;
   const bool chain = chain_domain != nullptr;
   auto reject = [&](const char* w) {
@@ -1492,7 +1560,7 @@ static int verify_impl(ProverState* S, const uint8_t* data, size_t len, const ch
 
     uint8_t digest[32];
     flock_statement_digest(m, digest);
-    fs::Transcript tr(chain ? chain_domain : "flock-bench-v0");
+    fs::Transcript tr = ext_tr ? *ext_tr : fs::Transcript(chain ? chain_domain : "flock-bench-v0");
     tr.label("flock-r1cs-v0");
     tr.observe_bytes(digest, 32);
     tr.observe_bytes(root0.data(), 32);
@@ -1836,6 +1904,7 @@ static int verify_impl(ProverState* S, const uint8_t* data, size_t len, const ch
         F inner = dot(yr.data(), cy.data(), cy.size());
         if (inner != t_r) return reject("ligerito residual check");
         *accepted = 1;
+        if (ext_tr) *ext_tr = tr;
         if (why) *why = "ok";
         return FLOCK_OK;
       }
@@ -1868,11 +1937,12 @@ static int verify_impl(ProverState* S, const uint8_t* data, size_t len, const ch
   }
 }
 
-int flock_prover_verify(ProverState* S, const uint8_t* data, size_t len, int* accepted, std::string* why) {
-  return verify_impl(S, data, len, nullptr, accepted, why);
+int flock_prover_verify(ProverState* S, const uint8_t* data, size_t len, int* accepted, std::string* why,
+                        fs::Transcript* tr) {
+  return verify_impl(S, data, len, nullptr, accepted, why, tr);
 }
 
 int flock_prover_verify_chain(ProverState* S, const uint8_t* data, size_t len, const char* domain, int* accepted,
                               std::string* why) {
-  return verify_impl(S, data, len, domain ? domain : "flock_chain-cli", accepted, why);
+  return verify_impl(S, data, len, domain ? domain : "flock_chain-cli", accepted, why, nullptr);
 }

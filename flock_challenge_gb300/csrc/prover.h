@@ -8,6 +8,9 @@
 #include "../../include/flock_gpu.h"
 
 struct ProverState;
+namespace fs {
+class Transcript;
+}
 
 // Host wall time of each phase of the last proof, in milliseconds.
 struct FlockPhaseTimes {
@@ -27,12 +30,21 @@ void flock_prover_destroy(ProverState* s);
 // Proves n host compressions in 2^n_log slots; `out` receives the wire bytes.
 // With `chain`, the n = 2^n_log compressions form a cv chain and `out` is the
 // chain bundle (ChainProofBundleLigerito) instead of the R1CS bundle.
+// With `tr`, the proof continues the caller's transcript instead of a fresh
+// one of the benchmark domain, and leaves it advanced (only on success);
+// `claim` (optional) receives the R1CS claim the proof opens.
 int flock_prover_prove(ProverState* s, const flock_compression* in, size_t n, int n_log, std::vector<uint8_t>& out,
-                       bool input_on_device = false, const ChainReq* chain = nullptr);
+                       bool input_on_device = false, const ChainReq* chain = nullptr, fs::Transcript* tr = nullptr,
+                       flock_r1cs_claim* claim = nullptr);
 cudaStream_t flock_prover_stream(const ProverState* s);
 // Generates the 2^log2 benchmark inputs of `seed` on the device, then proves them.
 int flock_prover_prove_seed(ProverState* s, int log2, uint64_t seed, std::vector<uint8_t>& out);
 const FlockPhaseTimes& flock_prover_times(const ProverState* s);
+// CUDA-event timing of the main kernels of each proof (off by default) and
+// the spans of the last proof in ms: witness, L0 NTT, L0 Merkle tree,
+// zerocheck round 1.
+int flock_prover_set_timing(ProverState* s, bool on);
+int flock_prover_kernel_times(const ProverState* s, double* ms, int n);
 // Device bytes the state holds (its buffers grow to the largest proof seen).
 size_t flock_prover_reserved_bytes(const ProverState* s);
 // Frees the state's device buffers (after its stream is idle); the next proof
@@ -43,7 +55,10 @@ void flock_prover_trim(ProverState* s);
 // (optional) names the failed check. Returns a CUDA error code only when the
 // device work fails.
 #include <string>
-int flock_prover_verify(ProverState* s, const uint8_t* data, size_t len, int* accepted, std::string* why);
+// With `tr`, the replay continues the caller's transcript (advanced only when
+// the proof is accepted).
+int flock_prover_verify(ProverState* s, const uint8_t* data, size_t len, int* accepted, std::string* why,
+                        fs::Transcript* tr = nullptr);
 // Verifies a chain bundle (verify_chain, blake3.rs:3807-3830) under `domain`.
 int flock_prover_verify_chain(ProverState* s, const uint8_t* data, size_t len, const char* domain, int* accepted,
                               std::string* why);

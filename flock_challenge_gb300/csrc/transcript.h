@@ -25,9 +25,9 @@ class Transcript {
     put_len(domain.size());
     h_.update(domain.data(), domain.size());
   }
-  void label(const char* s) {
+  void label(const char* s) { label(s, strlen(s)); }
+  void label(const void* s, size_t n) {
     uint8_t op = 0x02;
-    size_t n = strlen(s);
     h_.update(&op, 1);
     put_len(n);
     h_.update(s, n);

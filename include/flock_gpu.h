@@ -53,6 +53,14 @@ const char* flock_version(void);
  * contexts). No reference counterpart; used to count launches per proof. */
 uint64_t flock_kernel_launches(void);
 
+/* Threading: the library has no lock inside a context. A context (and the
+ * buffers, stream and staging memory it owns) must be used by one host thread
+ * at a time: give each thread its own context, or serialise the calls on a
+ * shared one. Different contexts may run concurrently, also on one device.
+ * The stage entry points without a context (flock_witness, flock_merkle_tree,
+ * flock_generate_inputs) are thread-safe; flock_ntt_noalloc is thread-safe
+ * only for calls whose work does not overlap on the GPU (see there). */
+
 /* Create / destroy a device context bound to `device`. `hbm_budget` bounds the
  * device memory the context may hold (0 = no limit): a proof whose
  * flock_footprint_bytes exceeds it returns FLOCK_ERR_OOM.
@@ -96,17 +104,23 @@ int flock_ntt_tuned_variant(int device, int log_d, int log_lanes, int start_laye
  * that owns the GPU's memory through its own pool, or code running where
  * cudaMalloc is not allowed). No counterpart in the reference: it exists for
  * those callers only. Same transform, arguments and output as flock_ntt on
- * the current device, without a context. The twiddle table lives in a fixed
- * 1 MiB device array of the library (held on every GPU that loads it until
- * exit); log_d above FLOCK_NTT_NOALLOC_MAX_LOG_D returns FLOCK_ERR_LIMIT. The
- * first call on a device looks up that array's address, so make it before any
- * stream capture. Calls share the array: calls whose work overlaps on the GPU
- * race. Calls no cudaMalloc, cudaFree or other allocating routine. */
+ * the current device, without a context, for 3 <= log_num_ntts <= 10 (8 to
+ * 1024 interleaved transforms; other counts return FLOCK_ERR_SHAPE). The
+ * twiddle table lives in a fixed 1 MiB device array of the library (held on
+ * every GPU that loads it until exit); log_d above FLOCK_NTT_NOALLOC_MAX_LOG_D
+ * returns FLOCK_ERR_LIMIT. The first call in a CUDA context (once per device,
+ * unless the context is reset) looks up that array's address, so make it
+ * before any stream capture. Calls share the array: calls whose work overlaps
+ * on the GPU race. It runs only the generic multiply passes (no byte-table
+ * passes, no tuned pass shape), so it is slower than flock_ntt. Calls no
+ * cudaMalloc, cudaFree or other allocating routine. */
 int flock_ntt_noalloc(void* d_data, int log_d, int log_num_ntts, int start_layer, void* stream);
 
 /* Flat BLAKE3 Merkle tree (leaves first, root last; 2*n_leaves-1 nodes of 32
- * bytes) over n_leaves equal leaves of leaf_bytes (a multiple of 64, at most
- * 4096). Replaces merkle::merkle_tree (crates/flock-core/src/merkle.rs:733-765). */
+ * bytes) over n_leaves (a power of two) equal leaves of leaf_bytes: a
+ * multiple of 16 up to 1024 (one BLAKE3 chunk), or 2048, 3072 or 4096 (whole
+ * chunks); other sizes return FLOCK_ERR_SHAPE.
+ * Replaces merkle::merkle_tree (crates/flock-core/src/merkle.rs:733-765). */
 int flock_merkle_tree(const void* d_data, size_t n_leaves, size_t leaf_bytes, void* d_tree, void* stream);
 
 /* PCS commit of a packed witness d_z (2^(m-7) F128): replicate into
@@ -162,6 +176,14 @@ void* flock_stream(flock_ctx* ctx);
  * FLOCK_PHASE_TIMING prints, crates/flock-prover/src/prover.rs:958-1216). */
 int flock_last_phase_times(const flock_ctx* ctx, double* ms, int n);
 
+/* CUDA-event timing of the main kernels of every proof on this context, on
+ * the prover's own stream (enable != 0 turns it on; off by default), and
+ * the device time (ms) of each span of the last proof: witness, L0 NTT,
+ * L0 Merkle tree, zerocheck round 1 (first n entries; 0 while timing is off).
+ * No reference counterpart (measurement only). */
+int flock_kernel_timing(flock_ctx* ctx, int enable);
+int flock_last_kernel_times(const flock_ctx* ctx, double* ms, int n);
+
 /* ---- Verification -------------------------------------------------------- */
 
 /* Verifies a serialized proof bundle: *accepted = 1 if it is a valid proof of
@@ -179,6 +201,74 @@ int flock_verify(flock_ctx* ctx, const uint8_t* proof, size_t len, int* accepted
  * of each trial). */
 int flock_verify_batch(flock_ctx* ctx, size_t count, const uint8_t* const* proofs, const size_t* lens,
                        int* accepted);
+
+/* ---- The prove_fast seam: a caller-owned transcript and the claims ------- */
+
+/* A Fiat-Shamir transcript on the host: FsChallenger::with_hash(domain,
+ * HashKind::Blake3) (crates/flock-core/src/challenger.rs:183-438), i.e. the
+ * `&mut impl Challenger` that Blake3Setup::prove_fast takes
+ * (crates/flock-prover/src/r1cs_hashes/blake3.rs:3405-3409). F128 values are
+ * {lo, hi} little-endian u64 pairs. A handle is not thread-safe: use one per
+ * thread or serialise the calls on it. */
+typedef struct flock_transcript flock_transcript;
+
+/* FsChallenger::with_hash(domain, Blake3) (challenger.rs:214-240). */
+int flock_transcript_create(const uint8_t* domain, size_t domain_len, flock_transcript** out);
+/* Challenger::fork (challenger.rs:95-110): an independent copy of the state. */
+int flock_transcript_fork(const flock_transcript* t, flock_transcript** out);
+void flock_transcript_destroy(flock_transcript* t);
+/* Challenger::observe_label / observe_f128 / observe_f128_slice /
+ * observe_bytes (challenger.rs:34-60, FsChallenger's byte encoding). */
+int flock_transcript_observe_label(flock_transcript* t, const uint8_t* label, size_t len);
+int flock_transcript_observe_f128(flock_transcript* t, const uint64_t value[2]);
+int flock_transcript_observe_f128_slice(flock_transcript* t, const uint64_t* values, size_t n);
+int flock_transcript_observe_bytes(flock_transcript* t, const uint8_t* bytes, size_t len);
+/* Challenger::sample_f128, and FsChallenger's sample_f128_vec (one squeeze of
+ * 16 n bytes, not n single samples). */
+int flock_transcript_sample_f128(flock_transcript* t, uint64_t out[2]);
+int flock_transcript_sample_f128_vec(flock_transcript* t, size_t n, uint64_t* out);
+
+/* Most outer coordinates a claim holds (m - 14 <= 21 for m <= 35). */
+#define FLOCK_CLAIM_MAX_OUTER 24
+
+/* ZClaim: z_hat(point) = value, point = QuirkyPoint { z_skip, x_inner_rest,
+ * x_outer } (crates/flock-core/src/proof.rs:26-29, lincheck.rs:418-426) in the
+ * BLAKE3 relation's RowMajor layout (crates/flock-core/src/r1cs.rs:289-334):
+ * 8 inner coordinates, n_outer = m - 14 outer ones. */
+typedef struct flock_zclaim {
+  uint64_t z_skip[2];
+  uint64_t x_inner_rest[8][2];
+  uint64_t x_outer[FLOCK_CLAIM_MAX_OUTER][2];
+  uint32_t n_outer;
+  uint64_t value[2];
+} flock_zclaim;
+
+/* R1csClaim { ab, c } (crates/flock-core/src/proof.rs:36-45): ab from
+ * lincheck, c from the zerocheck's extracted C evaluation. */
+typedef struct flock_r1cs_claim {
+  flock_zclaim ab, c;
+} flock_r1cs_claim;
+
+/* Blake3Setup::prove_fast(&self, &[Compression], &mut impl Challenger) ->
+ * (R1csProofLigerito, Commitment, R1csClaim) (blake3.rs:3405-3409). Proves n
+ * compressions (host records, or device records when in_on_device != 0) as
+ * flock_prove does, but continues the caller's transcript `tr` (its domain
+ * and whatever it has absorbed) instead of a fresh "flock-bench-v0" one, and
+ * leaves it advanced past the proof, as the reference leaves the challenger.
+ * Outputs: out = the proof bundle (the Commitment and R1csProofLigerito
+ * serialized as R1csProofBundleLigerito::to_bytes, proof_io.rs:161-208),
+ * root (32 bytes, may be null) = the commitment root, claim (may be null) =
+ * the R1csClaim. On any status other than FLOCK_OK, `tr` is unchanged: with
+ * FLOCK_ERR_CAPACITY (*len set) a second call with a larger buffer and the
+ * same transcript returns the same proof. */
+int flock_prove_challenger(flock_ctx* ctx, const flock_compression* in, size_t n, int in_on_device,
+                           flock_transcript* tr, uint8_t* out, size_t cap, size_t* len, uint8_t root[32],
+                           flock_r1cs_claim* claim);
+
+/* flock_verify continuing the caller's transcript (the verifier side of the
+ * same seam, crates/flock-core/src/verifier.rs); `tr` is advanced only when
+ * the proof is accepted. */
+int flock_verify_challenger(flock_ctx* ctx, const uint8_t* proof, size_t len, flock_transcript* tr, int* accepted);
 
 /* ---- Hash chains ---------------------------------------------------------- */
 

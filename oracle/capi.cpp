@@ -14,6 +14,32 @@ void oracle_gf_mul(const uint64_t* a, const uint64_t* b, uint64_t* out) {
   out[0] = r.lo;
   out[1] = r.hi;
 }
+// Products of count pseudo-random operand pairs (SplitMix64 from seed) by
+// gf_mul and by the portable code; returns how many differ.
+size_t oracle_gf_crosscheck(size_t count, uint64_t seed) {
+  uint64_t s = seed;
+  auto next = [&s]() {
+    s += 0x9E3779B97F4A7C15ull;
+    uint64_t z = s;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  };
+  size_t bad = 0;
+  for (size_t i = 0; i < count; i++) {
+    F128 a = f128(next(), next()), b = f128(next(), next());
+    if (i % 7 == 0) a.hi = 0;         // sparse operands too
+    if (i % 11 == 0) b.lo = ~0ull;
+    if (gf_mul(a, b) != gf_mul_portable(a, b)) bad++;
+  }
+  return bad;
+}
+int oracle_gf_uses_pmull() { return gf_mul_uses_pmull(); }
+void oracle_gf_mul_portable(const uint64_t* a, const uint64_t* b, uint64_t* out) {
+  F128 r = gf_mul_portable(f128(a[0], a[1]), f128(b[0], b[1]));
+  out[0] = r.lo;
+  out[1] = r.hi;
+}
 void oracle_gf_inv(const uint64_t* a, uint64_t* out) {
   F128 r = gf_inv(f128(a[0], a[1]));
   out[0] = r.lo;
@@ -160,6 +186,13 @@ void digest_for(int m, uint8_t out[32]) {
 
 extern "C" {
 
+// Builds and caches the base matrices and the statement digest of m (the
+// setup every proof of that m reuses), so a timed proof excludes them.
+void oracle_warm(int m) {
+  uint8_t dg[32];
+  digest_for(m, dg);
+}
+
 // Proves n compressions (padded to 2^n_blocks_log slots); writes the wire bytes.
 // Returns 0, or -5 when cap is too small (len receives the needed size).
 int oracle_prove(const Compression* blocks, size_t n, int n_blocks_log, uint8_t* out, size_t cap, size_t* len) {
@@ -172,6 +205,68 @@ int oracle_prove(const Compression* blocks, size_t n, int n_blocks_log, uint8_t*
   if (bytes.size() > cap) return -5;
   memcpy(out, bytes.data(), bytes.size());
   return 0;
+}
+
+// Caller-owned transcripts (the Challenger seam of prove_fast): the oracle's
+// FsChallenger restatement behind an opaque pointer.
+void* oracle_transcript_new(const uint8_t* domain, size_t n) {
+  return new Transcript(std::string((const char*)domain, n));
+}
+void* oracle_transcript_clone(const void* t) { return new Transcript(*(const Transcript*)t); }
+void oracle_transcript_free(void* t) { delete (Transcript*)t; }
+void oracle_transcript_label(void* t, const uint8_t* p, size_t n) {
+  ((Transcript*)t)->label(std::string((const char*)p, n));
+}
+void oracle_transcript_observe_f128(void* t, const uint64_t* v) { ((Transcript*)t)->observe_f128(f128(v[0], v[1])); }
+void oracle_transcript_observe_slice(void* t, const uint64_t* v, size_t n) {
+  ((Transcript*)t)->observe_slice((const F128*)v, n);
+}
+void oracle_transcript_observe_bytes(void* t, const uint8_t* p, size_t n) { ((Transcript*)t)->observe_bytes(p, n); }
+void oracle_transcript_sample(void* t, uint64_t* out) {
+  F128 v = ((Transcript*)t)->sample();
+  out[0] = v.lo;
+  out[1] = v.hi;
+}
+void oracle_transcript_sample_vec(void* t, size_t n, uint64_t* out) {
+  auto v = ((Transcript*)t)->sample_vec(n);
+  memcpy(out, v.data(), n * 16);
+}
+
+// oracle_prove with the caller's transcript, which the proof advances.
+// claim (F128 entries, may be null): ab z_skip, ab value, c z_skip, c value,
+// then ab x_inner_rest (8), ab x_outer (m - 14), c x_inner_rest (8), c x_outer.
+int oracle_prove_tr(const Compression* blocks, size_t n, int n_blocks_log, void* t, uint8_t* out, size_t cap,
+                    size_t* len, uint64_t* claim) {
+  std::vector<Compression> v(blocks, blocks + n);
+  uint8_t dg[32];
+  digest_for(K_LOG + n_blocks_log, dg);
+  R1csClaimOut c;
+  Bundle b = prove_with(v, n_blocks_log, dg, *(Transcript*)t, &c);
+  auto bytes = encode_bundle(b);
+  *len = bytes.size();
+  if (claim) {
+    std::vector<F128> flat = {c.ab_skip, c.ab_value, c.c_skip, c.c_value};
+    for (auto* part : {&c.ab_inner, &c.ab_outer, &c.c_inner, &c.c_outer}) flat.insert(flat.end(), part->begin(), part->end());
+    memcpy(claim, flat.data(), flat.size() * 16);
+  }
+  if (bytes.size() > cap) return -5;
+  memcpy(out, bytes.data(), bytes.size());
+  return 0;
+}
+
+// oracle_verify with the caller's transcript (advanced by the replay).
+int oracle_verify_tr(const uint8_t* bytes, size_t len, int m, void* t, char* why, size_t why_cap) {
+  Bundle b;
+  if (!decode_bundle(bytes, len, b)) {
+    if (why && why_cap) snprintf(why, why_cap, "malformed");
+    return -1;
+  }
+  uint8_t dg[32];
+  digest_for(m, dg);
+  std::string w;
+  bool ok = verify_with(b, m, dg, mats().A, mats().B, *(Transcript*)t, &w);
+  if (why && why_cap) snprintf(why, why_cap, "%s", ok ? "ok" : w.c_str());
+  return ok ? 0 : -2;
 }
 
 // 0 = accepted; -1 = malformed bytes; -2 = rejected. why (may be null) gets a

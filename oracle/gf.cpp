@@ -1,12 +1,17 @@
 // GF(2^128) / GF(2^8) arithmetic for the oracle (test infrastructure only).
 #include "oracle.h"
 
+#if defined(__aarch64__) && (defined(__ARM_FEATURE_AES) || defined(__ARM_FEATURE_CRYPTO))
+#include <arm_neon.h>
+#endif
+
 namespace oracle {
 
-// 64x64 -> 128 carry-less product with a 4-bit window table of b.
-// Same value as the reference's bit-serial clmul64
-// (crates/flock-core/src/field/gf2_128/portable.rs:4-20).
-static inline void clmul64(uint64_t a, uint64_t b, uint64_t& lo, uint64_t& hi) {
+// 64x64 -> 128 carry-less products. Same value as the reference's bit-serial
+// clmul64 (crates/flock-core/src/field/gf2_128/portable.rs:4-20).
+//
+// Portable form: a 4-bit window table of b.
+static inline void clmul64_portable(uint64_t a, uint64_t b, uint64_t& lo, uint64_t& hi) {
   uint64_t tl[16], th[16];
   tl[0] = 0; th[0] = 0;
   tl[1] = b; th[1] = 0;
@@ -29,6 +34,22 @@ static inline void clmul64(uint64_t a, uint64_t b, uint64_t& lo, uint64_t& hi) {
   }
 }
 
+#if defined(__aarch64__) && (defined(__ARM_FEATURE_AES) || defined(__ARM_FEATURE_CRYPTO))
+// The reference's aarch64 backend multiplies with PMULL
+// (crates/flock-core/src/field/gf2_128/aarch64.rs:26-60); so does the oracle
+// on an Arm host built with the crypto extension (oracle/Makefile).
+#define ORACLE_GF_PMULL 1
+static inline void clmul64(uint64_t a, uint64_t b, uint64_t& lo, uint64_t& hi) {
+  const poly128_t p = vmull_p64((poly64_t)a, (poly64_t)b);
+  const uint64x2_t v = vreinterpretq_u64_p128(p);
+  lo = vgetq_lane_u64(v, 0);
+  hi = vgetq_lane_u64(v, 1);
+}
+#else
+#define ORACLE_GF_PMULL 0
+static inline void clmul64(uint64_t a, uint64_t b, uint64_t& lo, uint64_t& hi) { clmul64_portable(a, b, lo, hi); }
+#endif
+
 // crates/flock-core/src/field/gf2_128.rs:192-216 (fold of the upper 128 bits).
 static inline F128 reduce(uint64_t r0, uint64_t r1, uint64_t r2, uint64_t r3) {
   uint64_t s1_lo = r2 << 1, s1_hi = (r3 << 1) | (r2 >> 63);
@@ -50,6 +71,20 @@ F128 gf_mul(F128 a, F128 b) {
   uint64_t cr_lo = lh_lo ^ hl_lo, cr_hi = lh_hi ^ hl_hi;
   return reduce(ll_lo, ll_hi ^ cr_lo, hh_lo ^ cr_hi, hh_hi);
 }
+
+// The portable product whatever the host; the test suite checks it against
+// gf_mul (PMULL on an Arm host with the crypto extension).
+F128 gf_mul_portable(F128 a, F128 b) {
+  uint64_t ll_lo, ll_hi, lh_lo, lh_hi, hl_lo, hl_hi, hh_lo, hh_hi;
+  clmul64_portable(a.lo, b.lo, ll_lo, ll_hi);
+  clmul64_portable(a.lo, b.hi, lh_lo, lh_hi);
+  clmul64_portable(a.hi, b.lo, hl_lo, hl_hi);
+  clmul64_portable(a.hi, b.hi, hh_lo, hh_hi);
+  uint64_t cr_lo = lh_lo ^ hl_lo, cr_hi = lh_hi ^ hl_hi;
+  return reduce(ll_lo, ll_hi ^ cr_lo, hh_lo ^ cr_hi, hh_hi);
+}
+
+int gf_mul_uses_pmull() { return ORACLE_GF_PMULL; }
 
 // Fermat inverse a^(2^128-2), gf2_128.rs:56-66.
 F128 gf_inv(F128 a) {

@@ -30,6 +30,8 @@ struct F128 {
 };
 inline F128 f128(uint64_t lo, uint64_t hi = 0) { F128 r; r.lo = lo; r.hi = hi; return r; }
 F128 gf_mul(F128 a, F128 b);
+F128 gf_mul_portable(F128 a, F128 b);  // same value, portable integer code on every host
+int gf_mul_uses_pmull();               // 1 when gf_mul runs on the Arm PMULL instruction
 F128 gf_inv(F128 a);
 F128 gf_mul_x(F128 a);
 inline F128 operator*(F128 a, F128 b) { return gf_mul(a, b); }

@@ -1264,14 +1264,13 @@ static RsOut ring_switch_prove(const std::vector<F128>& z, const std::vector<F12
 // shift sumcheck, then one opening over [ab, c] plus the packed-direct chain
 // claim (pcs.rs:1055-1090).
 static Bundle prove_impl(const std::vector<Compression>& blocks, int n_log, const uint8_t digest[32],
-                         const std::string& domain, ChainBundle* chain) {
+                         Transcript& tr, ChainBundle* chain, R1csClaimOut* claim_out) {
   Bundle out;
   Witness w = build_witness(blocks, n_log, true);
   int m = w.m;
   out.params.m = m;
   CommitData cd = commit(w.z, out.params);
   out.root = cd.root();
-  Transcript tr(domain);
   bind_statement(tr, digest, out.root);
   ZcClaim zc;
   out.zc = zc_prove((const uint64_t*)w.a.data(), (const uint64_t*)w.b.data(), (const uint64_t*)w.z.data(), m, tr, zc);
@@ -1295,6 +1294,16 @@ static Bundle prove_impl(const std::vector<Compression>& blocks, int n_log, cons
     chain->shift = prove_chain_shift(in_vals, out_vals, tr, cl);
     pd_point = chain_claim_point(tau, cl);
     pd_value = cl.value;
+  }
+  if (claim_out) {  // R1csClaim { ab, c } (prover.rs:255-262; r1cs.rs:289-334, RowMajor)
+    claim_out->ab_skip = lc.r_inner_skip;
+    claim_out->ab_inner = lc.r_inner_rest;
+    claim_out->ab_outer = x_out;
+    claim_out->ab_value = lc.w;
+    claim_out->c_skip = zc.z;
+    claim_out->c_inner.assign(zc.r_rest.begin(), zc.r_rest.begin() + (K_LOG - K_SKIP));
+    claim_out->c_outer.assign(zc.r_rest.begin() + (K_LOG - K_SKIP), zc.r_rest.end());
+    claim_out->c_value = zc.c_eval;
   }
   // Claims [ab, c]; x_full = x_inner_rest ++ x_outer (prover.rs:138-146).
   std::vector<F128> x_ab(lc.r_inner_rest);
@@ -1324,14 +1333,21 @@ static Bundle prove_impl(const std::vector<Compression>& blocks, int n_log, cons
 }
 
 Bundle prove(const std::vector<Compression>& blocks, int n_log, const uint8_t digest[32], const std::string& domain) {
-  return prove_impl(blocks, n_log, digest, domain, nullptr);
+  Transcript tr(domain);
+  return prove_impl(blocks, n_log, digest, tr, nullptr, nullptr);
+}
+
+Bundle prove_with(const std::vector<Compression>& blocks, int n_log, const uint8_t digest[32], Transcript& tr,
+                  R1csClaimOut* claim) {
+  return prove_impl(blocks, n_log, digest, tr, nullptr, claim);
 }
 
 ChainBundle prove_chain(const std::vector<Compression>& blocks, int n_log, const uint8_t digest[32],
                         const std::string& domain) {
   if (blocks.empty() || blocks.size() != ((size_t)1 << n_log)) throw std::runtime_error("chain: steps must fill 2^n");
   ChainBundle cb;
-  cb.b = prove_impl(blocks, n_log, digest, domain, &cb);
+  Transcript tr(domain);
+  cb.b = prove_impl(blocks, n_log, digest, tr, &cb, nullptr);
   uint32_t o[16];
   const Compression& l = blocks.back();
   b3_compress(l.cv, l.m, l.counter, l.block_len, l.flags, o);
@@ -1341,12 +1357,11 @@ ChainBundle prove_chain(const std::vector<Compression>& blocks, int n_log, const
 }
 
 static bool verify_impl(const Bundle& bd, int m, const uint8_t digest[32], const SparseRows& A, const SparseRows& B,
-                        const std::string& domain, std::string* why, const ChainBundle* chain) {
+                        Transcript& tr, std::string* why, const ChainBundle* chain) {
   if (bd.params.m != m || bd.params.log_inv_rate != 1 || bd.params.log_batch_size != 6) {
     if (why) *why = "params";
     return false;
   }
-  Transcript tr(domain);
   bind_statement(tr, digest, bd.root);
   ZcClaim zc;
   if (!zc_verify(bd.zc, m, tr, zc, why)) return false;
@@ -1424,12 +1439,19 @@ static bool verify_impl(const Bundle& bd, int m, const uint8_t digest[32], const
 
 bool verify(const Bundle& bd, int m, const uint8_t digest[32], const SparseRows& A, const SparseRows& B,
             const std::string& domain, std::string* why) {
-  return verify_impl(bd, m, digest, A, B, domain, why, nullptr);
+  Transcript tr(domain);
+  return verify_impl(bd, m, digest, A, B, tr, why, nullptr);
+}
+
+bool verify_with(const Bundle& bd, int m, const uint8_t digest[32], const SparseRows& A, const SparseRows& B,
+                 Transcript& tr, std::string* why) {
+  return verify_impl(bd, m, digest, A, B, tr, why, nullptr);
 }
 
 bool verify_chain(const ChainBundle& cb, int m, const uint8_t digest[32], const SparseRows& A, const SparseRows& B,
                   const std::string& domain, std::string* why) {
-  return verify_impl(cb.b, m, digest, A, B, domain, why, &cb);
+  Transcript tr(domain);
+  return verify_impl(cb.b, m, digest, A, B, tr, why, &cb);
 }
 
 // ============================================================================

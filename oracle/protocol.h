@@ -88,6 +88,20 @@ Bundle prove(const std::vector<Compression>& blocks, int n_blocks_log, const uin
 bool verify(const Bundle& b, int m, const uint8_t digest[32], const SparseRows& A, const SparseRows& B,
             const std::string& domain = "flock-bench-v0", std::string* why = nullptr);
 
+// The same with the caller's transcript (Blake3Setup::prove_fast takes
+// `&mut impl Challenger`, crates/flock-prover/src/r1cs_hashes/blake3.rs:3405-3409):
+// the proof continues from its state and leaves it advanced. `claim` receives
+// R1csClaim { ab, c } (crates/flock-core/src/proof.rs:26-45), points in the
+// RowMajor layout (crates/flock-core/src/r1cs.rs:289-334).
+struct R1csClaimOut {
+  F128 ab_skip, ab_value, c_skip, c_value;
+  std::vector<F128> ab_inner, ab_outer, c_inner, c_outer;
+};
+Bundle prove_with(const std::vector<Compression>& blocks, int n_blocks_log, const uint8_t digest[32], Transcript& tr,
+                  R1csClaimOut* claim);
+bool verify_with(const Bundle& b, int m, const uint8_t digest[32], const SparseRows& A, const SparseRows& B,
+                 Transcript& tr, std::string* why = nullptr);
+
 // ---------------------------------------------------------------------------
 // Hash-chain relation (chain.cpp; crates/flock-prover/src/chain.rs,
 // r1cs_hashes/chain_common.rs, r1cs_hashes/blake3.rs:3750-3830).

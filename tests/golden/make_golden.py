@@ -1,8 +1,9 @@
 """Regenerates the golden fixtures in this folder from the reference sources.
 
-Run once in a checkout that has the reference tree (path given as argv[1],
-default /root/reference). The fixtures are committed so the tests never read
-the reference at run time.
+Usage: python tests/golden/make_golden.py REFERENCE_ROOT
+
+REFERENCE_ROOT is the root of a Layr-Labs/flock-challenge checkout (required).
+The fixtures are committed so the tests never read the reference at run time.
 
 phi8.json          PHI_8_TABLE of crates/flock-core/src/field/phi8.rs:18-1040
                    (the GF(2^8) -> GF(2^128) embedding, 256 entries as [lo, hi]).
@@ -10,13 +11,19 @@ ghash_kat.json     the GHASH known-answer identities of
                    crates/flock-core/src/field/gf2_128.rs:378-405.
 layout.json        the BLAKE3 witness layout constants asserted at
                    crates/flock-prover/src/r1cs_hashes/blake3.rs:4334-4350.
+reference_pins.json  the canary's pinned proof length EXPECTED_PROOF_BYTES
+                   (blake3.rs:4914) and the worker's warm-up seed
+                   (benchmark-tools/worker/src/main.rs:29); make_oracle_digests.py
+                   checks the oracle's canary proof against the former.
 """
 import json
 import os
 import re
 import sys
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    raise SystemExit(__doc__)
+ref = sys.argv[1]
 here = os.path.dirname(os.path.abspath(__file__))
 
 src = open(os.path.join(ref, "crates/flock-core/src/field/phi8.rs")).read()
@@ -42,4 +49,13 @@ seg = b3[b3.index("fn layout_constants()"):]
 seg = seg[:seg.index("}\n")]
 layout = {k: int(v.replace("_", "")) for k, v in re.findall(r"assert_eq!\((\w+), ([0-9_]+)\)", seg)}
 json.dump(layout, open(os.path.join(here, "layout.json"), "w"), indent=1, sort_keys=True)
+canary = b3[b3.index("fn ranked_blake3_proof_canary()"):]
+expected = int(re.search(r"EXPECTED_PROOF_BYTES: usize = ([0-9_]+);", canary).group(1).replace("_", ""))
+worker = open(os.path.join(ref, "benchmark-tools/worker/src/main.rs")).read()
+warm = int(re.search(r"generate_compressions\(log2_size, (0x[0-9A-Fa-f_]+)\)", worker).group(1).replace("_", ""), 16)
+json.dump({"canary_expected_proof_bytes": expected,
+           "canary_source": "crates/flock-prover/src/r1cs_hashes/blake3.rs:4914 EXPECTED_PROOF_BYTES",
+           "worker_warmup_seed": warm,
+           "worker_warmup_source": "benchmark-tools/worker/src/main.rs:29"},
+          open(os.path.join(here, "reference_pins.json"), "w"), indent=1)
 print("wrote", sorted(os.listdir(here)))

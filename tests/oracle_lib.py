@@ -183,6 +183,7 @@ def _proto():
         L.oracle_shift_mle.argtypes = [P, P, ctypes.c_int, P]
         L.oracle_f8_extend_ntt.argtypes = [ctypes.c_uint64, P]
         L.oracle_f8_extend_lagrange.argtypes = [ctypes.c_uint64, P]
+        L.oracle_warm.argtypes = [ctypes.c_int]
         L._proto_ready = True
     return L
 
@@ -197,6 +198,16 @@ def prove(blocks, n_blocks_log):
     rc = L.oracle_prove(ptr(blocks), len(blocks), n_blocks_log, ptr(out), cap, ctypes.byref(ln))
     assert rc == 0, rc
     return out[:ln.value].tobytes()
+
+
+def warm(m):
+    """Builds the oracle's cached setup (matrices, statement digest) for m."""
+    _proto().oracle_warm(m)
+
+
+def uses_pmull():
+    """True when the oracle's GF(2^128) product runs on the Arm PMULL instruction."""
+    return bool(lib().oracle_gf_uses_pmull())
 
 
 def verify(proof_bytes, m):
@@ -255,3 +266,96 @@ def f8_extend(row, via="ntt"):
     out = np.zeros(64, np.uint8)
     (L.oracle_f8_extend_ntt if via == "ntt" else L.oracle_f8_extend_lagrange)(row, ptr(out))
     return out
+
+
+class Transcript:
+    """The oracle's FsChallenger restatement (challenger.rs:183-438) behind a
+    handle, mirroring flock_challenge_gb300.FsChallenger's methods."""
+
+    def __init__(self, domain=b"flock-bench-v0", _h=None):
+        L = _tr_lib()
+        self._h = _h if _h is not None else L.oracle_transcript_new(domain, len(domain))
+
+    def fork(self):
+        return Transcript(_h=_tr_lib().oracle_transcript_clone(self._h))
+
+    def observe_label(self, b):
+        _tr_lib().oracle_transcript_label(self._h, bytes(b), len(b))
+
+    def observe_f128(self, v):
+        _tr_lib().oracle_transcript_observe_f128(self._h, ptr(np.array(v, np.uint64)))
+
+    def observe_f128_slice(self, vs):
+        a = np.array(vs, np.uint64).reshape(-1) if len(vs) else np.zeros(2, np.uint64)
+        _tr_lib().oracle_transcript_observe_slice(self._h, ptr(a), len(vs))
+
+    def observe_bytes(self, b):
+        _tr_lib().oracle_transcript_observe_bytes(self._h, bytes(b), len(b))
+
+    def sample_f128(self):
+        out = np.zeros(2, np.uint64)
+        _tr_lib().oracle_transcript_sample(self._h, ptr(out))
+        return int(out[0]), int(out[1])
+
+    def sample_f128_vec(self, n):
+        out = np.zeros(2 * max(n, 1), np.uint64)
+        _tr_lib().oracle_transcript_sample_vec(self._h, n, ptr(out))
+        return [(int(out[2 * i]), int(out[2 * i + 1])) for i in range(n)]
+
+    def __del__(self):
+        try:
+            _tr_lib().oracle_transcript_free(self._h)
+        except Exception:
+            pass
+
+
+def _tr_lib():
+    L = _proto()
+    if not getattr(L, "_tr_ready", False):
+        P = ctypes.c_void_p
+        L.oracle_transcript_new.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+        L.oracle_transcript_new.restype = P
+        L.oracle_transcript_clone.argtypes = [P]
+        L.oracle_transcript_clone.restype = P
+        L.oracle_transcript_free.argtypes = [P]
+        L.oracle_transcript_label.argtypes = [P, ctypes.c_char_p, ctypes.c_size_t]
+        L.oracle_transcript_observe_f128.argtypes = [P, P]
+        L.oracle_transcript_observe_slice.argtypes = [P, P, ctypes.c_size_t]
+        L.oracle_transcript_observe_bytes.argtypes = [P, ctypes.c_char_p, ctypes.c_size_t]
+        L.oracle_transcript_sample.argtypes = [P, P]
+        L.oracle_transcript_sample_vec.argtypes = [P, ctypes.c_size_t, P]
+        L.oracle_prove_tr.argtypes = [P, ctypes.c_size_t, ctypes.c_int, P, P, ctypes.c_size_t,
+                                      ctypes.POINTER(ctypes.c_size_t), P]
+        L.oracle_verify_tr.argtypes = [P, ctypes.c_size_t, ctypes.c_int, P, ctypes.c_char_p, ctypes.c_size_t]
+        L._tr_ready = True
+    return L
+
+
+def prove_with(blocks, n_blocks_log, transcript):
+    """Oracle proof continuing `transcript` (advanced by the call). Returns
+    (bundle bytes, root bytes, claim dict shaped as the GPU binding's)."""
+    L = _tr_lib()
+    blocks = np.ascontiguousarray(blocks)
+    out = np.zeros(4_000_000, np.uint8)
+    ln = ctypes.c_size_t()
+    n_out = n_blocks_log  # m - 14
+    claim = np.zeros(2 * (4 + 16 + 2 * n_out), np.uint64)
+    rc = L.oracle_prove_tr(ptr(blocks), len(blocks), n_blocks_log, transcript._h, ptr(out), out.size,
+                           ctypes.byref(ln), ptr(claim))
+    assert rc == 0, rc
+    f = [(int(claim[2 * i]), int(claim[2 * i + 1])) for i in range(claim.size // 2)]
+    ab_inner, ab_outer = f[4:12], f[12:12 + n_out]
+    c_inner, c_outer = f[12 + n_out:20 + n_out], f[20 + n_out:20 + 2 * n_out]
+    cl = {"ab": {"z_skip": f[0], "x_inner_rest": ab_inner, "x_outer": ab_outer, "value": f[1]},
+          "c": {"z_skip": f[2], "x_inner_rest": c_inner, "x_outer": c_outer, "value": f[3]}}
+    bundle = out[:ln.value].tobytes()
+    return bundle, bundle[7:39], cl
+
+
+def verify_with(proof_bytes, m, transcript):
+    """Oracle verifier continuing `transcript`: (accepted, reason)."""
+    L = _tr_lib()
+    buf = np.frombuffer(proof_bytes, np.uint8).copy()
+    why = ctypes.create_string_buffer(256)
+    rc = L.oracle_verify_tr(ptr(buf), len(proof_bytes), m, transcript._h, why, 256)
+    return rc == 0, why.value.decode()

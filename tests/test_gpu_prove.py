@@ -37,14 +37,54 @@ def test_gpu_proof_deterministic_and_seed_sensitive(cuda_device):
 
 
 def test_ranked_canary_byte_identical(cuda_device):
-    # The reference pins this input's proof at 437,551 bytes; the oracle's
-    # proof (committed digest) has that length and verifies.
+    # The reference pins this input's proof at 437,551 bytes
+    # (reference_pins.json). The oracle's proof, computed here, has that
+    # length, matches the committed oracle digest and verifies; the GPU proof
+    # is byte-equal to it.
     gold = json.load(open(os.path.join(GOLD, "canary_2e18.json")))
+    pins = json.load(open(os.path.join(GOLD, "reference_pins.json")))
     blocks = O.compressions(18, 0, canary=True)
     setup = F.Blake3Setup(1 << 18)
     p = setup.prove_fast(blocks)
-    assert len(p) == gold["reference_expected_proof_bytes"]
-    assert O.b3_hash(p).hex() == gold["oracle_proof_blake3"]
+    ref = O.prove(blocks, 18)
+    assert len(ref) == pins["canary_expected_proof_bytes"] == gold["reference_expected_proof_bytes"]
+    assert O.b3_hash(ref).hex() == gold["oracle_proof_blake3"]
+    assert p == ref
+
+
+def _digests(log2):
+    d = json.load(open(os.path.join(GOLD, "oracle_digests.json")))
+    return {r["seed"]: r for r in d["proofs"] if r["log2"] == log2}
+
+
+def test_config0_proofs_match_oracle(cuda_device):
+    # The reference's CPU-runnable case: 2^14 benchmark compressions per proof
+    # (benchmark-tools/common/src/lib.rs:20-33) for seeds 0..4 and the worker's
+    # warm-up seed (benchmark-tools/worker/src/main.rs:29). Each GPU proof is
+    # byte-equal to the oracle's proof computed here and to the digest of the
+    # oracle proof committed in tests/golden (made on another host).
+    pins = json.load(open(os.path.join(GOLD, "reference_pins.json")))
+    gold = _digests(14)
+    setup = F.Blake3Setup(1 << 14)
+    for seed in [0, 1, 2, 3, 4, pins["worker_warmup_seed"]]:
+        gpu = setup.prove_seed(seed)
+        ref = O.prove(O.compressions(14, seed), 14)
+        assert gpu == ref, f"seed {seed:#x}: GPU proof differs from the oracle's"
+        assert len(gpu) == gold[seed]["bytes"] and O.b3_hash(gpu).hex() == gold[seed]["blake3"]
+    ok, why = O.verify(gpu, 28)
+    assert ok, why
+
+
+def test_ranked_seed_proofs_match_oracle(cuda_device):
+    # The ranked size (2^18 compressions) for benchmark seeds other than the
+    # canary: seed 0 against a live oracle proof, seeds 0 and 1 against the
+    # committed oracle digests.
+    gold = _digests(18)
+    setup = F.Blake3Setup(1 << 18)
+    p0 = setup.prove_seed(0)
+    assert p0 == O.prove(O.compressions(18, 0), 18)
+    for seed, p in [(0, p0), (1, setup.prove_seed(1))]:
+        assert len(p) == gold[seed]["bytes"] and O.b3_hash(p).hex() == gold[seed]["blake3"], f"seed {seed}"
 
 
 def test_device_input_generator_matches_reference_generator(cuda_device):

@@ -16,6 +16,24 @@ def test_ghash_kats():
         assert O.gf_mul((a0, a1), (b0, b1)) == (o0, o1)
 
 
+def test_product_paths_agree():
+    # The oracle multiplies with PMULL on an Arm host with the crypto extension
+    # (as the reference's aarch64 backend, crates/flock-core/src/field/gf2_128/
+    # aarch64.rs:26-60) and with portable integer code elsewhere; both must
+    # give the same products, KATs included.
+    import ctypes
+    L = O.lib()
+    L.oracle_gf_crosscheck.restype = ctypes.c_size_t
+    L.oracle_gf_crosscheck.argtypes = [ctypes.c_size_t, ctypes.c_uint64]
+    L.oracle_gf_mul_portable.argtypes = [ctypes.c_void_p] * 3
+    assert L.oracle_gf_crosscheck(200_000, 11) == 0
+    for a0, a1, b0, b1, o0, o1 in json.load(open(os.path.join(GOLD, "ghash_kat.json"))):
+        out = np.zeros(2, np.uint64)
+        L.oracle_gf_mul_portable(O.ptr(np.array([a0, a1], np.uint64)), O.ptr(np.array([b0, b1], np.uint64)),
+                                 O.ptr(out))
+        assert (int(out[0]), int(out[1])) == (o0, o1)
+
+
 def test_inverse_identities():
     # gf2_128.rs:408-430: a * a^-1 = 1, including top-bit inputs
     for a in [(0, 1 << 63), ((1 << 64) - 1, (1 << 64) - 1), (0, (1 << 64) - 1), (3, 0), (0x1234, 0x5678)]:

@@ -4,6 +4,8 @@ Mirrors the reference's end-to-end tests (crates/flock-prover/src/r1cs_hashes/
 blake3.rs:5006-5100 prove_verify roundtrips at m=22) and its mutation tests
 (zerocheck.rs:1791-2112, lincheck.rs:2444 verify_rejects_mutations).
 """
+import json
+import os
 import struct
 
 import numpy as np
@@ -91,4 +93,34 @@ def test_tamper_rejected(proof, where):
 
 def test_wrong_statement_size_rejected(proof):
     ok, _ = O.verify(proof, 14 + N_LOG + 1)
+    assert not ok
+
+
+@pytest.mark.slow
+@pytest.mark.skipif(os.environ.get("FLOCK_SLOW_TESTS") != "1",
+                    reason="one full 2^18 oracle proof (minutes on a few cores): set FLOCK_SLOW_TESTS=1")
+def test_oracle_canary_proof_has_reference_length():
+    # crates/flock-prover/src/r1cs_hashes/blake3.rs:4910-4939: the proof of the
+    # ranked canary input is EXPECTED_PROOF_BYTES long (reference_pins.json,
+    # extracted from the reference by make_golden.py), and its verifier accepts.
+    gold = os.path.join(os.path.dirname(__file__), "golden")
+    pins = json.load(open(os.path.join(gold, "reference_pins.json")))
+    canary = json.load(open(os.path.join(gold, "canary_2e18.json")))
+    p = O.prove(O.compressions(18, 0, canary=True), 18)
+    assert len(p) == pins["canary_expected_proof_bytes"] == 437_551
+    assert O.b3_hash(p).hex() == canary["oracle_proof_blake3"]
+    ok, why = O.verify(p, 32)
+    assert ok, why
+
+
+def test_prove_with_transcript_matches_default_prove(proof):
+    # a fresh transcript of the benchmark domain is the default proof; the
+    # claim's points have the RowMajor shapes (8 inner, m - 14 outer)
+    t = O.Transcript(b"flock-bench-v0")
+    p, root, claim = O.prove_with(O.compressions(N_LOG, 5), N_LOG, t)
+    assert p == proof and root == proof[7:39]
+    assert len(claim["ab"]["x_inner_rest"]) == 8 and len(claim["c"]["x_outer"]) == N_LOG
+    ok, why = O.verify_with(p, 14 + N_LOG, O.Transcript(b"flock-bench-v0"))
+    assert ok, why
+    ok, _ = O.verify_with(p, 14 + N_LOG, O.Transcript(b"another-domain"))
     assert not ok

@@ -55,3 +55,21 @@ def test_noalloc_ntt_rejects_sizes_above_limit(cuda_device):
     assert L.flock_ntt_noalloc(ctypes.c_void_p(buf.data_ptr()), 17, 3, 0, None) == FLOCK_ERR_LIMIT
     torch.cuda.synchronize()
     assert torch.equal(buf, before)
+
+
+def test_noalloc_ntt_takes_no_device_memory(cuda_device):
+    # The point of the entry point: after a first call of a shape (which loads
+    # its kernels), further calls leave the device's free memory unchanged. A
+    # cudaMalloc on this path would take at least one 2 MiB page.
+    import torch
+    L = _lib()
+    data = _data(14, 5, 21)
+    ptr = ctypes.c_void_p(data.data_ptr())
+    assert L.flock_ntt_noalloc(ptr, 14, 5, 1, None) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        assert L.flock_ntt_noalloc(ptr, 14, 5, 1, None) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
