@@ -26,8 +26,9 @@ forms: the batched form (64 proofs of 2^12..2^18 through the proof server vs
   2^10..2^20 proofs, p50/p99 latency); see flock_challenge_gb300/forms.py.
 
 --impl reference times the CPU oracle (a C++ restatement of the reference
-prover path; the reference's Rust cannot be built here) on all host cores, on
-a bounded sample (2^14-compression proofs, the reference's CPU-runnable case).
+prover path with the reference's PMULL carry-less product on Arm hosts; the
+reference's Rust cannot be built here) on all host cores, on a bounded sample
+of the same workload: a few full proofs of 2^18 compressions.
 Under torchrun (N > 1) each rank proves its own independent batches
 (replicas; proofs never shard) and rank 0 prints the line.
 """
@@ -35,6 +36,7 @@ import argparse
 import ctypes
 import json
 import os
+import statistics
 import subprocess
 import sys
 import threading
@@ -46,20 +48,22 @@ sys.path.insert(0, ROOT)
 METRIC = "verified BLAKE3 compressions/s at 2^18 per proof"
 PUBLISHED = 483866.0  # README.md:110-116, unmodified reference, Apple M4 Pro runner
 
-# dram__bytes_read.sum + dram__bytes_write.sum of the L0 commit NTT passes per
-# launch set, from ncu on a 2^18-position case scaled by positions (traffic
-# grows in proportion): profiles/ntt_pass_l0_2e16.md.
-# DRAM bytes (read + write) per NTT pass at the bench's shape (2^20 positions x
-# 64 lanes): 478.8 MB per pass measured by ncu at 2^18 positions (mean of the
-# eight L0 passes in profiles/ntt_instructions_2e18pos.md), times 4 for 4x the
-# positions.
+# Figures from ncu captures of the same kernels on smaller cases (the capture
+# commands and tables are kept with the other ncu summaries of the project);
+# DRAM traffic and instruction counts grow in proportion to the positions.
+#
+# L0 commit NTT: DRAM bytes (read + write) per pass at 2^18 positions x 64
+# lanes, mean of the eight L0 passes; times 4 for the bench's 2^20 positions.
 NTT_TRAFFIC_PER_PASS = {20: 4 * 478.8e6}
 NTT_MAX_LAYERS = {0: 4, 1: 6, 2: 8}  # layers per pass of the autotuner's pass shapes
 # Thread instructions per GF(2^128) product in the table passes and per
-# butterfly in the multiply passes, measured by ncu on the 2^18-position L0
-# transform (profiles/ntt_instructions_2e18pos.md).
+# butterfly in the multiply passes (2^18-position L0 transform).
 NTT_INSTR_PER_TABLE_PRODUCT = 179
 NTT_INSTR_PER_MULTIPLY_BUTTERFLY = 433
+# Zerocheck round 1 at m = 30 (2^17 outer blocks of 128 rows): warp
+# instructions and DRAM bytes (read + write) of one launch, per outer block.
+ZC1_WARP_INSTR_PER_OUTER = 819868496 / 2**17
+ZC1_DRAM_BYTES_PER_OUTER = (404941056 + 3680768) / 2**17
 
 
 def load_peaks():
@@ -138,8 +142,17 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
-def oracle_baseline(budget_s=20.0, log2=14, gpu_proof=None, gpu_m=None):
-    """CPU oracle proofs of 2^log2 compressions on all host cores (bounded sample).
+def workload_config(log2, ws):
+    """The workload description both arms print (the same dict on each)."""
+    return {"workload": f"one proof of 2^{log2} BLAKE3 compressions per step (m={14 + log2}, rate 1/2, "
+                        "64 lanes, Fast profile, BLAKE3 Merkle + transcript, inputs from the reference "
+                        "generator)",
+            "parallelism": f"replicas x{ws}", "l2": "working set > 5 GB, larger than L2"}
+
+
+def oracle_baseline(log2=18, proofs=2, gpu_proof=None, gpu_m=None):
+    """CPU oracle proofs of 2^log2 compressions on all host cores (bounded
+    sample: `proofs` timed proofs after the setup is cached).
 
     This leg is the only part of the benchmark that runs the oracle: it times
     the oracle prover and, as the checker, runs the oracle verifier on one
@@ -153,21 +166,23 @@ def oracle_baseline(budget_s=20.0, log2=14, gpu_proof=None, gpu_m=None):
         if not ok:
             raise SystemExit(f"GPU proof rejected by the CPU verifier: {why}")
         checked = f"GPU proof of m={gpu_m} ({len(gpu_proof)} bytes) accepted by the CPU verifier"
-    blocks = O.compressions(log2, 0)
-    O.prove(O.compressions(8, 0), 8)  # warm the setup caches (digests) outside the timer
-    t_setup = time.perf_counter()
-    O.prove(blocks, log2)  # untimed warm-up at the sampled size (statement digest)
-    t_setup = time.perf_counter() - t_setup
+    t = time.perf_counter()
+    O.warm(14 + log2)  # base matrices and statement digest, cached as the reference's setup is
+    setup_s = time.perf_counter() - t
     times = []
-    t0 = time.perf_counter()
-    while len(times) < 3 and (time.perf_counter() - t0 < budget_s or not times):
+    for i in range(proofs):
+        blocks = O.compressions(log2, 1_000_000 + i)
         t = time.perf_counter()
-        O.prove(O.compressions(log2, len(times) + 1), log2)
+        O.prove(blocks, log2)
         times.append(time.perf_counter() - t)
-    med = sorted(times)[len(times) // 2]
+    med = statistics.median(times)
+    arith = "PMULL carry-less product (the reference's aarch64 field backend)" if O.uses_pmull() else \
+        "portable carry-less product"
     out = {"value": (1 << log2) / med, "unit": "compressions/s", "cores": cores, "kind": "port",
-           "sample": f"{len(times)} full oracle proofs of 2^{log2} compressions (m={14 + log2}), "
-                     f"median {med:.2f} s, OpenMP on {cores} host threads"}
+           "sample": f"{len(times)} full oracle proofs of 2^{log2} compressions (m={14 + log2}), median "
+                     f"{med:.2f} s per proof ({', '.join(f'{x:.2f}' for x in times)} s), OpenMP on {cores} host "
+                     f"threads, {arith}; setup (matrices + statement digest) {setup_s:.1f} s outside the timer",
+           "seconds_per_proof": times}
     if checked:
         out["gpu_proof_check"] = checked
     return out
@@ -177,12 +192,15 @@ def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    cb = oracle_baseline(budget_s=min(60.0, 15.0 * max(args.steps, 1)))
+    cb = oracle_baseline(log2=args.log2, proofs=args.ref_proofs)
+    med_ms = statistics.median(cb["seconds_per_proof"]) * 1e3
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "compressions/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": med_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": cb["value"] / PUBLISHED,
             "dtype": "u32/gf2_128", "data": "synthetic (reference input generator)",
-            "config": {"workload": "BLAKE3 compression proofs, 2^14 per proof (CPU oracle sample; the 2^18 "
-                                   "ranked size takes minutes on the host)"},
+            "config": workload_config(args.log2, ws),
+            "timed_steps_note": f"each of the {len(cb['seconds_per_proof'])} timed steps is one full CPU proof "
+                                f"of the workload (a bounded sample; --steps does not change it)",
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "compressions/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -246,66 +264,78 @@ def kernel_microbench(F, ctx_handle, peaks, torch, dev, rows_logs=(16, 18, 20), 
     return out
 
 
-def kernel_roofline(F, ctx_handle, stream_ptr, log2, peaks, torch, dev, clock_mhz=None):
-    """Times the dominant kernel family (the L0 commit NTT) alone with CUDA events."""
-    m = 14 + log2
-    log_d = m - 7 - 6 + 1
-    n = 1 << log2
-    d_in = F.generate_inputs(log2, 99, device=dev)
-    z, _, _, _ = F.generate_witness(d_in, n, log2, want_ab=False, want_stripe=False)
-    cw = torch.empty((1 << (log_d + 6)) * 16, dtype=torch.uint8, device=dev)
-    torch.cuda.synchronize()
-    reps = 5
-    s = torch.cuda.Stream(device=dev)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(s):
-        for _ in range(2):
-            F.check(F.lib().flock_ntt(ctx_handle, F._dptr(cw), log_d, 6, 1, ctypes.c_void_p(s.cuda_stream)))
-        e0.record(s)
-        for _ in range(reps):
-            F.check(F.lib().flock_ntt(ctx_handle, F._dptr(cw), log_d, 6, 1, ctypes.c_void_p(s.cuda_stream)))
-        e1.record(s)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / reps
-    F.lib().flock_ntt_tuned_variant.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
-    variant = F.lib().flock_ntt_tuned_variant(dev.index or 0, log_d, 6, 1)
+def ntt_l0_structure(F, dev_index, log_d):
+    """(table passes, total passes, table-pass end layer, multiply-pass shape) of
+    the L0 commit NTT, by the library's rule: two-layer byte-table passes while
+    a block holds >= 2^9 quad-lanes, then multiply passes of the tuned shape."""
+    F.lib().flock_ntt_tuned_variant.argtypes = [ctypes.c_int] * 4
+    variant = F.lib().flock_ntt_tuned_variant(dev_index, log_d, 6, 1)
     max_f = NTT_MAX_LAYERS.get(variant, 6)
-    # byte-table passes of two layers while a block holds >= 2^9 quad-lanes
-    # (the library's rule), then multiply passes of <= max_f layers
     tab_end = 1
     while tab_end + 1 < log_d and log_d - tab_end - 2 + 6 >= 9:
         tab_end += 2
     tab_passes = (tab_end - 1) // 2
     passes = tab_passes + (log_d - tab_end + max_f - 1) // max_f
-    # algorithmic bytes: the first pass reads the 2^(log_d-1) x 64 x 16 B message,
-    # every pass writes the 2^log_d x 64 x 16 B codeword, later passes read it
-    cw = (1 << (log_d + 6)) * 16
-    alg = cw // 2 + cw + (passes - 1) * 2 * cw
-    achieved = alg / (ms * 1e-3) / 1e9
-    muls = (log_d - 1) * (1 << (log_d - 1)) * 64
-    # integer roofline: instruction counts (per product, from ncu) over the
-    # live time, against the SM issue peak (SMs x 4 sub-partitions x 32 lanes)
+    return tab_passes, passes, tab_end, variant, max_f
+
+
+def rooflines(F, log2, span_ms, peaks, sms, clock_mhz, dev_index):
+    """Roofline figures of the proof's main kernels from their CUDA-event times
+    inside the timed proofs (mean over the timed steps, on the prover's stream).
+
+    Algorithmic bytes follow the hot-path measurement rules: the NTT reads the
+    message once and writes the codeword once (16 B x rows x 64 lanes x (1 + 2));
+    zerocheck round 1 reads a, b and z once (3 x 2^m / 8 bytes); the witness
+    writes z, a, b and the stripe (4 x 2,048 B) and reads 112 B per compression.
+    `traffic` is the ncu DRAM traffic per launch (set) scaled to this size;
+    `integer_frac` is thread instructions (ncu counts) over the same time
+    against the SM issue peak, SMs x 4 x 32 lanes x SM clock."""
+    m = 14 + log2
+    log_d = m - 7 - 6 + 1
+    hbm = peaks["hbm_gbs"]
+    clock = clock_mhz or peaks.get("sm_max_mhz", 2070.0)
+    issue_peak = sms * 4 * 32 * clock * 1e6
+    out = {}
+    # L0 commit NTT
+    ms = span_ms["l0_ntt"]
+    tab_passes, passes, tab_end, variant, max_f = ntt_l0_structure(F, dev_index, log_d)
+    msg = (1 << (log_d - 1)) * 64 * 16
+    alg = msg + 2 * msg  # message read once + codeword written once
+    traffic = passes * NTT_TRAFFIC_PER_PASS[log_d] if log_d in NTT_TRAFFIC_PER_PASS else None
+
     def products(l):  # butterflies of layer l with a product (block 0 skips it)
         return ((1 << (log_d - 1)) - (1 << (log_d - l - 1))) * 64
     ins = (sum(products(l) for l in range(1, tab_end)) * NTT_INSTR_PER_TABLE_PRODUCT
            + sum(products(l) for l in range(tab_end, log_d)) * NTT_INSTR_PER_MULTIPLY_BUTTERFLY)
-    sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    issue_peak = sms * 4 * 32 * (clock_mhz or 2070.0) * 1e6
-    return {"kernel": f"L0 commit NTT (layers 1..{log_d - 1}: {tab_passes} two-layer table passes, then "
-                      f"{passes - tab_passes} multiply pass(es) of <= {max_f} layers)",
-            "bound": "hbm",
-            "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-            "traffic": (passes * NTT_TRAFFIC_PER_PASS[log_d]) if log_d in NTT_TRAFFIC_PER_PASS else None,
-            "algorithmic_bytes_per_set": alg, "pass_shape": variant,
-            "ms_per_launch_set": ms, "gf128_muls_per_s": muls / (ms * 1e-3),
-            "integer": {"achieved": ins / (ms * 1e-3) / 1e12, "peak": issue_peak / 1e12, "unit": "T thread-instr/s",
-                        "frac": ins / (ms * 1e-3) / issue_peak, "instructions_per_set": ins,
-                        "note": "instructions per product from ncu (profiles/ntt_instructions_2e18pos.md) times "
-                                "the set's products, over the live time; peak = SMs x 4 x 32 lanes x SM clock"},
-            "note": "the passes are bound by the integer pipes (byte-table lookups in the upper layers, "
-                    "carry-less multiplies below), not HBM: see profiles/ntt_pass_l0_2e16.md and "
-                    "profiles/ntt_tab_pass_l0_2e16.md"}
+    muls = sum(products(l) for l in range(1, log_d))
+    out["l0_ntt"] = {
+        "kernel": f"L0 commit NTT, layers 1..{log_d - 1} of 2^{log_d} positions x 64 lanes ({tab_passes} two-layer "
+                  f"table passes, then {passes - tab_passes} multiply pass(es) of <= {max_f} layers)",
+        "bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+        "frac": alg / (ms * 1e-3) / 1e9 / hbm, "traffic": traffic,
+        "algorithmic_bytes": alg, "traffic_over_algorithmic": (traffic / alg) if traffic else None,
+        "integer_frac": ins / (ms * 1e-3) / issue_peak, "integer_achieved_tips": ins / (ms * 1e-3) / 1e12,
+        "integer_peak_tips": issue_peak / 1e12, "ms_per_launch_set": ms, "passes": passes,
+        "gf128_products_per_s": muls / (ms * 1e-3), "pass_shape": variant}
+    # zerocheck round 1
+    ms = span_ms["zerocheck_round1"]
+    n_outer = (1 << m) // 64 // 128
+    alg = 3 * (1 << m) // 8
+    ins = ZC1_WARP_INSTR_PER_OUTER * 32 * n_outer
+    traffic = ZC1_DRAM_BYTES_PER_OUTER * n_outer
+    out["zerocheck_round1"] = {
+        "kernel": f"zerocheck univariate-skip round 1 over 2^{m - 6} rows of a, b, z",
+        "bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+        "frac": alg / (ms * 1e-3) / 1e9 / hbm, "traffic": traffic, "algorithmic_bytes": alg,
+        "traffic_over_algorithmic": traffic / alg, "integer_frac": ins / (ms * 1e-3) / issue_peak,
+        "integer_achieved_tips": ins / (ms * 1e-3) / 1e12, "ms_per_launch": ms}
+    # witness
+    ms = span_ms["witness"]
+    alg = (1 << log2) * (112 + 4 * 2048)
+    out["witness"] = {"kernel": f"witness z, a, b and lincheck stripe of 2^{log2} compressions", "bound": "hbm",
+                      "achieved": alg / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                      "frac": alg / (ms * 1e-3) / 1e9 / hbm, "algorithmic_bytes": alg, "ms_per_launch": ms}
+    return out
 
 
 def run_chain(F, setup, log2, reps=5):
@@ -334,6 +364,8 @@ def run_chain(F, setup, log2, reps=5):
 
 
 def run_gpu(args):
+    import statistics
+
     import numpy as np
     import torch
     import flock_challenge_gb300 as F
@@ -353,7 +385,6 @@ def run_gpu(args):
     # run on the device; host copies (pinned) feed the end-to-end leg
     d_seeded = [F.generate_inputs(log2, 1000 * rank + i, device=dev) for i in range(nseeds)]
     host = [d.cpu().pin_memory() for d in d_seeded]
-    d_ins = d_seeded[:2]
     L = F._proto_lib()
     obuf = np.zeros(1 << 20, np.uint8)
 
@@ -364,43 +395,44 @@ def run_gpu(args):
                               obuf.ctypes.data_as(ctypes.c_void_p), obuf.size, ctypes.byref(ln)), "flock_prove")
         return ln.value
 
-    def prove_dev(d_in):
-        return setup.prove_device(d_in)
-
-    # warm-up (untimed, like the reference worker's fixed-seed proof)
-    for i in range(max(args.warmup, 3)):
-        prove_dev(d_ins[i % 2])
-    first = prove_dev(d_ins[0])
-    second = prove_dev(d_ins[1])
+    # warm-up (untimed, like the reference worker's fixed-seed proof), then the
+    # proof of every step's input, against which the timed proofs are checked
+    for i in range(args.warmup):
+        setup.prove_device(d_seeded[i % nseeds])
+    expected = [setup.prove_device(d) for d in d_seeded]
     # the host-buffer and seed paths warm up too (their staging buffers; each
     # pinned input buffer once)
     for h in host:
         prove_host(h)
     setup.prove_seed(999_999)
+    setup.set_kernel_timing(True)
     torch.cuda.synchronize()
     if ws > 1:
         torch.distributed.barrier()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    spans = []
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         launches0 = F.kernel_launches()
-        e0.record(stream)
+        ev[0].record(stream)
         for i in range(args.steps):
-            p = prove_dev(d_ins[i % 2])
-            assert p == (first if i % 2 == 0 else second)  # deterministic, full-length proof bytes
-        e1.record(stream)
+            p = setup.prove_device(d_seeded[i])
+            ev[i + 1].record(stream)
+            spans.append(setup.kernel_times())
+            assert p == expected[i]  # deterministic, full-length proof bytes of this step's input
         torch.cuda.synchronize()
         launches = F.kernel_launches() - launches0
-        dev_ms = e0.elapsed_time(e1) / args.steps
+        step_ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
+        dev_ms = ev[0].elapsed_time(ev[-1]) / args.steps
         phases = setup.phase_times()
+        setup.set_kernel_timing(False)
         # End to end through the public C ABI with host buffers.
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         sizes, e2e_steps = [], []
         for i in range(args.steps):
             ts = time.perf_counter()
-            sizes.append(prove_host(host[i % len(host)]))
+            sizes.append(prove_host(host[i]))
             e2e_steps.append((time.perf_counter() - ts) * 1e3)
         torch.cuda.synchronize()
         e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
@@ -411,45 +443,57 @@ def run_gpu(args):
             setup.prove_seed(1000 * rank + i)
         torch.cuda.synchronize()
         seed_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    if sizes != [len(e) for e in expected]:
+        raise SystemExit("an end-to-end proof differs in length from the device-input proof of the same seed")
     # every timed proof checked by the device-accelerated verifier (outside the timer)
     t0 = time.perf_counter()
-    verified = F.verify(first, ctx=setup.ctx) and F.verify(second, ctx=setup.ctx)
-    verify_ms = (time.perf_counter() - t0) * 1e3 / 2
+    verified = all(F.verify(p, ctx=setup.ctx) for p in expected)
+    verify_ms = (time.perf_counter() - t0) * 1e3 / len(expected)
     if not verified:
         raise SystemExit("a timed proof was rejected by flock_verify")
     peaks, src = load_peaks()
-    roof = kernel_roofline(F, setup.ctx.handle, None, log2, peaks, torch, dev, clk.summary().get("sm_mhz"))
-    roof["peak_source"] = src
+    span_mean = {k: statistics.fmean(s[k] for s in spans) for k in F.KERNEL_SPANS}
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    roofs = rooflines(F, log2, span_mean, peaks, sms, clk.summary().get("sm_mhz"), dev.index or 0)
     dev_ms, e2e_ms, seed_ms = max_over_ranks([dev_ms, e2e_ms, seed_ms], ws, device=dev)
     if rank == 0:
         total = n * ws
+        med_ms = statistics.median(step_ms)
+        roof = dict(roofs["l0_ntt"])
+        roof["peak_source"] = f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else src
         line = {
             "metric": METRIC, "value": job_throughput(n, ws, dev_ms), "unit": "compressions/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": (total / (dev_ms * 1e-3)) / PUBLISHED,
-            "dtype": "u32/gf2_128", "data": "synthetic (reference input generator, per-step seeds)",
-            "config": {"workload": f"one proof of 2^{log2} BLAKE3 compressions per step (m={14 + log2}, "
-                                   "rate 1/2, 64 lanes, Fast profile, BLAKE3 Merkle + transcript)",
-                       "parallelism": f"replicas x{ws}", "l2": "working set > 5 GB, larger than L2",
-                       "proof_bytes": len(first), "verified": "a GPU proof accepted by the CPU verifier (see "
-                                                              "cpu_baseline); every timed proof byte-equal to "
-                                                              "its re-proof",
-                       "phase_ms_last_proof": {k: round(v, 3) for k, v in phases.items()}},
+            "dtype": "u32/gf2_128", "data": "synthetic (reference input generator, one seed per step)",
+            "config": workload_config(log2, ws),
+            "median": {"ms_per_step": med_ms, "value": job_throughput(n, ws, med_ms),
+                       "note": "the reference's score is 2^18 / median trial time"},
+            "step_ms": [round(x, 3) for x in step_ms],
+            "proof": {"bytes_first_step": len(expected[0]),
+                      "verified": "every timed proof byte-equal to the untimed proof of the same input and "
+                                  "accepted by flock_verify; one also by the CPU verifier (cpu_baseline)",
+                      "phase_ms_last_proof": {k: round(v, 3) for k, v in phases.items()},
+                      "kernel_ms_mean": {k: round(v, 4) for k, v in span_mean.items()}},
             "e2e": {"value": job_throughput(n, ws, e2e_ms), "unit": "compressions/s", "h2d_bytes_per_step": n * 112,
-                    "d2h_bytes_per_step": len(first), "step_ms": [round(x, 3) for x in e2e_steps]},
+                    "d2h_bytes_per_step": len(expected[0]), "step_ms": [round(x, 3) for x in e2e_steps],
+                    "median_ms": statistics.median(e2e_steps)},
             "e2e_seed_to_proof": {"value": job_throughput(n, ws, seed_ms), "unit": "compressions/s",
-                                  "h2d_bytes_per_step": 8, "d2h_bytes_per_step": len(first),
+                                  "h2d_bytes_per_step": 8, "d2h_bytes_per_step": len(expected[0]),
                                   "note": "seed in, inputs generated on the device, proof bytes out"},
             "verify": {"impl": "flock_verify (host transcript + device kernels)", "ms_per_proof": verify_ms,
-                       "accepted": verified, "note": "the timed steps alternate two inputs; both proofs verified"},
+                       "accepted": verified, "proofs": len(expected)},
             "gpu_launches": int(launches),
             "roofline": roof,
+            "roofline_kernels": roofs,
             "clocks": clk.summary(),
         }
         if ws == 1:
             line["chain"] = run_chain(F, setup, log2)
-            line["kernel_microbench"] = kernel_microbench(F, setup.ctx.handle, peaks, torch, dev)
-        line["cpu_baseline"] = oracle_baseline(budget_s=20.0, gpu_proof=first, gpu_m=14 + log2)
+            line["kernel_microbench"] = kernel_microbench(F, setup.ctx.handle, peaks, torch, dev,
+                                                          rows_logs=tuple(args.micro_rows))
+        line["cpu_baseline"] = oracle_baseline(log2=log2, proofs=args.cpu_proofs, gpu_proof=expected[0],
+                                               gpu_m=14 + log2)
         if args.forms and ws == 1:
             from flock_challenge_gb300 import forms
             plain = forms.PlainProver()
@@ -470,6 +514,10 @@ def main():
     ap.add_argument("--forms", dest="forms", action="store_true", default=True,
                     help="also measure the batched and served forms (default)")
     ap.add_argument("--no-forms", dest="forms", action="store_false")
+    ap.add_argument("--cpu-proofs", type=int, default=2, help="timed CPU oracle proofs in the cpu_baseline leg")
+    ap.add_argument("--ref-proofs", type=int, default=3, help="timed CPU oracle proofs of the reference arm")
+    ap.add_argument("--micro-rows", type=int, nargs="*", default=[16, 18, 20, 22],
+                    help="log2 rows of the kernel microbench (256 columns, rate 1/4)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
