@@ -1,10 +1,11 @@
 """Generates the Ligerito parameter tables from the reference's embedded TOMLs.
 
+Usage: python oracle/gen_ligerito_params.py REFERENCE_ROOT
+
 Reads crates/flock-core/configs/ligerito/m{22..35}_{fast,slim,secure}.toml of
-the reference tree (argv[1], default /root/reference) and writes the same
-numbers as C initializers into
-  oracle/ligerito_params.inc                      (oracle copy)
-  flock_challenge_gb300/csrc/ligerito_params.inc  (product copy)
+the reference tree (REFERENCE_ROOT, required) and writes the same numbers as C
+initializers into flock_challenge_gb300/csrc/ligerito_params.inc, which both
+the product library and the oracle include.
 Row: m, profile (0 fast, 1 slim, 2 secure), initial_k, yr_log_n, n_levels,
 then per level {log_inv_rate, log_msg_cols, log_num_interleaved, k_recursive,
 queries, grinding_bits, fold_grinding_bits, ood_samples}.
@@ -15,7 +16,9 @@ import os
 import re
 import sys
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    raise SystemExit(__doc__)
+ref = sys.argv[1]
 here = os.path.dirname(os.path.abspath(__file__))
 cfg_dir = os.path.join(ref, "crates/flock-core/configs/ligerito")
 KEYS = ["log_inv_rate", "log_msg_cols", "log_num_interleaved", "k_recursive", "queries", "grinding_bits",
@@ -53,7 +56,6 @@ for m, pi, k, yr, lv in rows:
     out.append("  {" + ", ".join(map(str, flat)) + "},")
 out.append("};")
 text = "\n".join(out) + "\n"
-for dst in [os.path.join(here, "ligerito_params.inc"),
-            os.path.join(os.path.dirname(here), "flock_challenge_gb300", "csrc", "ligerito_params.inc")]:
+for dst in [os.path.join(os.path.dirname(here), "flock_challenge_gb300", "csrc", "ligerito_params.inc")]:
     open(dst, "w").write(text)
     print("wrote", dst, len(rows), "configs")

@@ -713,7 +713,8 @@ static std::vector<F128> claim_weights(F128 z_skip, F128 x0) {
 // Ligerito
 // ============================================================================
 bool ligerito_config(int m, int profile, LigConfig& c) {
-#include "ligerito_params.inc"
+// the parameter table generated from the reference TOMLs, shared with the product library
+#include "../flock_challenge_gb300/csrc/ligerito_params.inc"
   for (int i = 0; i < LIGERITO_N_CONFIGS; i++) {
     const int* row = LIGERITO_CONFIGS[i];
     if (row[0] != m || row[1] != profile) continue;
