@@ -17,6 +17,9 @@
 namespace {
 
 constexpr int LG_THREADS = 256;
+#ifndef LG_MIN_BLOCKS
+#define LG_MIN_BLOCKS 2  // resident blocks per SM of the fold/message kernels
+#endif
 
 __device__ __forceinline__ void block_reduce_write(gf256 a, gf256 b, gf256 c, gf128* out) {
   __shared__ gf256 red[3][LG_THREADS / 32];
@@ -43,7 +46,7 @@ __device__ __forceinline__ void block_reduce_write(gf256 a, gf256 b, gf256 c, gf
 // message over the n_out-element state. Partials: (u0, u2, 0) per block.
 // use_tab: the fold multiplies through r's byte tables (gf_tab.cuh, dynamic
 // shared memory), worth their build when a CTA folds hundreds of pairs.
-__global__ void __launch_bounds__(LG_THREADS, 2)
+__global__ void __launch_bounds__(LG_THREADS, LG_MIN_BLOCKS)
 lig_fold_msg_kernel(const gf128* __restrict__ f, const gf128* __restrict__ b, size_t n_out, int fold,
                     const __grid_constant__ gf128p r, const gf128 r_plain, int use_tab,
                     gf128* __restrict__ fo, gf128* __restrict__ bo, gf128* __restrict__ partials) {

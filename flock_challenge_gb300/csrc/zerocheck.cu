@@ -28,7 +28,10 @@
 
 namespace {
 
-constexpr int R1_THREADS = 384;
+#ifndef ZC1_THREADS
+#define ZC1_THREADS 384
+#endif
+constexpr int R1_THREADS = ZC1_THREADS;  // 12 warps, one block per SM
 #ifndef ZC1_PAR_UNROLL
 #define ZC1_PAR_UNROLL 1
 #endif
@@ -178,6 +181,18 @@ __device__ __forceinline__ gf128 acc9_reduce(const Acc9& a) {
   return r;
 }
 
+// One 16-byte shared-memory load as a single 128-bit access. The extension
+// lookups below are conflict-free only as 128-bit accesses (quarter-warp
+// phases over eight distinct bank groups); split into two 64-bit loads, a
+// half-warp phase would pair lanes l and l + 8 on the same banks.
+__device__ __forceinline__ uint4 lds128(const uint4* p) {
+  uint4 v;
+  asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "r"((uint32_t)__cvta_generic_to_shared(p)));
+  return v;
+}
+
 __device__ __forceinline__ uint64_t shfl_xor64(uint64_t v, int m) {
   const uint32_t lo = __shfl_xor_sync(0xffffffffu, (uint32_t)v, m);
   const uint32_t hi = __shfl_xor_sync(0xffffffffu, (uint32_t)(v >> 32), m);
@@ -275,7 +290,7 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
           const uint4* pb = ext + ((((uint32_t)(rb >> (8 * c))) & 255) << 3) + c;
 #pragma unroll
           for (int q = 0; q < 4; q++) {
-            uint4 va = pa[q * 2048], vb = pb[q * 2048];
+            const uint4 va = lds128(pa + q * 2048), vb = lds128(pb + q * 2048);
             ea[2 * q] ^= ((uint64_t)va.y << 32) | va.x;
             ea[2 * q + 1] ^= ((uint64_t)va.w << 32) | va.z;
             eb[2 * q] ^= ((uint64_t)vb.y << 32) | vb.x;
