@@ -185,6 +185,26 @@ __device__ __forceinline__ gf256 gf_mul_wide_p(gf128 a, const gf128p& p) {
   return o;
 }
 __device__ __forceinline__ gf128 gf_mul_p(gf128 a, const gf128p& p) { return gf256_reduce(gf_mul_wide_p(a, p)); }
+
+// a * b for a multiplier below 2^32, from the masks of its low word (m[0] of
+// its prepared form): four 32-bit products, a 160-bit result.
+__device__ __forceinline__ gf128 gf_mul_p32(gf128 a, uint4 m0) {
+  const uint64_t p0 = clmul32_p(a.w[0], m0), p1 = clmul32_p(a.w[1], m0);
+  const uint64_t p2 = clmul32_p(a.w[2], m0), p3 = clmul32_p(a.w[3], m0);
+  return gf_reduce(p0 ^ (p1 << 32), (p1 >> 32) ^ p2 ^ (p3 << 32), p3 >> 32, 0);
+}
+
+// a * b for a multiplier below 2^64, from m[0..2] of its prepared form (the
+// masks of b0, b1, b0 ^ b1): a's two 64-bit halves times b by Karatsuba over
+// 32-bit words, six 32-bit products, a 192-bit result.
+__device__ __forceinline__ gf128 gf_mul_p64(gf128 a, uint4 m0, uint4 m1, uint4 m2) {
+  const uint64_t ll = clmul32_p(a.w[0], m0), lh = clmul32_p(a.w[1], m1);
+  const uint64_t lm = clmul32_p(a.w[0] ^ a.w[1], m2) ^ ll ^ lh;
+  const uint64_t hl = clmul32_p(a.w[2], m0), hh = clmul32_p(a.w[3], m1);
+  const uint64_t hm = clmul32_p(a.w[2] ^ a.w[3], m2) ^ hl ^ hh;
+  const uint64_t l0 = ll ^ (lm << 32), l1 = lh ^ (lm >> 32), h0 = hl ^ (hm << 32), h1 = hh ^ (hm >> 32);
+  return gf_reduce(l0, l1 ^ h0, h1, 0);
+}
 __device__ __forceinline__ gf128p gf_load_p(const gf128p* q) {
   gf128p p;
 #pragma unroll

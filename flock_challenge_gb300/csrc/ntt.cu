@@ -94,7 +94,7 @@ __host__ __device__ constexpr int rotr_bits(int j, int r) {
 template <int F, int TL, bool PREP, int V>
 __global__ void __launch_bounds__(PassShape<F, TL, V>::THREADS, PassShape<F, TL, V>::MIN_BLOCKS)
 ntt_pass_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t src_pos_mask,
-                const void* __restrict__ tw_any, int log_d, int log_lanes, int l0) {
+                const void* __restrict__ tw_any, int log_d, int log_lanes, int l0, int narrow) {
   using S = PassShape<F, TL, V>;
   constexpr int E = S::E, K1 = S::K1, K2 = S::K2, NE = 1 << E, H = NE / 2;
   extern __shared__ gf128 tile[];
@@ -143,12 +143,36 @@ ntt_pass_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t s
       // at the empty sum; all other blocks are non-zero): its butterflies
       // need no product. Blocks are uniform over a tile, so the test rarely
       // diverges.
+      // The deepest layers' twiddles are narrow (layer d-1 below 2^d, layer
+      // d-2 below 2^(2d-3)): from layer narrow & 255 on they fit 32 bits,
+      // from layer narrow >> 8 on 64 bits (the host reads both bounds off the
+      // table), and their products take four or six 32-bit products instead
+      // of nine. The class is uniform over a layer.
       const gf128p* twl = reinterpret_cast<const gf128p*>(tw_any) + twb;
       const bool hi0 = hi == 0;
+      const int layer = l0 + t;
+      const int wcls = layer >= (narrow & 255) ? 1 : layer >= (narrow >> 8) ? 2 : 0;
+      if (wcls == 1) {
 #pragma unroll
-      for (int j = 0; j < H; j++) {
-        if (!(hi0 && ti[j] == 0)) y[j] = gf_add(y[j], gf_mul_p(y[j + H], gf_load_p(&twl[ti[j]])));
-        y[j + H] = gf_add(y[j + H], y[j]);
+        for (int j = 0; j < H; j++) {
+          if (!(hi0 && ti[j] == 0)) y[j] = gf_add(y[j], gf_mul_p32(y[j + H], twl[ti[j]].m[0]));
+          y[j + H] = gf_add(y[j + H], y[j]);
+        }
+      } else if (wcls == 2) {
+#pragma unroll
+        for (int j = 0; j < H; j++) {
+          if (!(hi0 && ti[j] == 0)) {
+            const gf128p* q = &twl[ti[j]];
+            y[j] = gf_add(y[j], gf_mul_p64(y[j + H], q->m[0], q->m[1], q->m[2]));
+          }
+          y[j + H] = gf_add(y[j + H], y[j]);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < H; j++) {
+          if (!(hi0 && ti[j] == 0)) y[j] = gf_add(y[j], gf_mul_p(y[j + H], gf_load_p(&twl[ti[j]])));
+          y[j + H] = gf_add(y[j + H], y[j]);
+        }
       }
     } else {
       const gf128* twl = reinterpret_cast<const gf128*>(tw_any) + twb;
@@ -182,7 +206,9 @@ ntt_pass_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t s
 // Twiddle table of the standard basis {1, x, ..., x^(d-1)}:
 // normalized subspace-polynomial evaluations (additive_ntt_f128.rs:57-88),
 // expanded breadth-first (additive_ntt_f128.rs:106-129).
-std::vector<hf::F> host_twiddles(int d) {
+// Generator rows of the twiddle table: layer l's twiddles are the subset sums
+// of rows[d - l - 1][1 .. l].
+std::vector<std::vector<hf::F>> twiddle_rows(int d) {
   std::vector<std::vector<hf::F>> ev(d);
   for (int i = 0; i < d; i++) ev[0].push_back(i < 64 ? hf::F(1ULL << i, 0) : hf::F(0, 1ULL << (i - 64)));
   for (int i = 1; i < d; i++)
@@ -191,6 +217,11 @@ std::vector<hf::F> host_twiddles(int d) {
     hf::F iv = hf::inv(row[0]);
     for (auto& v : row) v = v * iv;
   }
+  return ev;
+}
+
+std::vector<hf::F> host_twiddles(int d) {
+  const std::vector<std::vector<hf::F>> ev = twiddle_rows(d);
   std::vector<hf::F> tw;
   tw.reserve(((size_t)1 << d) - 1);
   for (int layer = 0; layer < d; layer++) {
@@ -208,9 +239,38 @@ std::vector<hf::F> host_twiddles(int d) {
 std::mutex g_tw_mu;
 std::map<std::pair<int, int>, void*> g_tw;  // (device, log_d) -> device table
 
+// (w64 << 8) | w32: the first layers from which every twiddle of a transform
+// of 2^log_d positions is below 2^32 and below 2^64, read off the table
+// (the normalized subspace polynomials of the deepest layers have low degree:
+// layer d-1 below 2^d, layer d-2 below 2^(2d-3)). Cached per log_d.
+int flock_ntt_narrow_layers(int log_d) {
+  static std::mutex mu;
+  static std::map<int, int> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(log_d);
+  if (it != cache.end()) return it->second;
+  // a bit is set in some subset sum of a layer's generators iff it is set in
+  // one of the generators, so the OR of the generators bounds the layer
+  const std::vector<std::vector<hf::F>> ev = twiddle_rows(log_d);
+  int w32 = log_d, w64 = log_d;
+  for (int layer = log_d - 1; layer >= 0; layer--) {
+    uint64_t or_lo = 0, or_hi = 0;
+    const auto& row = ev[log_d - layer - 1];
+    for (int bit = 0; bit < layer; bit++) {
+      or_lo |= row[bit + 1].lo;
+      or_hi |= row[bit + 1].hi;
+    }
+    if (or_hi != 0) break;
+    w64 = layer;
+    if ((or_lo >> 32) == 0 && w32 == layer + 1) w32 = layer;
+  }
+  return cache[log_d] = (w64 << 8) | w32;
+}
+
 template <int F, bool PREP, int V>
 int launch_pass(gf128* dst, const gf128* src, size_t mask, const void* tw, int log_d, int log_lanes, int l0,
                 cudaStream_t st) {
+  const int narrow = PREP ? flock_ntt_narrow_layers(log_d) : (log_d << 8) | log_d;
   if constexpr (F > variant_max_layers(V)) {
     return FLOCK_ERR_SHAPE;
   } else {
@@ -224,7 +284,7 @@ int launch_pass(gf128* dst, const gf128* src, size_t mask, const void* tw, int l
         static_assert(S::SMEM <= 48 * 1024, "one-stage passes use no tile");
         size_t blocks = tiles * ((1 << log_lanes) / 32);
         ntt_pass_kernel<F, 32, PREP, V>
-            <<<(unsigned)blocks, S::THREADS, S::SMEM, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
+            <<<(unsigned)blocks, S::THREADS, S::SMEM, st>>>(dst, src, mask, tw, log_d, log_lanes, l0, narrow);
         flock_count_launch();
         return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
       }
@@ -239,12 +299,12 @@ int launch_pass(gf128* dst, const gf128* src, size_t mask, const void* tw, int l
         });
       }
       ntt_pass_kernel<F, 16, PREP, V>
-          <<<(unsigned)blocks, S::THREADS, S::SMEM, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
+          <<<(unsigned)blocks, S::THREADS, S::SMEM, st>>>(dst, src, mask, tw, log_d, log_lanes, l0, narrow);
     } else {
       using S = PassShape<F, 8, V>;
       size_t blocks = tiles * ((1 << log_lanes) / 8);
       ntt_pass_kernel<F, 8, PREP, V>
-          <<<(unsigned)blocks, S::THREADS, S::SMEM, st>>>(dst, src, mask, tw, log_d, log_lanes, l0);
+          <<<(unsigned)blocks, S::THREADS, S::SMEM, st>>>(dst, src, mask, tw, log_d, log_lanes, l0, narrow);
     }
     flock_count_launch();
     return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
