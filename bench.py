@@ -498,7 +498,7 @@ def run_gpu(args):
             from flock_challenge_gb300 import forms
             plain = forms.PlainProver()
             line["forms"] = {"batched": forms.run_batched(64, 4, plain=plain),
-                             "serving": forms.run_serving((8.0, 24.0, 40.0), 60, 4, plain=plain)}
+                             "serving": forms.run_serving((0.9, 1.0, 1.05, 1.1), 200, 4, plain=plain)}
         print(json.dumps(line))
     if ws > 1:
         torch.distributed.destroy_process_group()
