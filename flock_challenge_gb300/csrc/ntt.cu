@@ -31,7 +31,6 @@
 #include "flock_internal.h"
 #include "gf128.cuh"
 #include "gf_tab.cuh"
-#include "cp_async.cuh"
 #include "host_field.h"
 
 namespace {
@@ -371,8 +370,7 @@ constexpr int kMaxPassLayers = variant_max_layers(kDefaultVariant);
 // positions of one lane.
 constexpr int TAB_THREADS = 512;
 constexpr int TAB_ENTRIES = GF_TAB_ENTRIES;
-// three byte tables, then a prefetch slot of one quad (4 x 16 B) per thread
-constexpr size_t TAB_SMEM = (size_t)3 * TAB_ENTRIES * 16 + (size_t)4 * TAB_THREADS * 16;
+constexpr size_t TAB_SMEM = (size_t)3 * TAB_ENTRIES * 16;  // three byte tables
 static_assert(TAB_SMEM <= 232448, "table pass shared memory above the 227 KB per-block limit");
 
 
@@ -392,7 +390,7 @@ __device__ void build_tabs3(const gf128 t[3], uint4* __restrict__ T) {
 __global__ void __launch_bounds__(TAB_THREADS, 1)
 ntt_tab2_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t src_pos_mask,
                 const gf128* __restrict__ tw, int log_d, int log_lanes, int l, int cph) {
-  extern __shared__ uint4 tabs[];  // [3][TAB_ENTRIES], then the prefetch slots [4][TAB_THREADS]
+  extern __shared__ uint4 tabs[];  // [3][TAB_ENTRIES]
   const size_t hi = blockIdx.x / cph;
   const int part = blockIdx.x % cph;
   const gf128 t3[3] = {tw[((size_t)1 << l) - 1 + hi], tw[((size_t)1 << (l + 1)) - 1 + 2 * hi],
@@ -405,35 +403,29 @@ ntt_tab2_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t s
   const size_t nl = (size_t)1 << log_lanes;
   const size_t items = ((size_t)1 << lo_bits) << log_lanes;
   const uint32_t rot = threadIdx.x & 15;
-  // The next quad is fetched into this thread's slot (cp.async) while the
-  // current one is computed: with three 64 KiB tables an SM holds 16 warps,
-  // too few to hide the global-load latency otherwise. Each quad is read and
-  // written by one thread only, so the prefetch is safe in place (dst == src).
-  // The slot's reads for the current quad are issued before the copies into
-  // it (the asm's memory clobber keeps that order), and a copy writes the
-  // slot only when its global read returns.
-  uint4* slot = tabs + 3 * TAB_ENTRIES + threadIdx.x;  // entry b at slot[b * TAB_THREADS]
+  // The next quad is loaded into registers while the current one is computed:
+  // with three 64 KiB tables an SM holds 16 warps, too few to hide the global
+  // load latency otherwise (measured 1% faster than staging the quad through
+  // shared memory with cp.async, whose 32 bytes of shared traffic per element
+  // compete with the table lookups). Each quad is read and written by one
+  // thread only, so the prefetch is safe in place (dst == src).
+  const size_t stride = (size_t)cph * TAB_THREADS;
+  size_t it = (size_t)part * TAB_THREADS + threadIdx.x;
+  uint4 nx[4];
   auto prefetch = [&](size_t it2) {
     const size_t lane2 = it2 & (nl - 1), lo2 = it2 >> log_lanes;
     const size_t q0 = (hi << (lo_bits + 2)) | lo2;
 #pragma unroll
     for (int b = 0; b < 4; b++)
-      cp_async16(slot + b * TAB_THREADS, &src[((q0 | ((size_t)b << lo_bits)) & src_pos_mask) * nl + lane2]);
-    cp_async_commit();
+      nx[b] = *reinterpret_cast<const uint4*>(&src[((q0 | ((size_t)b << lo_bits)) & src_pos_mask) * nl + lane2]);
   };
-  const size_t stride = (size_t)cph * TAB_THREADS;
-  size_t it = (size_t)part * TAB_THREADS + threadIdx.x;
   if (it < items) prefetch(it);
   for (; it < items; it += stride) {
     const size_t lane = it & (nl - 1), lo = it >> log_lanes;
     const size_t p0 = (hi << (lo_bits + 2)) | lo;
-    cp_async_wait_all();
     gf128 y[4];
 #pragma unroll
-    for (int b = 0; b < 4; b++) {
-      const uint4 v = slot[b * TAB_THREADS];
-      y[b] = gf128{{v.x, v.y, v.z, v.w}};
-    }
+    for (int b = 0; b < 4; b++) y[b] = gf128{{nx[b].x, nx[b].y, nx[b].z, nx[b].w}};
     if (it + stride < items) prefetch(it + stride);
     // layer l: pairs (b, b + 2) with t_A
     if (!za) {
