@@ -52,6 +52,12 @@ int flock_launch_lc_quirky_eq(const void* lag, const void* x_rest, int n_rest, v
 
 // scratch: 32 x 128 F128 of partial sums
 int flock_launch_shv_from_zvec(const void* zvec, const void* eq_tail, void* scratch, void* out, cudaStream_t st);
+// The combined basis fused with the first Ligerito message over (f, b):
+// partials (u0, u2, 0) per block, flock_combined_basis_msg_grid(n, lo_bits) blocks.
+int flock_combined_basis_msg_grid(size_t n, int lo_bits);
+int flock_launch_combined_basis_msg(size_t n, const void* t0_lo, const void* t0_hi, const void* t1_lo,
+                                    const void* t1_hi, int lo_bits, const void* w, const void* f, void* b,
+                                    void* partials, cudaStream_t st);
 int flock_launch_combined_basis(size_t n, const void* t0_lo, const void* t0_hi, const void* t1_lo,
                                 const void* t1_hi, int lo_bits, const void* tables, void* b, cudaStream_t st);
 

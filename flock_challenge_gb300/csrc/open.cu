@@ -11,7 +11,10 @@
 
 namespace {
 
-constexpr int CB_THREADS = 256;
+constexpr int CB_THREADS = 256;  // at least 256: the table build's first phase takes one thread per image
+#ifndef CBM_THREADS
+#define CBM_THREADS 512
+#endif
 constexpr size_t CB_SMEM = (size_t)2 * 16 * 256 * 16 + 2 * 128 * 16;
 
 // x^i * h for 0 <= i < 128: shift into 256 bits, then reduce.
@@ -33,16 +36,11 @@ __device__ __forceinline__ gf128 gf_mul_xpow(gf128 h, int i) {
 // byte tables from the 128 images L_k(x^i h) and then needs no GF(2^128)
 // product per position: 2 x 16 table lookups. Each CTA owns one high index
 // and a slice of the low range.
-__global__ void __launch_bounds__(CB_THREADS)
-combined_basis_kernel(int lo_bits, int slices, const gf128* __restrict__ lo0, const gf128* __restrict__ hi0,
-                      const gf128* __restrict__ lo1, const gf128* __restrict__ hi1, const gf128* __restrict__ w,
-                      gf128* __restrict__ b) {
-  extern __shared__ gf128 cb[];
-  gf128* tab = cb;                  // [2][256 v][16 q]: entry (k, v, q) in bank group q mod 8
-  gf128* beta = cb + 2 * 16 * 256;  // [2][8 t][16 q]: L_k(x^(8q+t) h)
-  const size_t h = blockIdx.x / slices;
-  const int slice = blockIdx.x % slices;
-  {
+// The sixteen byte tables of both claims for high index h (tab: [2][256 v][16 q],
+// entry (k, v, q) in bank group q mod 8; beta: [2][8 t][16 q] scratch).
+__device__ __forceinline__ void cb_build_tables(size_t h, const gf128* __restrict__ hi0, const gf128* __restrict__ hi1,
+                                                const gf128* __restrict__ w, gf128* tab, gf128* beta) {
+  if (threadIdx.x < 256) {
     const int k = threadIdx.x >> 7, i = threadIdx.x & 127;
     const gf128 y = gf_mul_xpow(k ? hi1[h] : hi0[h], i);
     const gf128* wk = w + 128 * k;
@@ -56,7 +54,7 @@ combined_basis_kernel(int lo_bits, int slices, const gf128* __restrict__ lo0, co
   // subset sums by a Gray walk: item (k, c, q) owns entries v = 8c .. 8c+7 of
   // position q of claim k, starts from the sum over the bits of 8c and adds
   // one image per entry (consecutive items: consecutive q, distinct banks)
-  for (int it = threadIdx.x; it < 2 * 32 * 16; it += CB_THREADS) {
+  for (int it = threadIdx.x; it < 2 * 32 * 16; it += blockDim.x) {
     const int q = it & 15, c = (it >> 4) & 31, k = it >> 9;
     const gf128* bq = beta + k * 128 + q;
     gf128 acc = gf_zero();
@@ -71,26 +69,96 @@ combined_basis_kernel(int lo_bits, int slices, const gf128* __restrict__ lo0, co
     }
   }
   __syncthreads();
+}
+
+// b[p] for the low indices u0 = lo0[j], u1 = lo1[j]: 2 x 16 table lookups,
+// lane l starting at byte position l mod 16 (eight consecutive lanes read
+// eight distinct bank groups: conflict-free random lookups).
+__device__ __forceinline__ gf128 cb_value(const gf128* tab, const gf128 u0, const gf128 u1, int rot) {
+  const uint4 x0 = make_uint4(u0.w[0], u0.w[1], u0.w[2], u0.w[3]), x1 = make_uint4(u1.w[0], u1.w[1], u1.w[2], u1.w[3]);
+  gf128 acc = gf_zero();
+#pragma unroll
+  for (int t = 0; t < 16; t++) {
+    const int q = (rot + t) & 15;
+    const uint32_t w0 = (q & 8) ? ((q & 4) ? x0.w : x0.z) : ((q & 4) ? x0.y : x0.x);
+    const uint32_t w1 = (q & 8) ? ((q & 4) ? x1.w : x1.z) : ((q & 4) ? x1.y : x1.x);
+    const uint32_t b0 = (w0 >> (8 * (q & 3))) & 255, b1 = (w1 >> (8 * (q & 3))) & 255;
+    acc = gf_add(acc, tab[(b0 << 4) + q]);
+    acc = gf_add(acc, tab[4096 + (b1 << 4) + q]);
+  }
+  return acc;
+}
+
+__global__ void __launch_bounds__(CB_THREADS)
+combined_basis_kernel(int lo_bits, int slices, const gf128* __restrict__ lo0, const gf128* __restrict__ hi0,
+                      const gf128* __restrict__ lo1, const gf128* __restrict__ hi1, const gf128* __restrict__ w,
+                      gf128* __restrict__ b) {
+  extern __shared__ gf128 cb[];
+  gf128* tab = cb;
+  gf128* beta = cb + 2 * 16 * 256;
+  const size_t h = blockIdx.x / slices;
+  const int slice = blockIdx.x % slices;
+  cb_build_tables(h, hi0, hi1, w, tab, beta);
   const size_t lo_n = (size_t)1 << lo_bits;
   const size_t per = lo_n / slices;
   const size_t j0 = (size_t)slice * per;
-  // lane l starts at byte position l mod 16: eight consecutive lanes read
-  // eight distinct bank groups (conflict-free random lookups)
   const int rot = threadIdx.x & 15;
-  for (size_t j = j0 + threadIdx.x; j < j0 + per; j += CB_THREADS) {
-    const gf128 u0 = lo0[j], u1 = lo1[j];
-    const uint4 x0 = make_uint4(u0.w[0], u0.w[1], u0.w[2], u0.w[3]), x1 = make_uint4(u1.w[0], u1.w[1], u1.w[2], u1.w[3]);
-    gf128 acc = gf_zero();
+  for (size_t j = j0 + threadIdx.x; j < j0 + per; j += CB_THREADS) b[(h << lo_bits) + j] = cb_value(tab, lo0[j], lo1[j], rot);
+}
+
+// The combined basis fused with the first message of the Ligerito sumcheck
+// over (f, b) (ligerito.rs:6222-6300, as lig_fold_msg without a fold):
+// u0 = sum f[2q] b[2q], u2 = sum (f[2q] + f[2q+1]) (b[2q] + b[2q+1]). A thread
+// takes position pairs: the basis values come from the table lookups (load
+// and store pipes) and the two products from the carry-less multiply (integer
+// pipes) of the same pass, so the two overlap and b is not read back.
+// Partials: (u0, u2, 0) per block.
+__global__ void __launch_bounds__(CBM_THREADS)
+combined_basis_msg_kernel(int lo_bits, int slices, const gf128* __restrict__ lo0, const gf128* __restrict__ hi0,
+                          const gf128* __restrict__ lo1, const gf128* __restrict__ hi1, const gf128* __restrict__ w,
+                          const gf128* __restrict__ f, gf128* __restrict__ b, gf128* __restrict__ partials) {
+  extern __shared__ gf128 cb[];
+  gf128* tab = cb;
+  gf128* beta = cb + 2 * 16 * 256;
+  const size_t h = blockIdx.x / slices;
+  const int slice = blockIdx.x % slices;
+  cb_build_tables(h, hi0, hi1, w, tab, beta);
+  const size_t lo_n = (size_t)1 << lo_bits;
+  const size_t per = lo_n / slices;
+  const size_t j0 = (size_t)slice * per;
+  const int rot = threadIdx.x & 15;
+  gf256 u0 = {{0, 0, 0, 0}}, u2 = u0;
+  for (size_t j = j0 + 2 * threadIdx.x; j < j0 + per; j += 2 * CBM_THREADS) {
+    const size_t p = (h << lo_bits) + j;
+    const gf128 b0 = cb_value(tab, lo0[j], lo1[j], rot), b1 = cb_value(tab, lo0[j + 1], lo1[j + 1], rot ^ 8);
+    b[p] = b0;
+    b[p + 1] = b1;
+    const gf128 f0 = f[p], f1 = f[p + 1];
+    gf256_acc(u0, gf_mul_wide(f0, b0));
+    gf256_acc(u2, gf_mul_wide(gf_add(f0, f1), gf_add(b0, b1)));
+  }
+  __shared__ gf256 red[2][CBM_THREADS / 32];
+  for (int off = 16; off > 0; off >>= 1)
 #pragma unroll
-    for (int t = 0; t < 16; t++) {
-      const int q = (rot + t) & 15;
-      const uint32_t w0 = (q & 8) ? ((q & 4) ? x0.w : x0.z) : ((q & 4) ? x0.y : x0.x);
-      const uint32_t w1 = (q & 8) ? ((q & 4) ? x1.w : x1.z) : ((q & 4) ? x1.y : x1.x);
-      const uint32_t b0 = (w0 >> (8 * (q & 3))) & 255, b1 = (w1 >> (8 * (q & 3))) & 255;
-      acc = gf_add(acc, tab[(b0 << 4) + q]);
-      acc = gf_add(acc, tab[4096 + (b1 << 4) + q]);
+    for (int k = 0; k < 4; k++) {
+      u0.r[k] ^= __shfl_xor_sync(0xffffffffu, u0.r[k], off);
+      u2.r[k] ^= __shfl_xor_sync(0xffffffffu, u2.r[k], off);
     }
-    b[(h << lo_bits) + j] = acc;
+  const int wid = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    red[0][wid] = u0;
+    red[1][wid] = u2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    gf256 s0 = {{0, 0, 0, 0}}, s1 = s0;
+    for (int k = 0; k < CBM_THREADS / 32; k++) {
+      gf256_acc(s0, red[0][k]);
+      gf256_acc(s1, red[1][k]);
+    }
+    partials[3 * blockIdx.x] = gf256_reduce(s0);
+    partials[3 * blockIdx.x + 1] = gf256_reduce(s1);
+    partials[3 * blockIdx.x + 2] = gf_zero();
   }
 }
 
@@ -127,6 +195,16 @@ int flock_launch_shv_from_zvec(const void* zvec, const void* eq_tail, void* scra
 }
 
 
+namespace {
+// CTAs per high index: enough CTAs to fill the GPU, splitting the low range
+// when there are few high indices.
+int cb_slices(size_t n_hi, size_t lo_n) {
+  int slices = 1;
+  while (n_hi * slices < 152 * 2 && lo_n / (2 * slices) >= CB_THREADS) slices *= 2;
+  return slices;
+}
+}  // namespace
+
 int flock_launch_combined_basis(size_t n, const void* t0_lo, const void* t0_hi, const void* t1_lo, const void* t1_hi,
                                 int lo_bits, const void* w, void* b, cudaStream_t st) {
   flock_once_per_device((const void*)combined_basis_kernel, [] {
@@ -135,12 +213,33 @@ int flock_launch_combined_basis(size_t n, const void* t0_lo, const void* t0_hi, 
   const size_t lo_n = (size_t)1 << lo_bits;
   if (n % lo_n != 0 || lo_n < CB_THREADS) return FLOCK_ERR_SHAPE;
   const size_t n_hi = n >> lo_bits;
-  // enough CTAs to fill the GPU: split the low range when there are few high indices
-  int slices = 1;
-  while (n_hi * slices < 152 * 2 && lo_n / (2 * slices) >= CB_THREADS) slices *= 2;
+  const int slices = cb_slices(n_hi, lo_n);
   combined_basis_kernel<<<(unsigned)(n_hi * slices), CB_THREADS, CB_SMEM, st>>>(
       lo_bits, slices, (const gf128*)t0_lo, (const gf128*)t0_hi, (const gf128*)t1_lo, (const gf128*)t1_hi,
       (const gf128*)w, (gf128*)b);
+  flock_count_launch();
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
+int flock_combined_basis_msg_grid(size_t n, int lo_bits) {
+  const size_t lo_n = (size_t)1 << lo_bits, n_hi = n >> lo_bits;
+  return (int)(n_hi * cb_slices(n_hi, lo_n));
+}
+
+int flock_launch_combined_basis_msg(size_t n, const void* t0_lo, const void* t0_hi, const void* t1_lo,
+                                    const void* t1_hi, int lo_bits, const void* w, const void* f, void* b,
+                                    void* partials, cudaStream_t st) {
+  flock_once_per_device((const void*)combined_basis_msg_kernel, [] {
+    cudaFuncSetAttribute(combined_basis_msg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CB_SMEM);
+  });
+  const size_t lo_n = (size_t)1 << lo_bits;
+  if (n % lo_n != 0 || lo_n < CB_THREADS) return FLOCK_ERR_SHAPE;
+  const size_t n_hi = n >> lo_bits;
+  const int slices = cb_slices(n_hi, lo_n);
+  if ((lo_n / slices) % 2) return FLOCK_ERR_SHAPE;
+  combined_basis_msg_kernel<<<(unsigned)(n_hi * slices), CBM_THREADS, CB_SMEM, st>>>(
+      lo_bits, slices, (const gf128*)t0_lo, (const gf128*)t0_hi, (const gf128*)t1_lo, (const gf128*)t1_hi,
+      (const gf128*)w, (const gf128*)f, (gf128*)b, (gf128*)partials);
   flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }

@@ -961,6 +961,8 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     F gam[2] = {tr.sample(), tr.sample()};
     F target = gam[0] * claims[0] + gam[1] * claims[1];
     void* dbc = S->bc.get(n128 * 16);
+    int msg0_grid = 0;  // > 0: the first Ligerito message's partials are in msg0_part
+    void* msg0_part = nullptr;
     {
       // w_k[b] = gamma_k eq(r''_k)[b]: the basis is sum_k sum_b bit_b(t_k) w_k[b]
       std::vector<F> wk(2 * 128);
@@ -968,7 +970,16 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
         for (int bb = 0; bb < 128; bb++) wk[k * 128 + bb] = gam[k] * eqr[k][bb];
       void* dt = S->tables.get(wk.size() * 16);
       h2d(*S, dt, wk.data(), wk.size() * 16);
-      FK(flock_launch_combined_basis(n128, S->tlo0.p, S->thi0.p, S->tlo1.p, S->thi1.p, rs_lo, dt, dbc, st));
+      if (chain) {
+        FK(flock_launch_combined_basis(n128, S->tlo0.p, S->thi0.p, S->tlo1.p, S->thi1.p, rs_lo, dt, dbc, st));
+      } else {
+        // the first Ligerito message over (z, b) comes out of the same pass;
+        // nothing else writes the partials before the opening reads them
+        msg0_grid = flock_combined_basis_msg_grid(n128, rs_lo);
+        msg0_part = part_buf(*S, (size_t)msg0_grid * 3 * 16);
+        FK(flock_launch_combined_basis_msg(n128, S->tlo0.p, S->thi0.p, S->tlo1.p, S->thi1.p, rs_lo, dt, dz, dbc,
+                                           msg0_part, st));
+      }
     }
     if (chain) {
       // packed-direct chain claim (pcs.rs:1055-1090): point [tau, sel0, 0^5, instance]
@@ -1090,7 +1101,14 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       return dbs;
     };
 
-    run_msg(0, F());
+    if (msg0_grid) {  // computed with the combined basis
+      auto s0 = reduce_partials(*S, msg0_part, msg0_grid, 3);
+      msgs.push_back({s0[0], s0[1]});
+      tr.observe(s0[0]);
+      tr.observe(s0[1]);
+    } else {
+      run_msg(0, F());
+    }
     for (int j = 0; j < cfg.initial_k; j++) {
       int bits = cfg.fold_bits[0] - j;
       if (bits > 0) fold_nonces.push_back(grind((uint32_t)bits));

@@ -62,6 +62,10 @@ void oracle_b3_xof(const uint8_t* data, size_t len, uint8_t* out, size_t out_len
   h.update(data, len);
   h.finalize_xof(out, out_len);
 }
+// Parent chaining values of n node pairs: out[i] = parent(children[2i], children[2i+1]).
+void oracle_parent_cvs(const uint8_t* children, size_t n, uint8_t* out) {
+  for (size_t i = 0; i < n; i++) b3_parent_cv(children + 64 * i, children + 64 * i + 32, out + 32 * i);
+}
 void oracle_leaf_cv(const uint8_t* data, size_t len, uint8_t* out32) {
   Hash32 h = leaf_cv(data, len);
   memcpy(out32, h.b, 32);

@@ -169,6 +169,17 @@ def leaf_cv(data):
     return out.tobytes()
 
 
+def parent_cvs(children_u8):
+    """Parent chaining values (BLAKE3 PARENT nodes) of consecutive node pairs."""
+    c = np.ascontiguousarray(children_u8, dtype=np.uint8).reshape(-1)
+    n = c.size // 64
+    out = np.zeros(32 * n, np.uint8)
+    L = lib()
+    L.oracle_parent_cvs.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    L.oracle_parent_cvs(ptr(c), n, ptr(out))
+    return out.reshape(-1, 32)
+
+
 def _proto():
     L = lib()
     if not getattr(L, "_proto_ready", False):

@@ -152,3 +152,40 @@ def test_rate_quarter_256_columns_2e16_rows(ctx):
     otree = O.merkle_tree(cwb, 1 << (rows_log + 2))
     assert np.array_equal(host(tree).reshape(-1, 32), otree)
     assert root == otree[-1].tobytes()
+
+
+def test_rate_quarter_256_columns_2e22_rows(ctx):
+    """The kernel-microbench shape at its largest stated size, 2^22 rows x 256
+    columns at rate 1/4 (2^24 codeword positions, a 64 GiB codeword): two
+    columns against the oracle's one-column commit; the Merkle tree (4 KiB
+    leaves) by sampled leaves against the oracle's leaf hash, every parent of
+    the top eleven levels against the oracle's parent hash, and the root."""
+    import torch
+    rows_log, cols_log = 22, 8
+    m = 7 + cols_log + rows_log
+    n_pos = 1 << (rows_log + 2)
+    g = torch.Generator(device="cuda").manual_seed(2022)
+    z = torch.randint(-2**62, 2**62, ((1 << (m - 7)) * 2,), dtype=torch.int64, device="cuda", generator=g)
+    root, cw, tree = F.commit(ctx, z.view(torch.uint8), m, log_inv_rate=2, log_batch_size=cols_log)
+    torch.cuda.synchronize()
+    zc = z.view(1 << rows_log, 1 << cols_log, 2)
+    cwc = cw.view(torch.int64).view(n_pos, 1 << cols_log, 2)
+    for c in (3, 200):
+        col = zc[:, c, :].contiguous().cpu().numpy().view(np.uint64).reshape(-1)
+        _, ocw, _ = O.commit(col, 7 + rows_log, 2, 0, want_codeword=True)
+        assert np.array_equal(cwc[:, c, :].contiguous().cpu().numpy().view(np.uint64).reshape(-1), ocw), c
+        del ocw
+    t = tree.view(-1, 32)
+    rng = np.random.default_rng(22)
+    for leaf in [0, n_pos - 1] + [int(x) for x in rng.integers(0, n_pos, 30)]:
+        data = cw[leaf * 4096:(leaf + 1) * 4096].cpu().numpy()
+        assert O.leaf_cv(data) == t[leaf].cpu().numpy().tobytes(), leaf
+    # flat tree: level k (2^(24-k) nodes) starts at 2^25 - 2^(25-k)
+    starts = [(1 << 25) - (1 << (25 - k)) for k in range(25)]
+    for k in range(13, 24):
+        below = t[starts[k]:starts[k] + (1 << (24 - k))].cpu().numpy()
+        above = t[starts[k + 1]:starts[k + 1] + (1 << (23 - k))].cpu().numpy()
+        assert np.array_equal(O.parent_cvs(below), above), k
+    assert root == t[-1].cpu().numpy().tobytes()
+    del z, cw, tree
+    torch.cuda.empty_cache()
