@@ -7,6 +7,7 @@ Rebuilds only when a source or header is newer than the library.
 import concurrent.futures as cf
 import glob
 import os
+import platform
 import shutil
 import subprocess
 
@@ -16,6 +17,9 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libflock_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# On an Arm host the host-side GF(2^128) products use PMULL (the crypto
+# extension of every Grace core); other hosts keep the portable product.
+HOST_ARCH = ["-Xcompiler", "-march=armv8-a+crypto"] if platform.machine() == "aarch64" else []
 
 
 def nvcc():
@@ -47,7 +51,7 @@ def build(verbose=False, extra_flags=()):
     os.makedirs(BUILD, exist_ok=True)
     exe = nvcc()
     flags = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"),
-             *ARCH, *extra_flags]
+             *ARCH, *HOST_ARCH, *extra_flags]
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")

@@ -6,6 +6,14 @@
 #include <cstdint>
 #include <vector>
 
+#if defined(__aarch64__) && (defined(__ARM_FEATURE_AES) || defined(__ARM_FEATURE_CRYPTO))
+#define FLOCK_HOST_PMULL 1
+// 64x64 carry-less product by the Arm PMULL instruction (host_pmull.cpp).
+void flock_host_clmul64(uint64_t a, uint64_t b, uint64_t* lo, uint64_t* hi);
+#else
+#define FLOCK_HOST_PMULL 0
+#endif
+
 namespace hf {
 
 struct F {
@@ -37,6 +45,11 @@ inline uint64_t clmul32(uint32_t a, uint32_t b) {
   return (r0 & M0) | (r1 & M1) | (r2 & M2) | (r3 & M3);
 }
 
+#if FLOCK_HOST_PMULL
+// An Arm host built with the crypto extension multiplies with PMULL: the same
+// value as the portable form below, several times faster on a Grace core.
+inline void clmul(uint64_t a, uint64_t b, uint64_t& lo, uint64_t& hi) { flock_host_clmul64(a, b, &lo, &hi); }
+#else
 // 64x64 carry-less product (Karatsuba over 32-bit halves).
 inline void clmul(uint64_t a, uint64_t b, uint64_t& lo, uint64_t& hi) {
   const uint32_t al = (uint32_t)a, ah = (uint32_t)(a >> 32), bl = (uint32_t)b, bh = (uint32_t)(b >> 32);
@@ -45,6 +58,7 @@ inline void clmul(uint64_t a, uint64_t b, uint64_t& lo, uint64_t& hi) {
   lo = ll ^ (mm << 32);
   hi = hh ^ (mm >> 32);
 }
+#endif
 
 inline F reduce(uint64_t r0, uint64_t r1, uint64_t r2, uint64_t r3) {
   uint64_t t_lo = r2 ^ (r2 << 1) ^ (r2 << 2) ^ (r2 << 7);

@@ -331,6 +331,10 @@ struct ProverState {
 namespace {
 
 constexpr size_t kPinH2D = (size_t)4 << 20, kPinD2H = (size_t)1 << 20, kMapped = (size_t)256 << 10;
+// Zerocheck rounds of at most this many pairs run on the host (see the round loop).
+constexpr size_t kHostTailPairs = 512;
+// Lincheck product-sumcheck rounds over at most this many entries run on the host.
+constexpr size_t kHostTailLincheck = 1024;
 
 void h2d(ProverState& S, void* d, const void* h, size_t n) {
   if (n == 0) return;
@@ -742,7 +746,12 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       h2d(*S, djobs, jobs.data(), jobs.size() * sizeof(FlockEqJob));
       FK(flock_launch_eq_split_multi(djobs, n_mlv, max_entries, st));
     }
-    for (int i = 0; i < n_mlv; i++) {
+    // The last rounds, from kHostTailPairs pairs down, run on the host: a GPU
+    // round of a few hundred pairs is a latency-bound launch plus a round
+    // trip (~20 us), the same round on the host a few microseconds.
+    int host_from = n_mlv;
+    while (host_from > 1 && (rows0 >> host_from) <= kHostTailPairs && !qs[host_from - 1].grp) host_from--;
+    for (int i = 0; i < host_from; i++) {
       const size_t n_pairs = rows0 >> (i + 1);  // pairs of the round-i table
       const RoundEq& q = qs[i];
       const F* deq = (const F*)S->zceq.p;
@@ -779,12 +788,50 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       rho.push_back(tr.sample());
     }
     F fa, fb;
-    {
+    if (host_from == n_mlv) {
       uint64_t rp[2];
       u2(rho.back(), rp);
       FK(flock_launch_bind_pairs(curA, curB, 1, rp, nxtA, nxtB, st));
       d2h(*S, &fa, nxtA, 16);
       d2h(*S, &fb, nxtB, 16);
+    } else {
+      // rounds host_from .. n_mlv - 1 on the host, from the table the last
+      // GPU round wrote (2 entries per pair of that round, 4 per pair of round
+      // host_from, which binds them at the last GPU round's challenge first),
+      // as zc_round_kernel computes
+      // them: bind A' = A0 + rho (A0 + A1), then G(1) = sum_j eq[j] a1 b1,
+      // G(inf) = sum_j eq[j] (a0 + a1)(b0 + b1) over eq of the round's
+      // remaining variables
+      const size_t n_in = (rows0 >> host_from) * 2;
+      std::vector<F> tA(n_in), tB(n_in);
+      d2h(*S, tA.data(), curA, n_in * 16);
+      d2h(*S, tB.data(), curB, n_in * 16);
+      auto bind = [](std::vector<F>& v, F rr) {
+        for (size_t j = 0; j < v.size() / 2; j++) v[j] = v[2 * j] + rr * (v[2 * j] + v[2 * j + 1]);
+        v.resize(v.size() / 2);
+      };
+      for (int i = host_from; i < n_mlv; i++) {
+        bind(tA, rho.back());
+        bind(tB, rho.back());
+        const std::vector<F> rr(r.begin() + 6 + i + 1, r.end());
+        const std::vector<F> eq = eq_table(rr);
+        F g1, gi;
+        for (size_t j = 0; j < tA.size() / 2; j++) {
+          const F a0 = tA[2 * j], a1 = tA[2 * j + 1], b0 = tB[2 * j], b1 = tB[2 * j + 1];
+          g1 += eq[j] * (a1 * b1);
+          gi += eq[j] * ((a0 + a1) * (b0 + b1));
+        }
+        g1 = g1 * qs[i].dinv;
+        gi = gi * qs[i].dinv;
+        zc_rounds.push_back({g1, gi});
+        tr.observe(g1);
+        tr.observe(gi);
+        rho.push_back(tr.sample());
+      }
+      bind(tA, rho.back());
+      bind(tB, rho.back());
+      fa = tA[0];
+      fb = tB[0];
     }
     tr.observe(fa);
     tr.observe(fb);
@@ -827,8 +874,14 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       CK(cudaMemcpyAsync(S->zvec0.get(FLOCK_K * 16), dzv, FLOCK_K * 16, cudaMemcpyDeviceToDevice, st));
       // product sumcheck on (comb, z_vec) binding the top variable
       // (lincheck.rs:1242-1300): the same round as the chain shift sumcheck
+      // Rounds over at most kHostTailLincheck entries (and the final bind)
+      // run on the host from the tables the last device round left, as
+      // chain_round_kernel computes them: bind the top variable, then
+      // q(1) = sum W_hi g_hi, q(inf) = sum (W_lo + W_hi)(g_lo + g_hi).
       size_t len = FLOCK_K;
-      for (int t = 0; t < inner_rest; t++) {
+      int t = 0;
+      for (; t < inner_rest; t++) {
+        if (t > 0 && (len / 2) <= kHostTailLincheck) break;
         uint64_t rp[2] = {0, 0};
         if (t > 0) u2(lc_rr.back(), rp);
         if (t > 0) len /= 2;
@@ -841,14 +894,32 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
         lc_rounds.push_back({msg[0], msg[1]});
         lc_rr.push_back(tr.sample());
       }
-      uint64_t rp[2];
-      u2(lc_rr.back(), rp);
-      {  // final bind to the 64 entries of z_partial (its message is not used)
-        const int grid = flock_chain_round_grid(len / 2);
-        void* dpart = part_buf(*S, (size_t)grid * 2 * 16);
-        FK(flock_launch_chain_round(dcomb, dzv, len / 2, 1, rp, dpart, grid, st));
+      std::vector<F> hW(len), hg(len);  // the tables bound up to round t - 1 (2 x the next length)
+      d2h(*S, hW.data(), dcomb, len * 16);
+      d2h(*S, hg.data(), dzv, len * 16);
+      auto bind_top = [](std::vector<F>& v, F rr) {
+        const size_t h = v.size() / 2;
+        for (size_t i = 0; i < h; i++) v[i] = v[i] + rr * (v[i + h] + v[i]);
+        v.resize(h);
+      };
+      for (; t < inner_rest; t++) {
+        bind_top(hW, lc_rr.back());
+        bind_top(hg, lc_rr.back());
+        const size_t q = hW.size() / 2;
+        F e1, ei;
+        for (size_t i = 0; i < q; i++) {
+          e1 += hW[i + q] * hg[i + q];
+          ei += (hW[i] + hW[i + q]) * (hg[i] + hg[i + q]);
+        }
+        tr.observe(e1);
+        tr.observe(ei);
+        lc_rounds.push_back({e1, ei});
+        lc_rr.push_back(tr.sample());
       }
-      d2h(*S, z_partial.data(), dzv, 64 * 16);
+      // final bind to the 64 entries of z_partial
+      bind_top(hW, lc_rr.back());
+      bind_top(hg, lc_rr.back());
+      std::copy(hg.begin(), hg.begin() + 64, z_partial.begin());
     }
     tr.observe_slice(z_partial.data(), 64);
     const F lc_skip = tr.sample();  // lincheck's skip challenge: the ab claim's z_skip
