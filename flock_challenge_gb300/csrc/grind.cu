@@ -31,10 +31,13 @@ struct Digest {
   uint32_t w[8];
 };
 
+// `other` (may be null): the other result slot, reset here for the next grind
+// (which runs after this launch in stream order), so no grind needs a memset.
 __global__ void grind_kernel(const __grid_constant__ Digest digest, uint64_t start, uint64_t count, uint32_t bits,
-                             unsigned long long* __restrict__ best) {
+                             unsigned long long* __restrict__ best, unsigned long long* __restrict__ other) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
+  if (other && i == 0) *other = ~0ull;
   uint64_t nonce = start + i;
   uint32_t m[16];
 #pragma unroll
@@ -52,22 +55,31 @@ __global__ void grind_kernel(const __grid_constant__ Digest digest, uint64_t sta
 
 }  // namespace
 
-// Returns the smallest satisfying nonce. d_scratch: >= 8 bytes of device
-// memory; h_best: 8 bytes of host memory the window result is read into
-// (pinned memory keeps the read cheap). The digest travels as a kernel
-// argument, so nothing is copied to the device.
-int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, uint64_t* h_best, cudaStream_t st,
-                uint64_t* nonce) {
+// Returns the smallest satisfying nonce. d_scratch: >= 16 bytes of device
+// memory, two result slots; h_best: 8 bytes of host memory the window result
+// is read into (pinned memory keeps the read cheap). The digest travels as a
+// kernel argument, so nothing is copied to the device. With `parity` (a
+// caller's counter; the slots set to all ones before its first grind), the
+// grinds alternate slots and each resets the other one for the next; without,
+// the slot is cleared by a memset first.
+int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, int* parity, uint64_t* h_best,
+                cudaStream_t st, uint64_t* nonce) {
   if (bits == 0) {
     *nonce = 0;
     return FLOCK_OK;
   }
   if (bits > 60) return FLOCK_ERR_SHAPE;
   unsigned long long* d_best = (unsigned long long*)d_scratch;
+  unsigned long long* d_other = nullptr;
+  if (parity) {
+    d_best += *parity & 1;
+    d_other = (unsigned long long*)d_scratch + ((*parity & 1) ^ 1);
+    ++*parity;
+  }
   Digest dg;
   memcpy(dg.w, digest, 32);
   const unsigned long long none = ~0ull;
-  if (cudaMemsetAsync(d_best, 0xFF, 8, st) != cudaSuccess) return FLOCK_ERR_CUDA;
+  if (!parity && cudaMemsetAsync(d_best, 0xFF, 8, st) != cudaSuccess) return FLOCK_ERR_CUDA;
   // About two expected hits per window: a miss costs one more window, an
   // oversized window wastes work on every grind (most grinds are 2..14 bits).
   int wlog = (int)bits + 1;
@@ -75,7 +87,7 @@ int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, uint64
   if (wlog > 26) wlog = 26;
   uint64_t window = (uint64_t)1 << wlog;
   for (uint64_t start = 0;; start += window) {
-    grind_kernel<<<(unsigned)((window + 255) / 256), 256, 0, st>>>(dg, start, window, bits, d_best);
+    grind_kernel<<<(unsigned)((window + 255) / 256), 256, 0, st>>>(dg, start, window, bits, d_best, d_other);
     flock_count_launch();
     if (cudaGetLastError() != cudaSuccess) return FLOCK_ERR_CUDA;
     if (cudaMemcpyAsync(h_best, d_best, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess) return FLOCK_ERR_CUDA;

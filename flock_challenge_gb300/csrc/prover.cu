@@ -286,6 +286,7 @@ struct Open {
 }  // namespace
 
 // ============================================================================
+constexpr int kSklMax = 40;  // induced-basis variable counts below this
 constexpr int kKernelSpans = 4;  // witness, L0 NTT, L0 Merkle tree, zerocheck round 1
 
 struct ProverState {
@@ -297,6 +298,7 @@ struct ProverState {
       grind, lvl_cw[2], lvl_tree[2], chW, chG, zceq, zcr, zcjobs;
   DBuf csc_ap, csc_ai, csc_bp, csc_bi;
   bool csc_ready = false;
+  DBuf skl[kSklMax];  // What_k(x^b) tables of the induced basis, per number of variables
   FlockPhaseTimes times;
   // Optional CUDA-event timing of the main kernels of a proof, on the
   // prover's stream: pairs of events around each span of kKernelSpans.
@@ -317,10 +319,12 @@ struct ProverState {
   void* mapped_dev = nullptr;
 
   std::vector<DBuf*> bufs() {
-    return {&in, &z, &a, &b, &stripe, &cw, &tree, &A0, &B0, &A1, &B1, &eqlo, &eqhi, &eqout, &rdev, &part, &red,
+    std::vector<DBuf*> v = {&in, &z, &a, &b, &stripe, &cw, &tree, &A0, &B0, &A1, &B1, &eqlo, &eqhi, &eqout, &rdev, &part, &red,
             &lag, &small, &eqin, &comb, &zvec, &zvec0, &tlo0, &thi0, &tlo1, &thi1, &tables, &bc, &f1, &b1,
             &W, &LO, &HI, &basis, &qbuf, &abuf, &rows, &nidx, &nodes, &grind, &lvl_cw[0], &lvl_cw[1],
             &lvl_tree[0], &lvl_tree[1], &chW, &chG, &zceq, &zcr, &zcjobs, &csc_ap, &csc_ai, &csc_bp, &csc_bi};
+    for (DBuf& d : skl) v.push_back(&d);
+    return v;
   }
   std::vector<const DBuf*> bufs() const {
     auto v = const_cast<ProverState*>(this)->bufs();
@@ -359,6 +363,21 @@ void d2h(ProverState& S, void* h, const void* d, size_t n) {
     CK(cudaMemcpyAsync(h, d, n, cudaMemcpyDeviceToHost, S.st));
     CK(cudaStreamSynchronize(S.st));
   }
+}
+// Two device->host reads behind one wait.
+void d2h2(ProverState& S, void* h1, const void* d1, size_t n1, void* h2, const void* d2, size_t n2) {
+  const size_t off2 = (n1 + 255) & ~(size_t)255;
+  if (!S.pin || off2 + n2 > kPinD2H) {
+    d2h(S, h1, d1, n1);
+    d2h(S, h2, d2, n2);
+    return;
+  }
+  uint8_t* p = S.pin + kPinH2D;
+  if (n1) CK(cudaMemcpyAsync(p, d1, n1, cudaMemcpyDeviceToHost, S.st));
+  if (n2) CK(cudaMemcpyAsync(p + off2, d2, n2, cudaMemcpyDeviceToHost, S.st));
+  CK(cudaStreamSynchronize(S.st));
+  if (n1) std::memcpy(h1, p, n1);
+  if (n2) std::memcpy(h2, p + off2, n2);
 }
 void u2(const F& x, uint64_t out[2]) { out[0] = x.lo; out[1] = x.hi; }
 
@@ -400,9 +419,8 @@ Open open_rows(ProverState& S, const void* cw, const void* tree, size_t block_le
     FK(flock_launch_gather_nodes(tree, di, (int)idx.size(), dn, S.st));
   }
   o.rows.resize(q.size() * width);
-  d2h(S, o.rows.data(), dr, o.rows.size() * 16);
   o.nodes.resize(idx.size() * 32);
-  if (dn) d2h(S, o.nodes.data(), dn, o.nodes.size());
+  d2h2(S, o.rows.data(), dr, o.rows.size() * 16, o.nodes.data(), dn, dn ? o.nodes.size() : 0);
   return o;
 }
 
@@ -1078,13 +1096,15 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     std::vector<uint64_t> grind_nonces, fold_nonces;
     std::vector<F> ood_vals;
     void* dgr = S->grind.get(64);
+    int grind_parity = 0;  // the grinds alternate two result slots, both cleared here once
+    CK(cudaMemsetAsync(dgr, 0xFF, 16, st));
     auto grind = [&](uint32_t bits) {
       uint8_t dg[32];
       tr.digest(dg);
       uint64_t nonce = 0;
       uint64_t local_best = 0;
       uint64_t* h_best = S->pin ? reinterpret_cast<uint64_t*>(S->pin + kPinH2D) : &local_best;
-      FK(flock_grind(dg, bits, dgr, h_best, st, &nonce));
+      FK(flock_grind(dg, bits, dgr, &grind_parity, h_best, st, &nonce));
       tr.absorb_nonce(nonce);
       return nonce;
     };
@@ -1155,8 +1175,13 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       const Sks& sk = sks_for(nvars);
       auto aw = eq_table(alpha_v);
       aw.resize(q.size());
-      void* dsk = S->small.get((size_t)nvars * 32 * 16);
-      h2d(*S, dsk, sk.lin.data(), (size_t)nvars * 32 * 16);
+      // What_k(x^b) table of nvars: constant, copied to the device once
+      if (nvars >= kSklMax) throw Fail(FLOCK_ERR_SHAPE, "basis table size");
+      void* dsk = S->skl[nvars].p;
+      if (!dsk) {
+        dsk = S->skl[nvars].get((size_t)nvars * 32 * 16);
+        h2d(*S, dsk, sk.lin.data(), (size_t)nvars * 32 * 16);
+      }
       uint32_t* dq = (uint32_t*)S->qbuf.get(q.size() * 4);
       h2d(*S, dq, q.data(), q.size() * 4);
       void* dal = S->abuf.get(q.size() * 16);
