@@ -168,12 +168,13 @@ def main(argv=None):
     ap.add_argument("--loads", default="0.9,1.0,1.05,1.1",
                     help="offered loads as multiples of the plain path's compressions/s on the same mix")
     ap.add_argument("--bound", type=float, default=P99_BOUND_MS, help="p99 latency bound (ms)")
+    ap.add_argument("--budget-gb", type=float, default=120, help="server device-memory budget (GiB)")
     ap.add_argument("--workers", type=int, default=4)
     a = ap.parse_args(argv)
     plain = PlainProver()
     res = {"batched": run_batched(a.batch, a.workers, plain=plain),
-           "serving": run_serving([float(x) for x in a.loads.split(",")], a.requests, a.workers, plain=plain,
-                                  p99_bound_ms=a.bound)}
+           "serving": run_serving([float(x) for x in a.loads.split(",")], a.requests, a.workers, a.budget_gb,
+                                  plain=plain, p99_bound_ms=a.bound)}
     print(json.dumps(res))
 
 
