@@ -56,14 +56,17 @@ PUBLISHED = 483866.0  # README.md:110-116, unmodified reference, Apple M4 Pro ru
 # lanes, mean of the eight L0 passes; times 4 for the bench's 2^20 positions.
 NTT_TRAFFIC_PER_PASS = {20: 4 * 478.8e6}
 NTT_MAX_LAYERS = {0: 4, 1: 6, 2: 8}  # layers per pass of the autotuner's pass shapes
-# Thread instructions per GF(2^128) product in the table passes and per
-# butterfly in the multiply passes (2^18-position L0 transform).
-NTT_INSTR_PER_TABLE_PRODUCT = 179
-NTT_INSTR_PER_MULTIPLY_BUTTERFLY = 433
+# Thread instructions per GF(2^128) product in the table passes (mean of the
+# passes over layers 1..8; deeper passes spend more on their table builds) and
+# per butterfly in the multiply pass (its layers are the three deepest, whose
+# narrow twiddles take 4 or 6 32-bit carry-less pieces), 2^18-position L0
+# transform.
+NTT_INSTR_PER_TABLE_PRODUCT = 160
+NTT_INSTR_PER_MULTIPLY_BUTTERFLY = 259
 # Zerocheck round 1 at m = 30 (2^17 outer blocks of 128 rows): warp
 # instructions and DRAM bytes (read + write) of one launch, per outer block.
-ZC1_WARP_INSTR_PER_OUTER = 819868496 / 2**17
-ZC1_DRAM_BYTES_PER_OUTER = (404941056 + 3680768) / 2**17
+ZC1_WARP_INSTR_PER_OUTER = 786345072 / 2**17
+ZC1_DRAM_BYTES_PER_OUTER = (404989184 + 3690496) / 2**17
 
 
 def load_peaks():
