@@ -145,6 +145,8 @@ def _proto_lib():
         L.flock_setup.argtypes = [P, ctypes.c_size_t]
         L.flock_prove.argtypes = [P, P, ctypes.c_size_t, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
         L.flock_last_phase_times.argtypes = [P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+        L.flock_last_host_waits.argtypes = [P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_double),
+                                            ctypes.c_int]
         L.flock_kernel_timing.argtypes = [P, ctypes.c_int]
         L.flock_last_kernel_times.argtypes = [P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
         L.flock_prove_seed.argtypes = [P, ctypes.c_uint32, ctypes.c_uint64, P, ctypes.c_size_t,
@@ -381,6 +383,13 @@ class Blake3Setup:
         arr = (ctypes.c_double * 8)()
         check(_proto_lib().flock_last_phase_times(self.ctx.handle, arr, 8), "flock_last_phase_times")
         return dict(zip(PHASES, list(arr)))
+
+    def host_waits(self):
+        """Per phase of the last proof: (number of host waits for the stream, ms blocked in them)."""
+        n = (ctypes.c_uint64 * 8)()
+        ms = (ctypes.c_double * 8)()
+        check(_proto_lib().flock_last_host_waits(self.ctx.handle, n, ms, 8), "flock_last_host_waits")
+        return {k: (int(a), float(b)) for k, a, b in zip(PHASES, n, ms)}
 
 
 def kernel_launches():

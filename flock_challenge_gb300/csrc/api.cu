@@ -368,4 +368,14 @@ int flock_last_phase_times(const flock_ctx* ctx, double* ms, int n) {
   return FLOCK_OK;
 }
 
+int flock_last_host_waits(const flock_ctx* ctx, uint64_t* waits, double* blocked_ms, int n) {
+  if (!ctx || !ctx->prover || !waits || !blocked_ms) return FLOCK_ERR_ARG;
+  const FlockPhaseTimes& t = flock_prover_times(ctx->prover);
+  for (int i = 0; i < n && i < 8; i++) {
+    waits[i] = t.waits[i];
+    blocked_ms[i] = t.blocked_ms[i];
+  }
+  return FLOCK_OK;
+}
+
 }  // extern "C"

@@ -6,6 +6,7 @@
 #include <cstdint>
 
 #include "../../include/flock_gpu.h"
+#include "stream_wait.h"
 
 constexpr int FLOCK_K_LOG = 14;
 constexpr int FLOCK_K = 1 << FLOCK_K_LOG;
@@ -80,8 +81,9 @@ int flock_launch_induce_basis(const uint32_t* d_queries, int nq, int n, const vo
 int flock_launch_gather_rows(const void* mat, const uint32_t* rows, int n_rows, int width, void* out,
                              cudaStream_t st);
 int flock_launch_gather_nodes(const void* tree, const uint32_t* idx, int n, void* out, cudaStream_t st);
+// waits: the caller's count of host waits (nullptr: not counted).
 int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, int* parity, uint64_t* h_best,
-                cudaStream_t st, uint64_t* nonce);
+                cudaStream_t st, WaitStats* waits, uint64_t* nonce);
 
 // Launch counter of this library's kernels (read through flock_kernel_launches).
 int flock_launch_fold_lsb(const void* in, size_t n_out, const uint64_t r[2], void* out, cudaStream_t st);

@@ -63,7 +63,7 @@ __global__ void grind_kernel(const __grid_constant__ Digest digest, uint64_t sta
 // grinds alternate slots and each resets the other one for the next; without,
 // the slot is cleared by a memset first.
 int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, int* parity, uint64_t* h_best,
-                cudaStream_t st, uint64_t* nonce) {
+                cudaStream_t st, WaitStats* waits, uint64_t* nonce) {
   if (bits == 0) {
     *nonce = 0;
     return FLOCK_OK;
@@ -91,7 +91,7 @@ int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, int* p
     flock_count_launch();
     if (cudaGetLastError() != cudaSuccess) return FLOCK_ERR_CUDA;
     if (cudaMemcpyAsync(h_best, d_best, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess) return FLOCK_ERR_CUDA;
-    if (cudaStreamSynchronize(st) != cudaSuccess) return FLOCK_ERR_CUDA;
+    if (flock_stream_wait(st, waits) != cudaSuccess) return FLOCK_ERR_CUDA;
     if (*h_best != none) {
       *nonce = *h_best;
       return FLOCK_OK;

@@ -281,6 +281,10 @@ struct Open {
   std::vector<F> rows;  // q x width
   size_t width = 0;
   std::vector<uint8_t> nodes;  // 32-byte hashes
+  // Copied into the pinned openings area by the stream (no wait of its own):
+  // rows and nodes are filled from there by finish_open once a later wait
+  // has passed. -1: already filled.
+  ptrdiff_t pin_rows = -1, pin_nodes = -1;
 };
 
 }  // namespace
@@ -313,10 +317,17 @@ struct ProverState {
   // copies asynchronous); device->host reads go through the last kPinD2H bytes.
   uint8_t* pin = nullptr;
   size_t pin_off = 0;
+  // Pinned area the opened rows and Merkle nodes of a proof are copied into
+  // (bump-allocated per proof): they are only serialized at the end of the
+  // proof, so their copies ride on the stream and need no wait of their own.
+  uint8_t* pin_open = nullptr;
+  size_t pin_open_off = 0;
   // Mapped pinned area for round partials: kernels write them straight into
   // host memory, so reading a round's message needs only the stream sync.
   uint8_t* mapped = nullptr;
   void* mapped_dev = nullptr;
+  // The host's waits for the stream (flock_stream_wait) in the current proof.
+  WaitStats waits;
 
   std::vector<DBuf*> bufs() {
     std::vector<DBuf*> v = {&in, &z, &a, &b, &stripe, &cw, &tree, &A0, &B0, &A1, &B1, &eqlo, &eqhi, &eqout, &rdev, &part, &red,
@@ -335,6 +346,7 @@ struct ProverState {
 namespace {
 
 constexpr size_t kPinH2D = (size_t)4 << 20, kPinD2H = (size_t)1 << 20, kMapped = (size_t)256 << 10;
+constexpr size_t kPinOpen = (size_t)4 << 20;
 // Zerocheck rounds of at most this many pairs run on the host (see the round loop).
 constexpr size_t kHostTailPairs = 512;
 // Lincheck product-sumcheck rounds over at most this many entries run on the host.
@@ -357,11 +369,11 @@ void d2h(ProverState& S, void* h, const void* d, size_t n) {
   if (S.pin && n <= kPinD2H) {
     uint8_t* p = S.pin + kPinH2D;
     CK(cudaMemcpyAsync(p, d, n, cudaMemcpyDeviceToHost, S.st));
-    CK(cudaStreamSynchronize(S.st));
+    CK(flock_stream_wait(S.st, &S.waits));
     std::memcpy(h, p, n);
   } else {
     CK(cudaMemcpyAsync(h, d, n, cudaMemcpyDeviceToHost, S.st));
-    CK(cudaStreamSynchronize(S.st));
+    CK(flock_stream_wait(S.st, &S.waits));
   }
 }
 // Two device->host reads behind one wait.
@@ -375,7 +387,7 @@ void d2h2(ProverState& S, void* h1, const void* d1, size_t n1, void* h2, const v
   uint8_t* p = S.pin + kPinH2D;
   if (n1) CK(cudaMemcpyAsync(p, d1, n1, cudaMemcpyDeviceToHost, S.st));
   if (n2) CK(cudaMemcpyAsync(p + off2, d2, n2, cudaMemcpyDeviceToHost, S.st));
-  CK(cudaStreamSynchronize(S.st));
+  CK(flock_stream_wait(S.st, &S.waits));
   if (n1) std::memcpy(h1, p, n1);
   if (n2) std::memcpy(h2, p + off2, n2);
 }
@@ -420,8 +432,27 @@ Open open_rows(ProverState& S, const void* cw, const void* tree, size_t block_le
   }
   o.rows.resize(q.size() * width);
   o.nodes.resize(idx.size() * 32);
-  d2h2(S, o.rows.data(), dr, o.rows.size() * 16, o.nodes.data(), dn, dn ? o.nodes.size() : 0);
+  const size_t nr = o.rows.size() * 16, nn = dn ? o.nodes.size() : 0;
+  const size_t need = ((nr + 255) & ~(size_t)255) + ((nn + 255) & ~(size_t)255);
+  if (S.pin_open && S.pin_open_off + need <= kPinOpen) {
+    o.pin_rows = (ptrdiff_t)S.pin_open_off;
+    o.pin_nodes = (ptrdiff_t)(S.pin_open_off + ((nr + 255) & ~(size_t)255));
+    S.pin_open_off += need;
+    if (nr) CK(cudaMemcpyAsync(S.pin_open + o.pin_rows, dr, nr, cudaMemcpyDeviceToHost, S.st));
+    if (nn) CK(cudaMemcpyAsync(S.pin_open + o.pin_nodes, dn, nn, cudaMemcpyDeviceToHost, S.st));
+  } else {
+    d2h2(S, o.rows.data(), dr, nr, o.nodes.data(), dn, nn);
+  }
   return o;
+}
+
+// Fills an opening whose copies were queued by open_rows; the caller has
+// waited for the stream since.
+void finish_open(ProverState& S, Open& o) {
+  if (o.pin_rows < 0) return;
+  if (!o.rows.empty()) std::memcpy(o.rows.data(), S.pin_open + o.pin_rows, o.rows.size() * 16);
+  if (!o.nodes.empty()) std::memcpy(o.nodes.data(), S.pin_open + o.pin_nodes, o.nodes.size());
+  o.pin_rows = o.pin_nodes = -1;
 }
 
 void write_open(Wire& w, const Open& o) {
@@ -440,7 +471,7 @@ void write_open(Wire& w, const Open& o) {
 std::vector<F> reduce_partials(ProverState& S, const void* part, size_t count, int width) {
   std::vector<F> out(width);
   if (S.mapped && part == S.mapped_dev) {  // written by the kernel into host memory
-    CK(cudaStreamSynchronize(S.st));
+    CK(flock_stream_wait(S.st, &S.waits));
     const F* rows = reinterpret_cast<const F*>(S.mapped);
     for (size_t c = 0; c < count; c++)
       for (int k = 0; k < width; k++) out[k] += rows[c * width + k];
@@ -486,6 +517,9 @@ ProverState* flock_prover_create(int device) {
   void* pin = nullptr;
   if (cudaMallocHost(&pin, kPinH2D + kPinD2H) == cudaSuccess) S->pin = (uint8_t*)pin;
   else cudaGetLastError();
+  void* po = nullptr;
+  if (cudaMallocHost(&po, kPinOpen) == cudaSuccess) S->pin_open = (uint8_t*)po;
+  else cudaGetLastError();
   void* m = nullptr;
   if (cudaHostAlloc(&m, kMapped, cudaHostAllocMapped) == cudaSuccess) {
     if (cudaHostGetDevicePointer(&S->mapped_dev, m, 0) == cudaSuccess) S->mapped = (uint8_t*)m;
@@ -503,6 +537,7 @@ void flock_prover_destroy(ProverState* S) {
   if (S->d_r1t) cudaFree(S->d_r1t);
   if (S->st) cudaStreamDestroy(S->st);
   if (S->pin) cudaFreeHost(S->pin);
+  if (S->pin_open) cudaFreeHost(S->pin_open);
   if (S->mapped) cudaFreeHost(S->mapped);
   delete S;
 }
@@ -559,6 +594,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     CK(cudaSetDevice(S->device));
     CK(cudaStreamSynchronize(S->st));  // the staging area of the previous proof is free again
     S->pin_off = 0;
+    S->pin_open_off = 0;
     const int m = 14 + n_log;
     LigCfg cfg;
     if (!lig_config(m, 0, cfg)) return FLOCK_ERR_SHAPE;
@@ -568,6 +604,15 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     cudaStream_t st = S->st;
     FlockPhaseTimes& T = S->times;
     T = FlockPhaseTimes();
+    S->waits = WaitStats();
+    uint64_t waits_seen = 0;
+    double blocked_seen = 0;
+    auto snap_waits = [&](int phase) {
+      T.waits[phase] = S->waits.waits - waits_seen;
+      T.blocked_ms[phase] = S->waits.blocked_ms - blocked_seen;
+      waits_seen = S->waits.waits;
+      blocked_seen = S->waits.blocked_ms;
+    };
     Clock clk;
     // ---- setup constants (cached) ----
     uint8_t digest[32];
@@ -590,6 +635,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     }
     const Lagrange& LG = lagrange();
     T.setup_ms = clk.lap();
+    snap_waits(0);
 
     // ---- witness + commit ----
     const size_t nbits = (size_t)1 << m, nbytes = nbits / 8, n128 = nbits / 128;
@@ -617,6 +663,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     uint8_t root0[32];
     d2h(*S, root0, (const uint8_t*)dtree + (2 * block0 - 2) * 32, 32);
     T.commit_ms = clk.lap();
+    snap_waits(1);
 
     Wire w;
     w.raw("FLOCK", 5);
@@ -679,6 +726,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       }
     }
     T.zc_round1_ms = clk.lap();
+    snap_waits(2);
     tr.observe_slice(p_ab.data(), 64);
     tr.observe_slice(p_c.data(), 64);
     F zc_z = tr.sample();
@@ -854,6 +902,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     tr.observe(fa);
     tr.observe(fb);
     T.zc_rounds_ms = clk.lap();
+    snap_waits(3);
     w.fv(p_ab);
     w.fv(p_c);
     w.pv(zc_rounds);
@@ -966,6 +1015,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       claim->ab.n_outer = claim->c.n_outer = (uint32_t)n_out;
     }
     T.lincheck_ms = clk.lap();
+    snap_waits(4);
     w.pv(lc_rounds);
     w.fv(z_partial);
 
@@ -1084,6 +1134,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       FK(flock_launch_chain_claim_basis(dbc, (size_t)1 << n_log, S->eqlo.p, S->eqhi.p, lob, c, st));
     }
     T.ring_switch_ms = clk.lap();
+    snap_waits(5);
     w.u64(2);
     w.fv(s_hat[0]);
     w.fv(s_hat[1]);
@@ -1104,7 +1155,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       uint64_t nonce = 0;
       uint64_t local_best = 0;
       uint64_t* h_best = S->pin ? reinterpret_cast<uint64_t*>(S->pin + kPinH2D) : &local_best;
-      FK(flock_grind(dg, bits, dgr, &grind_parity, h_best, st, &nonce));
+      FK(flock_grind(dg, bits, dgr, &grind_parity, h_best, st, &S->waits, &nonce));
       tr.absorb_nonce(nonce);
       return nonce;
     };
@@ -1275,7 +1326,14 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       prev_block = (size_t)1 << (n_next - lni2 + rate2);
       prev_width = 1 << lni2;
     }
+    // one wait for the openings' queued copies (the final opening's gathers
+    // are the last work of the phase)
+    CK(flock_stream_wait(st, &S->waits));
+    finish_open(*S, open0);
+    for (Open& o : rec_opens) finish_open(*S, o);
+    finish_open(*S, final_open);
     T.ligerito_ms = clk.lap();
+    snap_waits(6);
 
     // ---- bundle tail: BatchOpeningProofLigerito.ligerito ----
     w.raw(root0, 32);  // initial_root
@@ -1312,6 +1370,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       cudaGetLastError();
     }
     T.serialize_ms = clk.lap();
+    snap_waits(7);
     return FLOCK_OK;
   } catch (const Fail& f) {
     return f.code;

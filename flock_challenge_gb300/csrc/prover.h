@@ -12,10 +12,13 @@ namespace fs {
 class Transcript;
 }
 
-// Host wall time of each phase of the last proof, in milliseconds.
+// Host wall time of each phase of the last proof, in milliseconds, and the
+// host's waits for the stream in each phase (count, and time blocked in them).
 struct FlockPhaseTimes {
   double setup_ms = 0, commit_ms = 0, zc_round1_ms = 0, zc_rounds_ms = 0, lincheck_ms = 0, ring_switch_ms = 0,
          ligerito_ms = 0, serialize_ms = 0;
+  uint64_t waits[8] = {};
+  double blocked_ms[8] = {};
 };
 
 // A hash-chain proof (Blake3Setup::prove_chain, crates/flock-prover/src/r1cs_hashes/blake3.rs:3785-3805):

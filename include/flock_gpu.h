@@ -176,6 +176,13 @@ void* flock_stream(flock_ctx* ctx);
  * FLOCK_PHASE_TIMING prints, crates/flock-prover/src/prover.rs:958-1216). */
 int flock_last_phase_times(const flock_ctx* ctx, double* ms, int n);
 
+/* The host's waits for the context's stream in each phase of the last proof
+ * (same phase order, first n entries): how many, and the host time spent
+ * blocked in them (ms). A phase's wall time minus its blocked time is the
+ * host's own work (launches, transcript, host rounds). No reference
+ * counterpart (measurement only). */
+int flock_last_host_waits(const flock_ctx* ctx, uint64_t* waits, double* blocked_ms, int n);
+
 /* CUDA-event timing of the main kernels of every proof on this context, on
  * the prover's own stream (enable != 0 turns it on; off by default), and
  * the device time (ms) of each span of the last proof: witness, L0 NTT,

@@ -97,3 +97,18 @@ def test_device_input_generator_matches_reference_generator(cuda_device):
 def test_prove_seed_equals_prove_of_generated_inputs(cuda_device):
     setup = F.Blake3Setup(1 << 9)
     assert setup.prove_seed(77) == setup.prove_fast(O.compressions(9, 77))
+
+
+def test_phase_times_and_host_waits_describe_the_last_proof(cuda_device):
+    setup = F.Blake3Setup(1 << 10)
+    proof = setup.prove_seed(3)
+    phases = setup.phase_times()
+    waits = setup.host_waits()
+    assert set(waits) == set(phases) == set(F.PHASES)
+    # every sumcheck phase reads its messages back: at least one wait each,
+    # and the time blocked in a phase's waits lies within its wall time
+    for k in ("commit", "zerocheck_rounds", "lincheck", "ligerito"):
+        n, blocked = waits[k]
+        assert n >= 1 and 0.0 <= blocked <= phases[k] + 1e-3, (k, n, blocked, phases[k])
+    # the openings' copies ride on the stream: the proof is still the oracle's
+    assert proof == O.prove(O.compressions(10, 3), 10)
