@@ -27,7 +27,7 @@ enum {
   FLOCK_ERR_OOM = -3,     /* device allocation failed / over budget */
   FLOCK_ERR_ARG = -4,     /* null or inconsistent argument */
   FLOCK_ERR_CAPACITY = -5,/* output buffer too small */
-  FLOCK_ERR_TIMEOUT = -6, /* a bounded device wait expired */
+  FLOCK_ERR_TIMEOUT = -6, /* a bounded search gave up: the grind's nonce range ran out */
   FLOCK_ERR_VERIFY = -7,  /* an internal consistency check failed */
   FLOCK_ERR_LIMIT = -8    /* size above the fixed limit of an entry point that allocates nothing */
 };
