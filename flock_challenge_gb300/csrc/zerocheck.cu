@@ -206,14 +206,16 @@ __device__ __forceinline__ uint64_t shfl_xor64(uint64_t v, int m) {
 //        step k lane l looks up byte position (l + k) mod 8, so any eight
 //        consecutive lanes hit eight distinct bank groups and the random
 //        lookups are conflict-free;
-//   LH   per warp (one outer block xo per warp at a time): the eq-weighted
-//        phi8 nibble tables L[j] = phi8(j) e and H[g] = phi8(16 g) e,
-//        e = eq_out(xo), eight replicas each (entry j of replica r at slot
-//        8 j + r, H 128 slots after L; lane l reads replica l mod 8, so the
-//        lookups are conflict-free): phi8(v) e = L[v & 15] + H[v >> 4],
-//        because phi8 is additive, so the block's values come out already
+//   T8   per warp (one outer block xo per warp at a time): the eq-weighted
+//        phi8 table T8[v] = phi8(v) e for the 256 bytes v, e = eq_out(xo)
+//        (entry v at slot v), so the block's values come out already
 //        weighted and need no GF(2^128) product (eight per block build the
-//        tables instead of twelve per lane);
+//        table's basis phi8(2^k) e, k < 8: phi8 is additive). One lookup per
+//        value: the random bytes of a quarter warp share bank groups at times
+//        (about 2.6 wavefronts per quarter-warp lookup), which the load/store
+//        pipe absorbs; with two nibble tables L[v & 15] + H[v >> 4] in eight
+//        conflict-free replicas (the same 4 KiB) each value took two lookups,
+//        two index computations and a four-word XOR on the busy ALU pipe;
 //   P    per warp: phi8(2^k) e for k < 8, the tables' basis;
 //   xch  per warp: [16 producer rows] of 20 words (64 bytes used; the odd
 //        80-byte row pitch makes the 16-byte stores conflict-free), one plane
@@ -221,10 +223,6 @@ __device__ __forceinline__ uint64_t shfl_xor64(uint64_t v, int m) {
 // The two half-warps share the outer block: each sums half of its rows, the
 // halves add their planes with one exchange of registers, each converts half
 // of the points to bytes, and each lane then handles two of the 64 points.
-// One block per warp (instead of one per half-warp) halves the nibble tables
-// per warp, which makes room for the eight replicas: with four, two lanes of
-// a quarter warp shared a bank group and nine quarter-warp lookups in ten
-// took two wavefronts.
 constexpr int R1_ROW = 20;
 constexpr int R1_XCH = 16 * R1_ROW;
 constexpr int R1_WARPS = R1_THREADS / 32;
@@ -255,10 +253,8 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int xm = lane & 15, h = lane >> 4;
   uint32_t* my_x = xch + warp * R1_XCH;
-  uint4* my_lh = lh + warp * 256;
+  uint4* my_t8 = lh + warp * 256;
   uint4* my_p = pk_s + warp * 8;
-  const uint4* my_l = my_lh + (lane & 7);
-  const uint4* my_h = my_lh + 128 + (lane & 7);
   // points 4 xm + 2 h + {0, 1}: a b sums, then c sums of parity 0 and 1
   gf128 sum_ab[2], sum_c[4];
 #pragma unroll
@@ -335,7 +331,7 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
     for (int j = 0; j < 8; j++) w[j] ^= shfl_xor64(w[j], 16);
 #pragma unroll
     for (int j = 0; j < 16; j++) t[j] ^= shfl_xor64(t[j], 16);
-    // eq-weighted phi8 nibble tables of this block (see the layout above)
+    // eq-weighted phi8 table of this block (see the layout above)
     if (lane < 8) {
       const gf128 e = gf_load(&eq_out[xo]);
       const uint4 f = phik[lane];
@@ -344,19 +340,28 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
     }
     __syncwarp();
     {
-      // half 0 builds L[xm], half 1 H[xm]; replica (r + xm) mod 8 at step r
-      // keeps the eight stores of a quarter warp in distinct bank groups
-      const uint4* src = my_p + 4 * h;
-      uint4 val = make_uint4(0, 0, 0, 0);
+      // lane l writes T8[l + 32 i], i < 8: the part of bits 0..4 (l) once,
+      // then the part of bits 5..7 (i) along a Gray walk, one XOR per entry;
+      // a quarter warp's stores are 128 consecutive bytes
+      uint4 pb[8];
 #pragma unroll
-      for (int k = 0; k < 4; k++)
-        if ((xm >> k) & 1) {
-          const uint4 a = src[k];
-          val.x ^= a.x; val.y ^= a.y; val.z ^= a.z; val.w ^= a.w;
+      for (int k = 0; k < 8; k++) pb[k] = my_p[k];
+      uint4 lo = make_uint4(0, 0, 0, 0);
+#pragma unroll
+      for (int k = 0; k < 5; k++) {
+        const uint32_t m = 0u - ((uint32_t)(lane >> k) & 1u);
+        lo.x ^= pb[k].x & m; lo.y ^= pb[k].y & m; lo.z ^= pb[k].z & m; lo.w ^= pb[k].w & m;
+      }
+      uint4 hp = make_uint4(0, 0, 0, 0);
+#pragma unroll
+      for (int g = 0; g < 8; g++) {
+        if (g) {
+          const uint4 a = pb[5 + ((g & 1) ? 0 : (g & 2) ? 1 : 2)];
+          hp.x ^= a.x; hp.y ^= a.y; hp.z ^= a.z; hp.w ^= a.w;
         }
-      uint4* dst = my_lh + 128 * h + 8 * xm;
-#pragma unroll
-      for (int r = 0; r < 8; r++) dst[(r + xm) & 7] = val;
+        const int i = g ^ (g >> 1);
+        my_t8[lane + 32 * i] = make_uint4(lo.x ^ hp.x, lo.y ^ hp.y, lo.z ^ hp.z, lo.w ^ hp.w);
+      }
     }
     // Hand the three plane sets, one at a time, to the lanes as bytes: the
     // lanes of point quad xm read word xm of every producer row, half h
@@ -380,8 +385,7 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
 #pragma unroll
         for (int q = 0; q < 2; q++) {
           const uint32_t v8 = (bw >> (8 * q)) & 255;
-          const uint4 a = my_l[(v8 & 15) << 3], b = my_h[(v8 >> 4) << 3];
-          acc_shift_xor_v(v[q], make_uint4(a.x ^ b.x, a.y ^ b.y, a.z ^ b.z, a.w ^ b.w), (uint32_t)mm2);
+          acc_shift_xor_v(v[q], my_t8[v8], (uint32_t)mm2);
         }
       }
 #pragma unroll

@@ -90,24 +90,40 @@ def test_lincheck_stripe_rotation():
         assert sorted((l + st) & 7 for st in range(8)) == list(range(8))
 
 
-def test_phi8_nibble_tables_weight_by_eq():
-    # phi8(v) e = L[v & 15] + H[v >> 4] with L[j] = sum_{k<4, bit k of j} phi8(2^k) e
-    # and H[g] = sum_{k<4, bit k of g} phi8(2^(k+4)) e (phi8 is additive)
+def test_phi8_table_weights_by_eq():
+    # zc_round1_kernel's per-warp table T8[v] = phi8(v) e: lane l writes slots
+    # l + 32 i (i < 8) as the XOR of phi8(2^k) e over the bits k < 5 of l and,
+    # along a Gray walk over g (i = g ^ (g >> 1), one XOR of basis 5 + ctz(g)
+    # per step), over the bits k of i at 5 + k; every slot once, and a quarter
+    # warp's eight stores are 128 consecutive bytes
     import oracle_lib as O
     e = (0x0123456789ABCDEF, 0xF0E1D2C3B4A59687)
     P = [O.gf_mul(O.phi8(1 << k), e) for k in range(8)]
 
-    def combo(j, base):
-        acc = (0, 0)
-        for k in range(4):
-            if (j >> k) & 1:
-                acc = (acc[0] ^ P[base + k][0], acc[1] ^ P[base + k][1])
-        return acc
-    L = [combo(j, 0) for j in range(16)]
-    H = [combo(g, 4) for g in range(16)]
+    def xor(a, b):
+        return (a[0] ^ b[0], a[1] ^ b[1])
+    t8 = {}
+    for lane in range(32):
+        lo = (0, 0)
+        for k in range(5):
+            if (lane >> k) & 1:
+                lo = xor(lo, P[k])
+        hp = (0, 0)
+        for g in range(8):
+            if g:
+                hp = xor(hp, P[5 + (0 if g & 1 else 1 if g & 2 else 2)])
+            i = g ^ (g >> 1)
+            slot = lane + 32 * i
+            assert slot not in t8
+            t8[slot] = xor(lo, hp)
+    assert sorted(t8) == list(range(256))
     for v in range(256):
-        lo, hi = L[v & 15], H[v >> 4]
-        assert (lo[0] ^ hi[0], lo[1] ^ hi[1]) == O.gf_mul(O.phi8(v), e), v
+        assert t8[v] == O.gf_mul(O.phi8(v), e), v
+    for g in range(8):  # the slots a quarter warp writes at one step
+        i = g ^ (g >> 1)
+        for q in range(4):
+            slots = [lane + 32 * i for lane in range(8 * q, 8 * q + 8)]
+            assert slots == list(range(slots[0], slots[0] + 8)) and slots[0] % 8 == 0
 
 
 def test_gf_tab_row_direct_gray_walk():
