@@ -25,8 +25,12 @@ int flock_launch_merkle(const void* d_data, size_t n_leaves, size_t leaf_bytes, 
 
 // ---- protocol kernels ------------------------------------------------------
 struct ZcRound1Tables;
-int flock_launch_zc_round1(const void* a, const void* b, const void* c, size_t n_outer, const void* eq_out,
+// eq_basis: n_outer x 8 F128 from flock_launch_zc1_eq_basis.
+int flock_launch_zc_round1(const void* a, const void* b, const void* c, size_t n_outer, const void* eq_basis,
                            const ZcRound1Tables* d_tables, void* partials, int grid, cudaStream_t st);
+// out[8 xo + k] = phi8(2^k) eq_out[xo] for xo < n_outer (round 1's table basis).
+int flock_launch_zc1_eq_basis(const void* eq_out, size_t n_outer, const ZcRound1Tables* d_tables, void* out,
+                              cudaStream_t st);
 int flock_launch_reduce_rows(const void* in, size_t count, int width, void* out, cudaStream_t st);
 int flock_launch_eq_split(const void* r, int lo_bits, int hi_bits, void* lo, void* hi, cudaStream_t st);
 // Several eq table pairs in one launch (device array of jobs; lo_bits and

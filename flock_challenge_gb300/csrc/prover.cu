@@ -705,12 +705,16 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       int nv = (int)rout.size();
       void* dr = S->rdev.get(rout.size() * 16 + 16);
       h2d(*S, dr, rout.data(), rout.size() * 16);
-      void* deq = S->eqout.get(n_outer * 16);
+      // eq_out, then round 1's per-block table basis phi8(2^k) eq_out(xo)
+      // behind it in the same buffer
+      void* deq = S->eqout.get(n_outer * 16 * 9);
+      void* dbasis = (uint8_t*)deq + n_outer * 16;
       FK(flock_launch_eq_split(dr, nv, 0, deq, S->eqhi.get(16), st));
+      FK(flock_launch_zc1_eq_basis(deq, n_outer, S->d_r1t, dbasis, st));
       const int grid = 152;
       void* dpart = S->part.get((size_t)grid * 192 * 16);
       S->mark(6);
-      FK(flock_launch_zc_round1(da, db, dz, n_outer, deq, S->d_r1t, dpart, grid, st));
+      FK(flock_launch_zc_round1(da, db, dz, n_outer, dbasis, S->d_r1t, dpart, grid, st));
       S->mark(7);
       auto sums = reduce_partials(*S, dpart, grid, 192);
       F dinv = zc::medium_dinv();

@@ -171,10 +171,11 @@ size_t flock_footprint_bytes(uint32_t log2_size) {
   // compressions (m = 14 + log2_size): the witness planes and stripe
   // (4 x 2^m / 8), the rate-1/2 codeword (2^m / 4), the zerocheck tables
   // (2^m / 2 + 2^m / 4), the combined basis and first Ligerito fold (2^m / 4),
+  // round 1's eq table and its per-block basis (9 x 16 B per 2^13 bits: 2^m / 57),
   // smaller per-level buffers, the inputs, and the fixed matrices and partials.
   const int n_log = log2_slots((size_t)1 << log2_size);
   const double two_m = (double)((uint64_t)1 << (14 + n_log));
-  return (size_t)(1.85 * two_m) + ((size_t)128 << n_log) + ((size_t)320 << 20);
+  return (size_t)(1.87 * two_m) + ((size_t)128 << n_log) + ((size_t)320 << 20);
 }
 
 int flock_server_create(int device, size_t hbm_budget, int n_workers, flock_server** out) {

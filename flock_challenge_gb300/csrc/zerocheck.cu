@@ -21,6 +21,8 @@
 // (C_s = (1 + r6) S[s] + r6 S[64 + s], mapped to Lambda on the host), and S is
 // exactly the ring-switch statistic s_hat_v of the c-claim (bit 64t + s of
 // packed word x >> 1), so the opening reuses it.
+#include <algorithm>
+
 #include "flock_internal.h"
 #include "gf128.cuh"
 #include "gf_tab.cuh"
@@ -209,14 +211,14 @@ __device__ __forceinline__ uint64_t shfl_xor64(uint64_t v, int m) {
 //   T8   per warp (one outer block xo per warp at a time): the eq-weighted
 //        phi8 table T8[v] = phi8(v) e for the 256 bytes v, e = eq_out(xo)
 //        (entry v at slot v), so the block's values come out already
-//        weighted and need no GF(2^128) product (eight per block build the
-//        table's basis phi8(2^k) e, k < 8: phi8 is additive). One lookup per
+//        weighted and need no GF(2^128) product; the table is the subset
+//        sums of its basis phi8(2^k) e, k < 8 (phi8 is additive), which
+//        zc1_eq_basis_kernel computes for every block beforehand. One lookup per
 //        value: the random bytes of a quarter warp share bank groups at times
 //        (about 2.6 wavefronts per quarter-warp lookup), which the load/store
 //        pipe absorbs; with two nibble tables L[v & 15] + H[v >> 4] in eight
 //        conflict-free replicas (the same 4 KiB) each value took two lookups,
 //        two index computations and a four-word XOR on the busy ALU pipe;
-//   P    per warp: phi8(2^k) e for k < 8, the tables' basis;
 //   xch  per warp: [16 producer rows] of 20 words (64 bytes used; the odd
 //        80-byte row pitch makes the 16-byte stores conflict-free), one plane
 //        set at a time.
@@ -226,35 +228,30 @@ __device__ __forceinline__ uint64_t shfl_xor64(uint64_t v, int m) {
 constexpr int R1_ROW = 20;
 constexpr int R1_XCH = 16 * R1_ROW;
 constexpr int R1_WARPS = R1_THREADS / 32;
-constexpr size_t R1_SMEM = (size_t)8 * 4 * 256 * 16 + (size_t)R1_WARPS * 256 * 16 + (size_t)R1_WARPS * 8 * 16 + 128 +
-                           (size_t)R1_WARPS * R1_XCH * 4;
+constexpr size_t R1_SMEM = (size_t)8 * 4 * 256 * 16 + (size_t)R1_WARPS * 256 * 16 + (size_t)R1_WARPS * R1_XCH * 4;
 static_assert(R1_SMEM <= 232448, "round-1 shared memory above the 227 KB per-block limit");
 
 // grid: each warp walks outer blocks; lane: xm = lane & 15 (producer row
 // group, then point quad), h = lane >> 4 (row half, then point pair).
 __global__ void __launch_bounds__(R1_THREADS, 1)
 zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B, const uint64_t* __restrict__ C,
-                 size_t n_outer, const gf128* __restrict__ eq_out, const ZcRound1Tables* __restrict__ T,
+                 size_t n_outer, const uint4* __restrict__ eq_basis, const ZcRound1Tables* __restrict__ T,
                  gf128* __restrict__ partials) {
   extern __shared__ uint4 sm[];
   uint4* ext = sm;                                                   // [4][256][8]
-  uint4* lh = ext + 8 * 4 * 256;                                     // per warp [L, H][16][8]
-  uint4* pk_s = lh + R1_WARPS * 256;                                 // per warp [8]
-  uint4* phik = pk_s + R1_WARPS * 8;                                 // phi8(2^k), k < 8
-  uint32_t* xch = reinterpret_cast<uint32_t*>(phik + 8);             // per warp [R1_XCH]
+  uint4* lh = ext + 8 * 4 * 256;                                     // per warp T8[256]
+  uint32_t* xch = reinterpret_cast<uint32_t*>(lh + R1_WARPS * 256);  // per warp [R1_XCH]
   const uint64_t* ext_src = &T->ext[0][0][0];
   for (int i = threadIdx.x; i < 8 * 4 * 256; i += R1_THREADS) {
     const int q = i >> 11, v = (i >> 3) & 255, c = i & 7;
     const uint64_t* e = ext_src + ((size_t)(c * 256 + v) << 3) + 2 * q;
     ext[i] = make_uint4((uint32_t)e[0], (uint32_t)(e[0] >> 32), (uint32_t)e[1], (uint32_t)(e[1] >> 32));
   }
-  if (threadIdx.x < 8) phik[threadIdx.x] = reinterpret_cast<const uint4*>(T->phi8)[1 << threadIdx.x];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int xm = lane & 15, h = lane >> 4;
   uint32_t* my_x = xch + warp * R1_XCH;
   uint4* my_t8 = lh + warp * 256;
-  uint4* my_p = pk_s + warp * 8;
   // points 4 xm + 2 h + {0, 1}: a b sums, then c sums of parity 0 and 1
   gf128 sum_ab[2], sum_c[4];
 #pragma unroll
@@ -332,20 +329,13 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
 #pragma unroll
     for (int j = 0; j < 16; j++) t[j] ^= shfl_xor64(t[j], 16);
     // eq-weighted phi8 table of this block (see the layout above)
-    if (lane < 8) {
-      const gf128 e = gf_load(&eq_out[xo]);
-      const uint4 f = phik[lane];
-      const gf128 p = gf_mul(gf128{{f.x, f.y, f.z, f.w}}, e);
-      my_p[lane] = make_uint4(p.w[0], p.w[1], p.w[2], p.w[3]);
-    }
-    __syncwarp();
     {
       // lane l writes T8[l + 32 i], i < 8: the part of bits 0..4 (l) once,
       // then the part of bits 5..7 (i) along a Gray walk, one XOR per entry;
       // a quarter warp's stores are 128 consecutive bytes
       uint4 pb[8];
 #pragma unroll
-      for (int k = 0; k < 8; k++) pb[k] = my_p[k];
+      for (int k = 0; k < 8; k++) pb[k] = eq_basis[xo * 8 + k];
       uint4 lo = make_uint4(0, 0, 0, 0);
 #pragma unroll
       for (int k = 0; k < 5; k++) {
@@ -417,6 +407,19 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
     gf128 acc = gf_zero();
     for (int w2 = 0; w2 < R1_WARPS; w2++) acc = gf_add(acc, red[w2 * 192 + col]);
     partials[(size_t)blockIdx.x * 192 + col] = acc;
+  }
+}
+
+// The basis of round 1's per-block tables: out[8 xo + k] = phi8(2^k) eq[xo]
+// for every outer block xo (eight products per block, all in parallel here
+// instead of on eight lanes of the block's warp).
+__global__ void __launch_bounds__(256)
+zc1_eq_basis_kernel(const gf128* __restrict__ eq, size_t n, const ZcRound1Tables* __restrict__ T,
+                    gf128* __restrict__ out) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * 8; i += (size_t)gridDim.x * blockDim.x) {
+    const uint64_t* f = T->phi8[1u << (i & 7)];
+    out[i] = gf_mul(gf128{{(uint32_t)f[0], (uint32_t)(f[0] >> 32), (uint32_t)f[1], (uint32_t)(f[1] >> 32)}},
+                    gf_load(&eq[i >> 3]));
   }
 }
 
@@ -771,17 +774,26 @@ __global__ void bind_pairs_kernel(const gf128* __restrict__ A, const gf128* __re
 
 }  // namespace
 
-int flock_launch_zc_round1(const void* a, const void* b, const void* c, size_t n_outer, const void* eq_out,
+int flock_launch_zc_round1(const void* a, const void* b, const void* c, size_t n_outer, const void* eq_basis,
                            const ZcRound1Tables* d_tables, void* partials, int grid, cudaStream_t st) {
   const size_t smem = R1_SMEM;
   flock_once_per_device((const void*)zc_round1_kernel, [] {
     cudaFuncSetAttribute(zc_round1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)R1_SMEM);
   });
   zc_round1_kernel<<<grid, R1_THREADS, smem, st>>>((const uint64_t*)a, (const uint64_t*)b, (const uint64_t*)c,
-                                                   n_outer, (const gf128*)eq_out, d_tables, (gf128*)partials); flock_count_launch();
+                                                   n_outer, (const uint4*)eq_basis, d_tables, (gf128*)partials); flock_count_launch();
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
+
+int flock_launch_zc1_eq_basis(const void* eq_out, size_t n_outer, const ZcRound1Tables* d_tables, void* out,
+                              cudaStream_t st) {
+  const size_t items = n_outer * 8;
+  const unsigned grid = (unsigned)std::min<size_t>((items + 255) / 256, (size_t)152 * 16);
+  zc1_eq_basis_kernel<<<grid, 256, 0, st>>>((const gf128*)eq_out, n_outer, d_tables, (gf128*)out);
+  flock_count_launch();
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
 
 int flock_launch_reduce_rows(const void* in, size_t count, int width, void* out, cudaStream_t st) {
   reduce_rows_kernel<<<(width + 7) / 8, 256, 0, st>>>((const gf128*)in, count, width, (gf128*)out); flock_count_launch();
