@@ -17,6 +17,15 @@
 namespace {
 
 constexpr int LEAF_THREADS = 128;
+// Parent levels folded into the leaf kernel by shuffles (at most 5). Zero:
+// a fused level runs one whole-warp compression for half as many parents as
+// the level before, so five levels cost 160 lane-compressions for 31 parents
+// of 32 leaves, while the parent kernel (full warps over 512 nodes per CTA)
+// does them in about 40 (the 2^20-leaf tree: 0.71 ms with five fused levels,
+// 0.62 / 0.63 ms with one / two, 0.61 ms with none).
+#ifndef MERKLE_WARP_LEVELS
+#define MERKLE_WARP_LEVELS 0
+#endif
 
 // Hashes `nblocks` 64-byte blocks of a chunk whose bytes this warp stages.
 // data points at the first byte of this warp's 32 leaves' chunk; leaf_stride
@@ -32,6 +41,15 @@ __device__ __forceinline__ void chunk_cv(const uint8_t* __restrict__ warp_base, 
     uint32_t len = chunk_bytes - off < 64 ? chunk_bytes - off : 64;
     // Stage block `blk` of all 32 leaves: 32 x 64 B, 16-byte granules.
     __syncwarp();
+    if (len == 64 && nlanes == 32) {
+      // whole blocks of a full warp: four unconditional 16-byte loads
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const int q = lane + 32 * i, leaf = q >> 2, part = q & 3;
+        reinterpret_cast<uint4*>(stage)[leaf * 4 + (leaf >> 1) + part] =
+            *reinterpret_cast<const uint4*>(warp_base + (size_t)leaf * leaf_stride + off + part * 16);
+      }
+    } else
     for (int q = lane; q < 32 * 4; q += 32) {
       int leaf = q >> 2, part = q & 3;
       uint4 v = make_uint4(0, 0, 0, 0);
@@ -207,7 +225,7 @@ int flock_launch_merkle(const void* d_data, size_t n_leaves, size_t leaf_bytes, 
     return FLOCK_ERR_SHAPE;
   size_t blocks = (n_leaves + LEAF_THREADS - 1) / LEAF_THREADS;
   int fuse = 0;
-  while (fuse < 5 && ((size_t)2 << fuse) <= n_leaves) fuse++;  // levels inside a warp of 32 leaves
+  while (fuse < MERKLE_WARP_LEVELS && ((size_t)2 << fuse) <= n_leaves) fuse++;  // levels inside a warp of 32 leaves
   if (n_leaves < 32) fuse = 0;
   if (leaf_bytes <= 1024)
     leaf_kernel<false><<<(unsigned)blocks, LEAF_THREADS, 0, st>>>((const uint8_t*)d_data, n_leaves,
