@@ -1224,9 +1224,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
         FK(flock_launch_glue_eq(bcur, len, S->eqlo.p, S->eqhi.p, lob, bp, st));
       }
     };
-    auto induce = [&](int nvars, const std::vector<Open>::value_type& op, const std::vector<uint32_t>& q,
-                      const std::vector<F>& alpha_v) {
-      (void)op;
+    auto induce = [&](int nvars, const std::vector<uint32_t>& q, const std::vector<F>& alpha_v) {
       const Sks& sk = sks_for(nvars);
       auto aw = eq_table(alpha_v);
       aw.resize(q.size());
@@ -1283,11 +1281,11 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     grind_nonces.push_back(grind((uint32_t)cfg.grind_bits[0]));
     auto q0 = sample_queries(tr, block0, cfg.queries[0]);
     auto a0 = tr.sample_vec(ilog2(cfg.queries[0]));
+    // the induced basis needs the queries only: its kernels are queued first
+    // and run while the host prepares the opening (multiproof indices)
+    void* dbs0 = induce(n1, q0, a0);
     Open open0 = open_rows(*S, dcw, dtree, block0, 1 << lbs, q0);
-    {
-      void* dbs = induce(n1, open0, q0, a0);
-      introduce(dbs);
-    }
+    introduce(dbs0);
     std::vector<Open> rec_opens;
     std::vector<F> yr;
     Open final_open;
@@ -1322,9 +1320,8 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       grind_nonces.push_back(grind((uint32_t)cfg.grind_bits[i + 1]));
       auto qi = sample_queries(tr, prev_block, cfg.queries[i + 1]);
       auto ai = tr.sample_vec(ilog2(cfg.queries[i + 1]));
-      Open oi = open_rows(*S, S->lvl_cw[slot].p, S->lvl_tree[slot].p, prev_block, prev_width, qi);
-      void* dbs = induce(n_next, oi, qi, ai);
-      rec_opens.push_back(std::move(oi));
+      void* dbs = induce(n_next, qi, ai);
+      rec_opens.push_back(open_rows(*S, S->lvl_cw[slot].p, S->lvl_tree[slot].p, prev_block, prev_width, qi));
       introduce(dbs);
       slot = ns;
       prev_block = (size_t)1 << (n_next - lni2 + rate2);
