@@ -65,8 +65,8 @@ NTT_INSTR_PER_TABLE_PRODUCT = 160
 NTT_INSTR_PER_MULTIPLY_BUTTERFLY = 259
 # Zerocheck round 1 at m = 30 (2^17 outer blocks of 128 rows): warp
 # instructions and DRAM bytes (read + write) of one launch, per outer block.
-ZC1_WARP_INSTR_PER_OUTER = 786345072 / 2**17
-ZC1_DRAM_BYTES_PER_OUTER = (404989184 + 3690496) / 2**17
+ZC1_WARP_INSTR_PER_OUTER = 603870960 / 2**17
+ZC1_DRAM_BYTES_PER_OUTER = (419600128 + 3706624) / 2**17
 
 
 def load_peaks():
