@@ -215,8 +215,8 @@ __device__ __forceinline__ uint64_t shfl_xor64(uint64_t v, int m) {
 //        sums of its basis phi8(2^k) e, k < 8 (phi8 is additive), which
 //        zc1_eq_basis_kernel computes for every block beforehand. One lookup per
 //        value: the random bytes of a quarter warp share bank groups at times
-//        (about 2.6 wavefronts per quarter-warp lookup), which the load/store
-//        pipe absorbs; with two nibble tables L[v & 15] + H[v >> 4] in eight
+//        (about two wavefronts per quarter-warp lookup, measured), which the
+//        load/store pipe absorbs; with two nibble tables L[v & 15] + H[v >> 4] in eight
 //        conflict-free replicas (the same 4 KiB) each value took two lookups,
 //        two index computations and a four-word XOR on the busy ALU pipe;
 //   xch  per warp: [16 producer rows] of 20 words (64 bytes used; the odd
@@ -239,8 +239,8 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
                  gf128* __restrict__ partials) {
   extern __shared__ uint4 sm[];
   uint4* ext = sm;                                                   // [4][256][8]
-  uint4* lh = ext + 8 * 4 * 256;                                     // per warp T8[256]
-  uint32_t* xch = reinterpret_cast<uint32_t*>(lh + R1_WARPS * 256);  // per warp [R1_XCH]
+  uint4* t8 = ext + 8 * 4 * 256;                                     // per warp T8[256]
+  uint32_t* xch = reinterpret_cast<uint32_t*>(t8 + R1_WARPS * 256);  // per warp [R1_XCH]
   const uint64_t* ext_src = &T->ext[0][0][0];
   for (int i = threadIdx.x; i < 8 * 4 * 256; i += R1_THREADS) {
     const int q = i >> 11, v = (i >> 3) & 255, c = i & 7;
@@ -251,7 +251,7 @@ zc_round1_kernel(const uint64_t* __restrict__ A, const uint64_t* __restrict__ B,
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int xm = lane & 15, h = lane >> 4;
   uint32_t* my_x = xch + warp * R1_XCH;
-  uint4* my_t8 = lh + warp * 256;
+  uint4* my_t8 = t8 + warp * 256;
   // points 4 xm + 2 h + {0, 1}: a b sums, then c sums of parity 0 and 1
   gf128 sum_ab[2], sum_c[4];
 #pragma unroll
