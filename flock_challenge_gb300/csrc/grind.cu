@@ -5,11 +5,14 @@
 // least `bits` leading zero bits, read MSB-first from byte 0. Each thread
 // tests one nonce of a window and lowers a device minimum with atomicMin; the
 // host scans windows in increasing order and stops at the first window with a
-// hit, so the result is the global minimum.
+// hit, so the result is the global minimum. Grinds of a few bits (about 2^bits
+// hashes) are cheaper on the host than a launch and a wait: they test the
+// nonces in increasing order there.
 #include <cstring>
 
 #include "blake3.cuh"
 #include "flock_internal.h"
+#include "host_blake3.h"
 
 namespace {
 
@@ -53,6 +56,29 @@ __global__ void grind_kernel(const __grid_constant__ Digest digest, uint64_t sta
   if (leading_zeros_ok(cv, bits)) atomicMin(best, (unsigned long long)nonce);
 }
 
+// Grinds of at most this many bits run on the host: about 2^bits hashes of
+// ~0.1 us each against a kernel launch and a wait for its result (~13 us of
+// idle device per grind).
+constexpr uint32_t kHostGrindBits = 6;
+
+bool host_pow(const uint32_t dg[8], uint64_t nonce, uint32_t bits) {
+  uint32_t m[16] = {0}, o[16];
+  for (int k = 0; k < 8; k++) m[k] = dg[k];
+  m[8] = (uint32_t)nonce;
+  m[9] = (uint32_t)(nonce >> 32);
+  hb3::compress(hb3::IV, m, 0, 64, hb3::CHUNK_START | hb3::CHUNK_END | hb3::ROOT, o);
+  for (uint32_t k = 0; k < 32 && bits > 0; k++) {
+    const uint32_t byte = (o[k >> 2] >> (8 * (k & 3))) & 255;
+    if (bits >= 8) {
+      if (byte) return false;
+      bits -= 8;
+    } else {
+      return (byte >> (8 - bits)) == 0;
+    }
+  }
+  return true;
+}
+
 }  // namespace
 
 // Returns the smallest satisfying nonce. d_scratch: >= 16 bytes of device
@@ -69,6 +95,17 @@ int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, int* p
     return FLOCK_OK;
   }
   if (bits > 60) return FLOCK_ERR_SHAPE;
+  Digest dg;
+  memcpy(dg.w, digest, 32);
+  if (bits <= kHostGrindBits) {
+    // in increasing order, as the windows below; the result slots are left
+    // alone, so the alternation of the device grinds is unchanged
+    for (uint64_t n = 0; n < ((uint64_t)1 << 20); n++)
+      if (host_pow(dg.w, n, bits)) {
+        *nonce = n;
+        return FLOCK_OK;
+      }
+  }
   unsigned long long* d_best = (unsigned long long*)d_scratch;
   unsigned long long* d_other = nullptr;
   if (parity) {
@@ -76,8 +113,6 @@ int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, int* p
     d_other = (unsigned long long*)d_scratch + ((*parity & 1) ^ 1);
     ++*parity;
   }
-  Digest dg;
-  memcpy(dg.w, digest, 32);
   const unsigned long long none = ~0ull;
   if (!parity && cudaMemsetAsync(d_best, 0xFF, 8, st) != cudaSuccess) return FLOCK_ERR_CUDA;
   // About two expected hits per window: a miss costs one more window, an
