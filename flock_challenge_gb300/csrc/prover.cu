@@ -295,7 +295,8 @@ constexpr int kKernelSpans = 4;  // witness, L0 NTT, L0 Merkle tree, zerocheck r
 
 struct ProverState {
   int device = 0;
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr;  // the stream in use: st_normal or st_high
+  cudaStream_t st_normal = nullptr, st_high = nullptr;
   ZcRound1Tables* d_r1t = nullptr;
   DBuf in, z, a, b, stripe, cw, tree, A0, B0, A1, B1, eqlo, eqhi, eqout, rdev, part, red, lag, small, eqin, comb,
       zvec, zvec0, tlo0, thi0, tlo1, thi1, tables, bc, f1, b1, W, LO, HI, basis, qbuf, abuf, rows, nidx, nodes,
@@ -513,6 +514,14 @@ ProverState* flock_prover_create(int device) {
     delete S;
     return nullptr;
   }
+  S->st_normal = S->st;
+  // the high-priority stream (flock_prover_set_priority); without one, the
+  // prover keeps its normal stream
+  int least = 0, greatest = 0;
+  if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&S->st_high, cudaStreamNonBlocking, greatest) != cudaSuccess)
+    S->st_high = nullptr;
+  cudaGetLastError();
   // Without pinned staging the copies still work, through the driver's own.
   void* pin = nullptr;
   if (cudaMallocHost(&pin, kPinH2D + kPinD2H) == cudaSuccess) S->pin = (uint8_t*)pin;
@@ -535,7 +544,8 @@ void flock_prover_destroy(ProverState* S) {
   for (cudaEvent_t e : S->tev)
     if (e) cudaEventDestroy(e);
   if (S->d_r1t) cudaFree(S->d_r1t);
-  if (S->st) cudaStreamDestroy(S->st);
+  if (S->st_normal) cudaStreamDestroy(S->st_normal);
+  if (S->st_high) cudaStreamDestroy(S->st_high);
   if (S->pin) cudaFreeHost(S->pin);
   if (S->pin_open) cudaFreeHost(S->pin_open);
   if (S->mapped) cudaFreeHost(S->mapped);
@@ -572,6 +582,14 @@ int flock_prover_kernel_times(const ProverState* S, double* ms, int n) {
   return FLOCK_OK;
 }
 cudaStream_t flock_prover_stream(const ProverState* S) { return S->st; }
+
+void flock_prover_set_priority(ProverState* S, bool high) {
+  cudaStream_t want = high && S->st_high ? S->st_high : S->st_normal;
+  if (want == S->st) return;
+  cudaSetDevice(S->device);
+  cudaStreamSynchronize(S->st);  // the previous proof's work is done before its buffers change streams
+  S->st = want;
+}
 
 int flock_prover_prove_seed(ProverState* S, int log2, uint64_t seed, std::vector<uint8_t>& out) {
   try {

@@ -40,6 +40,10 @@ int flock_prover_prove(ProverState* s, const flock_compression* in, size_t n, in
                        bool input_on_device = false, const ChainReq* chain = nullptr, fs::Transcript* tr = nullptr,
                        flock_r1cs_claim* claim = nullptr);
 cudaStream_t flock_prover_stream(const ProverState* s);
+// Proofs from now on run on the prover's high-priority stream (high) or its
+// normal one: the device dispatches blocks of high-priority kernels first.
+// Waits for the prover's outstanding work when the stream changes.
+void flock_prover_set_priority(ProverState* s, bool high);
 // Generates the 2^log2 benchmark inputs of `seed` on the device, then proves them.
 int flock_prover_prove_seed(ProverState* s, int log2, uint64_t seed, std::vector<uint8_t>& out);
 const FlockPhaseTimes& flock_prover_times(const ProverState* s);
