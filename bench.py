@@ -269,14 +269,19 @@ def kernel_microbench(F, ctx_handle, peaks, torch, dev, rows_logs=(16, 18, 20), 
 
 def ntt_l0_structure(F, dev_index, log_d):
     """(table passes, total passes, table-pass end layer, multiply-pass shape) of
-    the L0 commit NTT, by the library's rule: two-layer byte-table passes while
-    a block holds >= 2^9 quad-lanes, then multiply passes of the tuned shape."""
-    F.lib().flock_ntt_tuned_variant.argtypes = [ctypes.c_int] * 4
-    variant = F.lib().flock_ntt_tuned_variant(dev_index, log_d, 6, 1)
+    the L0 commit NTT as the library's autotuner chose them: two-layer
+    byte-table passes from layer 1 to the tuned end layer, then multiply passes
+    of the tuned shape (the untuned default when the shape has not run)."""
+    L = F.lib()
+    L.flock_ntt_tuned_variant.argtypes = [ctypes.c_int] * 4
+    L.flock_ntt_tuned_table_end.argtypes = [ctypes.c_int] * 4
+    variant = L.flock_ntt_tuned_variant(dev_index, log_d, 6, 1)
     max_f = NTT_MAX_LAYERS.get(variant, 6)
-    tab_end = 1
-    while tab_end + 1 < log_d and log_d - tab_end - 2 + 6 >= 9:
-        tab_end += 2
+    tab_end = L.flock_ntt_tuned_table_end(dev_index, log_d, 6, 1)
+    if tab_end < 0:  # the default depth: blocks of >= 2^9 quad-lanes
+        tab_end = 1
+        while tab_end + 1 < log_d and log_d - tab_end - 2 + 6 >= 9:
+            tab_end += 2
     tab_passes = (tab_end - 1) // 2
     passes = tab_passes + (log_d - tab_end + max_f - 1) // max_f
     return tab_passes, passes, tab_end, variant, max_f

@@ -11,21 +11,25 @@
 // each warp stages its 32 leaves' current 64-byte blocks through shared memory
 // so the global reads are coalesced 2 KiB runs. Parent levels are reduced
 // 512 nodes per CTA in shared memory (nine levels per launch).
+#include <cstdlib>
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "blake3.cuh"
 #include "flock_internal.h"
 
 namespace {
 
 constexpr int LEAF_THREADS = 128;
-// Parent levels folded into the leaf kernel by shuffles (at most 5). Zero:
-// a fused level runs one whole-warp compression for half as many parents as
-// the level before, so five levels cost 160 lane-compressions for 31 parents
-// of 32 leaves, while the parent kernel (full warps over 512 nodes per CTA)
-// does them in about 40 (the 2^20-leaf tree: 0.71 ms with five fused levels,
-// 0.62 / 0.63 ms with one / two, 0.61 ms with none).
-#ifndef MERKLE_WARP_LEVELS
-#define MERKLE_WARP_LEVELS 0
-#endif
+// Parent levels folded into the leaf kernel by shuffles (at most 5): a fused
+// level runs one whole-warp compression for half as many parents as the level
+// before, so five levels cost 160 lane-compressions for 31 parents of 32
+// leaves, while the parent kernel (full warps over 512 nodes per CTA) does
+// them in about 40 (the 2^20-leaf tree: 0.71 ms with five fused levels,
+// 0.62 / 0.63 ms with one / two, 0.61 ms with none). The autotuner below
+// picks among 0..kMaxTunedWarpLevels per tree shape; untuned calls use none.
+constexpr int kMaxTunedWarpLevels = 2;
 
 // Hashes `nblocks` 64-byte blocks of a chunk whose bytes this warp stages.
 // data points at the first byte of this warp's 32 leaves' chunk; leaf_stride
@@ -219,13 +223,14 @@ parent_kernel(uint32_t* __restrict__ tree, size_t level_off, size_t level_len, i
 
 }  // namespace
 
-int flock_launch_merkle(const void* d_data, size_t n_leaves, size_t leaf_bytes, void* d_tree, cudaStream_t st) {
-  if (n_leaves == 0 || (n_leaves & (n_leaves - 1)) || leaf_bytes == 0 || leaf_bytes % 16 ||
-      (leaf_bytes > 1024 && (leaf_bytes % 1024 || leaf_bytes > 4096)))
-    return FLOCK_ERR_SHAPE;
+namespace {
+
+// The leaf kernel with `levels` fused parent levels (fewer where the tree or
+// a warp's 32 leaves have fewer), then the parent kernels up to the root.
+int launch_tree(const void* d_data, size_t n_leaves, size_t leaf_bytes, void* d_tree, int levels, cudaStream_t st) {
   size_t blocks = (n_leaves + LEAF_THREADS - 1) / LEAF_THREADS;
   int fuse = 0;
-  while (fuse < MERKLE_WARP_LEVELS && ((size_t)2 << fuse) <= n_leaves) fuse++;  // levels inside a warp of 32 leaves
+  while (fuse < levels && ((size_t)2 << fuse) <= n_leaves) fuse++;  // levels inside a warp of 32 leaves
   if (n_leaves < 32) fuse = 0;
   if (leaf_bytes <= 1024)
     leaf_kernel<false><<<(unsigned)blocks, LEAF_THREADS, 0, st>>>((const uint8_t*)d_data, n_leaves,
@@ -253,5 +258,75 @@ int flock_launch_merkle(const void* d_data, size_t n_leaves, size_t leaf_bytes, 
       len >>= 1;
     }
   }
+  return FLOCK_OK;
+}
+
+// ---- autotuner: fused parent levels per tree shape --------------------------
+//
+// The first tree of a (device, leaves, leaf bytes) shape with at least
+// kTuneMinLeaves leaves is built once per candidate level count (every build
+// writes the same tree, so the caller's tree is final whichever is last), timed
+// with CUDA events on the caller's stream; later trees of the shape use the
+// fastest. FLOCK_MERKLE_TUNE=0 in the environment turns tuning off.
+constexpr size_t kTuneMinLeaves = (size_t)1 << 12;
+struct MerkleKey {
+  int dev;
+  size_t leaves, leaf_bytes;
+  bool operator<(const MerkleKey& o) const {
+    return std::tie(dev, leaves, leaf_bytes) < std::tie(o.dev, o.leaves, o.leaf_bytes);
+  }
+};
+std::mutex g_mtune_mu;
+std::map<MerkleKey, int> g_mtuned;
+
+bool merkle_tuning_enabled() {
+  const char* e = std::getenv("FLOCK_MERKLE_TUNE");
+  return !(e && e[0] == '0');
+}
+
+}  // namespace
+
+extern "C" int flock_merkle_tuned_levels(int device, size_t n_leaves, size_t leaf_bytes) {
+  std::lock_guard<std::mutex> lk(g_mtune_mu);
+  auto it = g_mtuned.find(MerkleKey{device, n_leaves, leaf_bytes});
+  return it == g_mtuned.end() ? -1 : it->second;
+}
+
+int flock_launch_merkle(const void* d_data, size_t n_leaves, size_t leaf_bytes, void* d_tree, cudaStream_t st) {
+  if (n_leaves == 0 || (n_leaves & (n_leaves - 1)) || leaf_bytes == 0 || leaf_bytes % 16 ||
+      (leaf_bytes > 1024 && (leaf_bytes % 1024 || leaf_bytes > 4096)))
+    return FLOCK_ERR_SHAPE;
+  if (n_leaves < kTuneMinLeaves || !merkle_tuning_enabled()) return launch_tree(d_data, n_leaves, leaf_bytes, d_tree, 0, st);
+  MerkleKey k{0, n_leaves, leaf_bytes};
+  cudaGetDevice(&k.dev);
+  {
+    std::lock_guard<std::mutex> lk(g_mtune_mu);
+    auto it = g_mtuned.find(k);
+    if (it != g_mtuned.end()) return launch_tree(d_data, n_leaves, leaf_bytes, d_tree, it->second, st);
+  }
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return FLOCK_ERR_CUDA;
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return FLOCK_ERR_CUDA;
+  }
+  int best = 0, rc = FLOCK_OK;
+  float best_ms = 1e30f;
+  for (int levels = 0; levels <= kMaxTunedWarpLevels && rc == FLOCK_OK; levels++) {
+    cudaEventRecord(e0, st);
+    rc = launch_tree(d_data, n_leaves, leaf_bytes, d_tree, levels, st);
+    cudaEventRecord(e1, st);
+    float ms = 0;
+    if (rc == FLOCK_OK && cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess &&
+        ms < best_ms) {
+      best_ms = ms;
+      best = levels;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != FLOCK_OK) return rc;
+  std::lock_guard<std::mutex> lk(g_mtune_mu);
+  g_mtuned[k] = best;
   return FLOCK_OK;
 }

@@ -445,15 +445,17 @@ ntt_tab2_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t s
 }
 
 // Layers [start, end) handled by table passes: pairs of layers while a block
-// of the pass's first layer l holds at least 2^kTabMinLog quad-lanes (its three
-// tables are then built for at least 2 K products; deeper blocks are left to
-// the multiply passes). Measured at 2^20 positions x 64 lanes: 2^9 beats 2^11
-// by 0.3 ms (one more table pass, two layers fewer in the multiply pass), 2^8
-// ties and 2^7 (a lone last layer in the multiply pass) loses 2.2 ms.
+// of the pass's first layer l holds at least 2^min_log quad-lanes (its three
+// tables are then built for at least 4 x 2^min_log products; deeper blocks are
+// left to the multiply passes). The autotuner picks min_log per transform
+// shape among kTabMinLogs; the default, for untuned calls, is kTabMinLog
+// (measured at 2^20 positions x 64 lanes: 2^9 beats 2^11 by 0.3 ms, 2^8 ties
+// and 2^7, a lone last layer in the multiply pass, loses 2.2 ms).
 constexpr int kTabMinLog = 9;
-int tab_layers_end(int log_d, int log_lanes, int start) {
+constexpr int kTabMinLogs[] = {8, 9, 10};
+int tab_layers_end(int log_d, int log_lanes, int start, int min_log = kTabMinLog) {
   int l = start;
-  while (l + 1 < log_d && log_d - l - 2 + log_lanes >= kTabMinLog) l += 2;
+  while (l + 1 < log_d && log_d - l - 2 + log_lanes >= min_log) l += 2;
   return l;
 }
 
@@ -541,14 +543,17 @@ const void* flock_ntt_twiddles_prepared(int log_d) {
   return d;
 }
 
-// ---- pass-shape autotuner -----------------------------------------------
+// ---- autotuner -------------------------------------------------------------
 //
-// Per (device, log_d, lanes, start layer), the first call times every pass
-// variant on a scratch buffer of the same shape (two runs each, CUDA events
-// on the caller's stream) and keeps the fastest for later calls. The variants
-// compute identical results; only speed differs. FLOCK_NTT_TUNE=0 in the
-// environment turns tuning off (the default variant everywhere);
-// FLOCK_NTT_VARIANT=0|1|2 fixes one shape.
+// Per (device, log_d, lanes, start layer), the first call times on a scratch
+// buffer of the same shape (CUDA events on the caller's stream, one warm-up
+// and two timed runs per candidate): the table passes for each table depth of
+// kTabMinLogs, and the multiply passes of every pass shape from each depth's
+// end layer; it keeps the pair with the smallest sum for later calls. All
+// candidates compute identical results; only speed differs.
+// FLOCK_NTT_TUNE=0 in the environment turns tuning off (the default depth and
+// shape everywhere); FLOCK_NTT_VARIANT=0|1|2 fixes the multiply-pass shape
+// (with the default depth).
 namespace {
 
 struct TuneKey {
@@ -557,55 +562,88 @@ struct TuneKey {
     return std::tie(dev, log_d, log_lanes, start) < std::tie(o.dev, o.log_d, o.log_lanes, o.start);
   }
 };
+struct TunedShape {
+  int tab_end;  // table passes cover layers [start, tab_end)
+  int variant;  // multiply-pass shape of the layers [tab_end, log_d)
+};
 std::mutex g_tune_mu;
-std::map<TuneKey, int> g_tuned;
+std::map<TuneKey, TunedShape> g_tuned;
 
 bool tuning_enabled() {
   const char* e = std::getenv("FLOCK_NTT_TUNE");
   return !(e && e[0] == '0');
 }
 
-int tune_variant(const TuneKey& k, const void* tw, cudaStream_t st) {
+// Table passes of layers [from, to) in place on d.
+int run_tab_passes(gf128* d, const gf128* twp, int log_d, int log_lanes, int from, int to, cudaStream_t st) {
+  for (int l = from; l + 2 <= to; l += 2) {
+    const int rc = launch_tab2(d, d, ~(size_t)0, twp, log_d, log_lanes, l, st);
+    if (rc != FLOCK_OK) return rc;
+  }
+  return FLOCK_OK;
+}
+
+TunedShape tune_shape(const TuneKey& k, const void* tw, const gf128* twp, cudaStream_t st) {
+  TunedShape best{tab_layers_end(k.log_d, k.log_lanes, k.start), kDefaultVariant};
   const size_t bytes = ((size_t)16 << k.log_lanes) << k.log_d;
   void* scratch = nullptr;
   if (cudaMalloc(&scratch, bytes) != cudaSuccess) {
     cudaGetLastError();
-    return kDefaultVariant;
+    return best;
   }
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  int best = kDefaultVariant;
-  float best_ms = 1e30f;
   gf128* d = (gf128*)scratch;
   cudaMemsetAsync(scratch, 0, bytes, st);
-  for (int v = 0; v < kVariants; v++) {
-    if (run_passes<true>(v, d, d, ~(size_t)0, tw, k.log_d, k.log_lanes, k.start, st) != FLOCK_OK) continue;
+  // ms of fn over two runs after a warm-up one; infinity when a launch fails
+  auto time_of = [&](auto&& fn) {
+    if (fn() != FLOCK_OK) return 1e30f;
     cudaEventRecord(e0, st);
-    bool ok = true;
-    for (int rep = 0; rep < 2 && ok; rep++)
-      ok = run_passes<true>(v, d, d, ~(size_t)0, tw, k.log_d, k.log_lanes, k.start, st) == FLOCK_OK;
+    bool ok = fn() == FLOCK_OK && fn() == FLOCK_OK;
     cudaEventRecord(e1, st);
     float ms = 0;
-    if (ok && cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess &&
-        ms < best_ms) {
-      best_ms = ms;
-      best = v;
+    if (!ok || cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+      return 1e30f;
+    return ms;
+  };
+  std::map<int, float> tab_ms;                    // per table end layer
+  std::map<std::pair<int, int>, float> mult_ms;  // per (table end layer, shape)
+  float best_ms = 1e30f;
+  for (int ml : kTabMinLogs) {
+    const int te = tab_layers_end(k.log_d, k.log_lanes, k.start, ml);
+    if (te > k.start && !twp) continue;
+    if (!tab_ms.count(te))
+      tab_ms[te] = te == k.start ? 0.f
+                                 : time_of([&] { return run_tab_passes(d, twp, k.log_d, k.log_lanes, k.start, te, st); });
+    for (int v = 0; v < kVariants; v++) {
+      const auto key = std::make_pair(te, v);
+      if (!mult_ms.count(key))
+        mult_ms[key] = te == k.log_d ? 0.f : time_of([&] {
+          return run_passes<true>(v, d, d, ~(size_t)0, tw, k.log_d, k.log_lanes, te, st);
+        });
+      const float t = tab_ms[te] + mult_ms[key];
+      if (t < best_ms) {
+        best_ms = t;
+        best = TunedShape{te, v};
+      }
     }
   }
   cudaStreamSynchronize(st);
+  cudaGetLastError();
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(scratch);
   return best;
 }
 
-int pick_variant(int log_d, int log_lanes, int start, const void* tw, cudaStream_t st) {
+TunedShape pick_shape(int log_d, int log_lanes, int start, const void* tw, const gf128* twp, cudaStream_t st) {
+  const TunedShape dflt{tab_layers_end(log_d, log_lanes, start), kDefaultVariant};
   if (const char* f = std::getenv("FLOCK_NTT_VARIANT")) {  // a fixed shape, for measurements
     const int v = f[0] - '0';
-    if (v >= 0 && v < kVariants) return v;
+    if (v >= 0 && v < kVariants) return TunedShape{dflt.tab_end, v};
   }
-  if (!tuning_enabled()) return kDefaultVariant;
+  if (!tuning_enabled()) return dflt;
   TuneKey k{0, log_d, log_lanes, start};
   cudaGetDevice(&k.dev);
   {
@@ -613,20 +651,24 @@ int pick_variant(int log_d, int log_lanes, int start, const void* tw, cudaStream
     auto it = g_tuned.find(k);
     if (it != g_tuned.end()) return it->second;
   }
-  const int v = tune_variant(k, tw, st);
+  const TunedShape sh = tune_shape(k, tw, twp, st);
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  g_tuned[k] = v;
-  return v;
+  g_tuned[k] = sh;
+  return sh;
 }
 
 }  // namespace
 
 extern "C" int flock_ntt_tuned_variant(int device, int log_d, int log_lanes, int start_layer) {
-  // the tuned multiply passes start where the table passes end
-  const int l = tab_layers_end(log_d, log_lanes, start_layer);
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  auto it = g_tuned.find(TuneKey{device, log_d, log_lanes, l});
-  return it == g_tuned.end() ? -1 : it->second;
+  auto it = g_tuned.find(TuneKey{device, log_d, log_lanes, start_layer});
+  return it == g_tuned.end() ? -1 : it->second.variant;
+}
+
+extern "C" int flock_ntt_tuned_table_end(int device, int log_d, int log_lanes, int start_layer) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tuned.find(TuneKey{device, log_d, log_lanes, start_layer});
+  return it == g_tuned.end() ? -1 : it->second.tab_end;
 }
 
 // Applies layers [start_layer, log_d) in passes whose shape the autotuner
@@ -653,12 +695,14 @@ int flock_launch_ntt(void* d_data, const void* d_src, int log_d, int log_lanes, 
     }
     return FLOCK_OK;
   }
-  // upper layers in table passes, then the multiply passes of the tuned shape
+  // upper layers in table passes, then the multiply passes, of the tuned
+  // depth and shape
   int l = start_layer;
-  const int tab_end = tab_layers_end(log_d, log_lanes, start_layer);
+  const gf128* twp = (const gf128*)flock_ntt_twiddles(log_d);
+  if (!twp) return FLOCK_ERR_OOM;
+  const TunedShape sh = pick_shape(log_d, log_lanes, start_layer, tw, twp, stream);
+  const int tab_end = sh.tab_end;
   if (tab_end > l) {
-    const gf128* twp = (const gf128*)flock_ntt_twiddles(log_d);
-    if (!twp) return FLOCK_ERR_OOM;
     for (; l + 2 <= tab_end; l += 2) {
       int rc = launch_tab2(data, src, mask, twp, log_d, log_lanes, l, stream);
       if (rc != FLOCK_OK) return rc;
@@ -667,8 +711,7 @@ int flock_launch_ntt(void* d_data, const void* d_src, int log_d, int log_lanes, 
     }
   }
   if (l == log_d) return FLOCK_OK;
-  const int v = pick_variant(log_d, log_lanes, l, tw, stream);
-  return run_passes<true>(v, data, src, mask, tw, log_d, log_lanes, l, stream);
+  return run_passes<true>(sh.variant, data, src, mask, tw, log_d, log_lanes, l, stream);
 }
 
 // ---- NTT without device allocation -----------------------------------------

@@ -88,14 +88,26 @@ int flock_witness(const flock_compression* d_in, size_t n, int n_blocks_log, voi
  * (crates/flock-core/src/ntt/additive_ntt_f128.rs:599-622). */
 int flock_ntt(flock_ctx* ctx, void* d_data, int log_d, int log_num_ntts, int start_layer, void* stream);
 
-/* Pass shape (0, 1, 2: 4, 8 or 16 positions per thread) the NTT autotuner
- * chose for a transform shape on `device`, or -1 if that shape has not run
- * yet. The first flock_ntt / commit / proof of a shape times the shapes on a
- * scratch buffer and keeps the fastest; FLOCK_NTT_TUNE=0 in the environment
- * disables tuning. The shape applies to the multiply passes: the upper
- * layers, whose blocks hold at least 2^9 position-quads x lanes, run as
- * byte-table passes of two layers. No reference counterpart. */
+/* The NTT autotuner's choice for a transform shape (2^log_d positions x
+ * 2^log_lanes lanes from start_layer) on `device`, or -1 if that shape has not
+ * run yet: the multiply-pass shape (0, 1, 2: 4, 8 or 16 positions per thread)
+ * and the end layer of the byte-table passes (the upper layers run as
+ * two-layer table passes while a block holds at least 2^k position-quads x
+ * lanes, k tuned among 8, 9, 10; the layers from the end layer on run as
+ * multiply passes). The first flock_ntt / commit / proof of a shape times the
+ * candidates on a scratch buffer and keeps the fastest; FLOCK_NTT_TUNE=0 in the
+ * environment disables tuning (k = 9, shape 1). No reference counterpart. */
 int flock_ntt_tuned_variant(int device, int log_d, int log_lanes, int start_layer);
+int flock_ntt_tuned_table_end(int device, int log_d, int log_lanes, int start_layer);
+
+/* The Merkle autotuner's choice for a tree shape (n_leaves leaves of
+ * leaf_bytes) on `device`, or -1 if that shape has not run yet (or has fewer
+ * than 2^12 leaves, which are never tuned): how many parent levels (0..2) the
+ * leaf kernel folds in by warp shuffles before the parent kernels take over.
+ * The first tree of a shape is built once per candidate and timed (every build
+ * writes the same tree); FLOCK_MERKLE_TUNE=0 in the environment disables
+ * tuning (no fused levels). No reference counterpart. */
+int flock_merkle_tuned_levels(int device, size_t n_leaves, size_t leaf_bytes);
 
 /* Largest log_d flock_ntt_noalloc accepts (2^16 positions per transform). */
 #define FLOCK_NTT_NOALLOC_MAX_LOG_D 16

@@ -101,12 +101,20 @@ def test_ntt_autotuner_records_a_shape_and_keeps_results(ctx, monkeypatch):
     import ctypes
     L = F.lib()
     L.flock_ntt_tuned_variant.argtypes = [ctypes.c_int] * 4
+    L.flock_ntt_tuned_table_end.argtypes = [ctypes.c_int] * 4
     rng = np.random.default_rng(5)
     data = rng.integers(0, 2**63, (1 << (15 + 4)) * 2, dtype=np.uint64)
     ref = O.ntt_interleaved(data, 16, 1)
     d = to_dev(data)
     F.ntt(ctx, d, 15, 4, 1)
     assert L.flock_ntt_tuned_variant(0, 15, 4, 1) in (0, 1, 2)
+    # table passes of two layers from the start layer, ending where blocks
+    # hold 2^8..2^10 quad-lanes (the tuned depth)
+    te = L.flock_ntt_tuned_table_end(0, 15, 4, 1)
+    assert (te - 1) % 2 == 0 and 1 <= te <= 15
+    assert np.array_equal(host(d).view(np.uint64), ref)
+    d = to_dev(data)
+    F.ntt(ctx, d, 15, 4, 1)  # the tuned shape again: the same result
     assert np.array_equal(host(d).view(np.uint64), ref)
     # tuning off: the default shape, same result, nothing recorded
     monkeypatch.setenv("FLOCK_NTT_TUNE", "0")
@@ -115,6 +123,27 @@ def test_ntt_autotuner_records_a_shape_and_keeps_results(ctx, monkeypatch):
     F.ntt(ctx, d2, 14, 4, 1)
     assert L.flock_ntt_tuned_variant(0, 14, 4, 1) == -1
     assert np.array_equal(host(d2).view(np.uint64), O.ntt_interleaved(data2, 16, 1))
+
+
+def test_merkle_autotuner_records_levels_and_keeps_the_tree(cuda_device, monkeypatch):
+    import ctypes
+    L = F.lib()
+    L.flock_merkle_tuned_levels.argtypes = [ctypes.c_int, ctypes.c_size_t, ctypes.c_size_t]
+    rng = np.random.default_rng(12)
+    n, leaf = 1 << 12, 64
+    data = rng.integers(0, 256, n * leaf, dtype=np.uint8)
+    ref = O.merkle_tree(data, n)
+    tree = F.merkle_tree(to_dev(data), n, leaf)  # tuned here: every candidate writes the same tree
+    assert L.flock_merkle_tuned_levels(0, n, leaf) in (0, 1, 2)
+    assert np.array_equal(host(tree).reshape(-1, 32), ref)
+    tree = F.merkle_tree(to_dev(data), n, leaf)  # the tuned level count
+    assert np.array_equal(host(tree).reshape(-1, 32), ref)
+    # tuning off: nothing recorded for a new shape, the same tree
+    monkeypatch.setenv("FLOCK_MERKLE_TUNE", "0")
+    data2 = rng.integers(0, 256, n * 32, dtype=np.uint8)
+    tree2 = F.merkle_tree(to_dev(data2), n, 32)
+    assert L.flock_merkle_tuned_levels(0, n, 32) == -1
+    assert np.array_equal(host(tree2).reshape(-1, 32), O.merkle_tree(data2, n))
 
 
 @pytest.mark.parametrize("variant", ["0", "1", "2"])
