@@ -71,22 +71,52 @@ __device__ __forceinline__ void cb_build_tables(size_t h, const gf128* __restric
   __syncthreads();
 }
 
-// b[p] for the low indices u0 = lo0[j], u1 = lo1[j]: 2 x 16 table lookups,
-// lane l starting at byte position l mod 16 (eight consecutive lanes read
-// eight distinct bank groups: conflict-free random lookups).
+// The bytes of u permuted so that byte st of p is byte st ^ rot of u (rot < 16):
+// a half swap for bit 3 of rot, a word swap for bit 2, a byte permutation
+// within each word for bits 0..1.
+__device__ __forceinline__ void cb_permute(const gf128& u, int rot, uint32_t p[4]) {
+  const bool s8 = rot & 8, s4 = rot & 4;
+  const uint32_t a0 = s8 ? u.w[2] : u.w[0], a1 = s8 ? u.w[3] : u.w[1];
+  const uint32_t a2 = s8 ? u.w[0] : u.w[2], a3 = s8 ? u.w[1] : u.w[3];
+  const uint32_t x3 = rot & 3;
+  const uint32_t sel = x3 == 0 ? 0x3210u : x3 == 1 ? 0x2301u : x3 == 2 ? 0x1032u : 0x0123u;
+  p[0] = __byte_perm(s4 ? a1 : a0, 0, sel);
+  p[1] = __byte_perm(s4 ? a0 : a1, 0, sel);
+  p[2] = __byte_perm(s4 ? a3 : a2, 0, sel);
+  p[3] = __byte_perm(s4 ? a2 : a3, 0, sel);
+}
+
+// b[p] for the low indices u0 = lo0[j], u1 = lo1[j]: 2 x 16 table lookups.
+// At step st a lane reads byte position q = st ^ rot (rot = lane mod 16), so
+// eight consecutive lanes read eight distinct bank groups (entry (v, q) is
+// 16-byte slot 16 v + q: bank group q mod 8) and the random lookups are
+// conflict-free. The bytes are permuted once to that order (cb_permute), so
+// each step is a byte move, one logic op for the slot offset, the load and the
+// XORs, with no position-dependent word select or shift.
 __device__ __forceinline__ gf128 cb_value(const gf128* tab, const gf128 u0, const gf128 u1, int rot) {
-  const uint4 x0 = make_uint4(u0.w[0], u0.w[1], u0.w[2], u0.w[3]), x1 = make_uint4(u1.w[0], u1.w[1], u1.w[2], u1.w[3]);
-  gf128 acc = gf_zero();
+  uint32_t p0[4], p1[4];
+  cb_permute(u0, rot, p0);
+  cb_permute(u1, rot, p1);
+  const char* base = reinterpret_cast<const char*>(tab);
+  const uint32_t xk = (uint32_t)rot << 4;  // byte offset of the position XOR
+  uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
 #pragma unroll
-  for (int t = 0; t < 16; t++) {
-    const int q = (rot + t) & 15;
-    const uint32_t w0 = (q & 8) ? ((q & 4) ? x0.w : x0.z) : ((q & 4) ? x0.y : x0.x);
-    const uint32_t w1 = (q & 8) ? ((q & 4) ? x1.w : x1.z) : ((q & 4) ? x1.y : x1.x);
-    const uint32_t b0 = (w0 >> (8 * (q & 3))) & 255, b1 = (w1 >> (8 * (q & 3))) & 255;
-    acc = gf_add(acc, tab[(b0 << 4) + q]);
-    acc = gf_add(acc, tab[4096 + (b1 << 4) + q]);
+  for (int st = 0; st < 16; st++) {
+    // byte st of p at bits 8..15 = v << 8: slot (v << 4) | (st ^ rot) is byte
+    // offset (v << 8) | ((st ^ rot) << 4); claim 1's table is 4096 slots on
+    const uint32_t sh = 0x4404u | ((uint32_t)(st & 3) << 4);
+    const uint32_t o0 = (__byte_perm(p0[st >> 2], 0, sh) | ((uint32_t)st << 4)) ^ xk;
+    const uint32_t o1 = (__byte_perm(p1[st >> 2], 0, sh) | ((uint32_t)st << 4)) ^ xk;
+    const uint4 t0 = *reinterpret_cast<const uint4*>(base + o0);
+    const uint4 t1 = *reinterpret_cast<const uint4*>(base + 4096 * 16 + o1);
+    a0 ^= t0.x ^ t1.x;
+    a1 ^= t0.y ^ t1.y;
+    a2 ^= t0.z ^ t1.z;
+    a3 ^= t0.w ^ t1.w;
   }
-  return acc;
+  gf128 r;
+  r.w[0] = a0; r.w[1] = a1; r.w[2] = a2; r.w[3] = a3;
+  return r;
 }
 
 __global__ void __launch_bounds__(CB_THREADS)
