@@ -77,7 +77,9 @@ def load_peaks():
 
 
 class ClockSampler:
-    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+    """Samples nvidia-smi clocks and throttle reasons during the timed region:
+    one nvidia-smi process in its own sampling loop (-lms 200), read line by
+    line, rather than a process started per sample."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -86,28 +88,36 @@ class ClockSampler:
     def __init__(self, index=0):
         self.index = index
         self.samples = []
-        self._stop = threading.Event()
+        self._p = None
         self._t = None
 
-    def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
-                                     timeout=5).stdout.strip()
-                if out:
-                    self.samples.append([x.strip() for x in out.split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+    def _read(self):
+        for line in self._p.stdout:
+            out = line.strip()
+            if out:
+                self.samples.append([x.strip() for x in out.split(",")])
 
     def __enter__(self):
-        self._t = threading.Thread(target=self._run, daemon=True)
+        try:
+            self._p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                        "--format=csv,noheader,nounits", "-lms", "200"],
+                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self._p = None
+            return self
+        self._t = threading.Thread(target=self._read, daemon=True)
         self._t.start()
         return self
 
     def __exit__(self, *a):
-        self._stop.set()
+        if self._p is None:
+            return
+        self._p.terminate()
+        try:
+            self._p.wait(timeout=10)
+        except subprocess.TimeoutExpired:
+            self._p.kill()
+            self._p.wait()
         self._t.join(timeout=10)
 
     def summary(self):
