@@ -205,6 +205,25 @@ __device__ __forceinline__ gf128 gf_mul_p64(gf128 a, uint4 m0, uint4 m1, uint4 m
   const uint64_t l0 = ll ^ (lm << 32), l1 = lh ^ (lm >> 32), h0 = hl ^ (hm << 32), h1 = hh ^ (hm >> 32);
   return gf_reduce(l0, l1 ^ h0, h1, 0);
 }
+// a * t for t below 2^72 given the prepared low 64 bits of t (m0, m1, m2, as
+// gf_mul_p64) and its bits 64..71 (thi): the 64-bit product's 192 bits plus
+// a * thi placed at bit 64, one shifted copy of a per set bit of thi (thi is
+// the same in every lane of a layer's block, so the loop does not diverge).
+__device__ __forceinline__ gf128 gf_mul_p72(gf128 a, uint4 m0, uint4 m1, uint4 m2, uint32_t thi) {
+  const uint64_t ll = clmul32_p(a.w[0], m0), lh = clmul32_p(a.w[1], m1);
+  const uint64_t lm = clmul32_p(a.w[0] ^ a.w[1], m2) ^ ll ^ lh;
+  const uint64_t hl = clmul32_p(a.w[2], m0), hh = clmul32_p(a.w[3], m1);
+  const uint64_t hm = clmul32_p(a.w[2] ^ a.w[3], m2) ^ hl ^ hh;
+  uint64_t r1 = lh ^ (lm >> 32) ^ hl ^ (hm << 32), r2 = hh ^ (hm >> 32), r3 = 0;
+  const uint64_t alo = a.w[0] | ((uint64_t)a.w[1] << 32), ahi = a.w[2] | ((uint64_t)a.w[3] << 32);
+  for (uint32_t t = thi; t; t &= t - 1) {
+    const int j = __ffs(t) - 1;
+    r1 ^= alo << j;
+    r2 ^= (ahi << j) | (j ? alo >> (64 - j) : 0);
+    r3 ^= j ? ahi >> (64 - j) : 0;
+  }
+  return gf_reduce(ll ^ (lm << 32), r1, r2, r3);
+}
 __device__ __forceinline__ gf128p gf_load_p(const gf128p* q) {
   gf128p p;
 #pragma unroll

@@ -144,13 +144,18 @@ ntt_pass_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t s
       // diverges.
       // The deepest layers' twiddles are narrow (layer d-1 below 2^d, layer
       // d-2 below 2^(2d-3)): from layer narrow & 255 on they fit 32 bits,
-      // from layer narrow >> 8 on 64 bits (the host reads both bounds off the
-      // table), and their products take four or six 32-bit products instead
-      // of nine. The class is uniform over a layer.
+      // from layer (narrow >> 8) & 255 on 64 bits, from layer narrow >> 16 on
+      // 72 bits (the host reads the bounds off the table), and their
+      // products take four or six 32-bit products instead of nine (72 bits:
+      // six, plus one shifted copy per set bit above bit 63). The class is
+      // uniform over a layer.
       const gf128p* twl = reinterpret_cast<const gf128p*>(tw_any) + twb;
       const bool hi0 = hi == 0;
       const int layer = l0 + t;
-      const int wcls = layer >= (narrow & 255) ? 1 : layer >= (narrow >> 8) ? 2 : 0;
+      const int wcls = layer >= (narrow & 255)          ? 1
+                       : layer >= ((narrow >> 8) & 255) ? 2
+                       : layer >= (narrow >> 16)        ? 3
+                                                        : 0;
       if (wcls == 1) {
 #pragma unroll
         for (int j = 0; j < H; j++) {
@@ -163,6 +168,16 @@ ntt_pass_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t s
           if (!(hi0 && ti[j] == 0)) {
             const gf128p* q = &twl[ti[j]];
             y[j] = gf_add(y[j], gf_mul_p64(y[j + H], q->m[0], q->m[1], q->m[2]));
+          }
+          y[j + H] = gf_add(y[j + H], y[j]);
+        }
+      } else if (wcls == 3) {
+#pragma unroll
+        for (int j = 0; j < H; j++) {
+          if (!(hi0 && ti[j] == 0)) {
+            const gf128p* q = &twl[ti[j]];
+            const uint4 m3 = q->m[3];  // word 2 of the twiddle in its four masked parts
+            y[j] = gf_add(y[j], gf_mul_p72(y[j + H], q->m[0], q->m[1], q->m[2], m3.x | m3.y | m3.z | m3.w));
           }
           y[j + H] = gf_add(y[j + H], y[j]);
         }
@@ -238,10 +253,11 @@ std::vector<hf::F> host_twiddles(int d) {
 std::mutex g_tw_mu;
 std::map<std::pair<int, int>, void*> g_tw;  // (device, log_d) -> device table
 
-// (w64 << 8) | w32: the first layers from which every twiddle of a transform
-// of 2^log_d positions is below 2^32 and below 2^64, read off the table
-// (the normalized subspace polynomials of the deepest layers have low degree:
-// layer d-1 below 2^d, layer d-2 below 2^(2d-3)). Cached per log_d.
+// (w72 << 16) | (w64 << 8) | w32: the first layers from which every twiddle
+// of a transform of 2^log_d positions is below 2^32, 2^64 and 2^72, read off
+// the table (the normalized subspace polynomials of the deepest layers have
+// low degree: layer d-1 below 2^d, layer d-2 below 2^(2d-3), layer d-3 below
+// 2^69 at d = 20). Cached per log_d.
 int flock_ntt_narrow_layers(int log_d) {
   static std::mutex mu;
   static std::map<int, int> cache;
@@ -251,7 +267,7 @@ int flock_ntt_narrow_layers(int log_d) {
   // a bit is set in some subset sum of a layer's generators iff it is set in
   // one of the generators, so the OR of the generators bounds the layer
   const std::vector<std::vector<hf::F>> ev = twiddle_rows(log_d);
-  int w32 = log_d, w64 = log_d;
+  int w32 = log_d, w64 = log_d, w72 = log_d;
   for (int layer = log_d - 1; layer >= 0; layer--) {
     uint64_t or_lo = 0, or_hi = 0;
     const auto& row = ev[log_d - layer - 1];
@@ -259,17 +275,18 @@ int flock_ntt_narrow_layers(int log_d) {
       or_lo |= row[bit + 1].lo;
       or_hi |= row[bit + 1].hi;
     }
-    if (or_hi != 0) break;
-    w64 = layer;
-    if ((or_lo >> 32) == 0 && w32 == layer + 1) w32 = layer;
+    if ((or_hi >> 8) != 0) break;
+    w72 = layer;
+    if (or_hi == 0 && w64 == layer + 1) w64 = layer;
+    if (or_hi == 0 && (or_lo >> 32) == 0 && w32 == layer + 1) w32 = layer;
   }
-  return cache[log_d] = (w64 << 8) | w32;
+  return cache[log_d] = (w72 << 16) | (w64 << 8) | w32;
 }
 
 template <int F, bool PREP, int V>
 int launch_pass(gf128* dst, const gf128* src, size_t mask, const void* tw, int log_d, int log_lanes, int l0,
                 cudaStream_t st) {
-  const int narrow = PREP ? flock_ntt_narrow_layers(log_d) : (log_d << 8) | log_d;
+  const int narrow = PREP ? flock_ntt_narrow_layers(log_d) : (log_d << 16) | (log_d << 8) | log_d;
   if constexpr (F > variant_max_layers(V)) {
     return FLOCK_ERR_SHAPE;
   } else {
