@@ -205,6 +205,24 @@ __device__ __forceinline__ gf128 gf_mul_p64(gf128 a, uint4 m0, uint4 m1, uint4 m
   const uint64_t l0 = ll ^ (lm << 32), l1 = lh ^ (lm >> 32), h0 = hl ^ (hm << 32), h1 = hh ^ (hm >> 32);
   return gf_reduce(l0, l1 ^ h0, h1, 0);
 }
+// a * t for t below 2^40 given the prepared low 32 bits of t (m0, as
+// gf_mul_p32) and its bits 32..39 (thi): the four 32-bit products plus one
+// copy of a shifted by 32 + j per set bit j of thi (the same in every lane of
+// a layer's block, so the loop does not diverge).
+__device__ __forceinline__ gf128 gf_mul_p40(gf128 a, uint4 m0, uint32_t thi) {
+  const uint64_t p0 = clmul32_p(a.w[0], m0), p1 = clmul32_p(a.w[1], m0);
+  const uint64_t p2 = clmul32_p(a.w[2], m0), p3 = clmul32_p(a.w[3], m0);
+  uint64_t r0 = p0 ^ (p1 << 32), r1 = (p1 >> 32) ^ p2 ^ (p3 << 32), r2 = p3 >> 32;
+  const uint64_t alo = a.w[0] | ((uint64_t)a.w[1] << 32), ahi = a.w[2] | ((uint64_t)a.w[3] << 32);
+  for (uint32_t t = thi; t; t &= t - 1) {
+    const int s = 32 + __ffs(t) - 1;  // 32 <= s < 40
+    r0 ^= alo << s;
+    r1 ^= (ahi << s) | (alo >> (64 - s));
+    r2 ^= ahi >> (64 - s);
+  }
+  return gf_reduce(r0, r1, r2, 0);
+}
+
 // a * t for t below 2^72 given the prepared low 64 bits of t (m0, m1, m2, as
 // gf_mul_p64) and its bits 64..71 (thi): the 64-bit product's 192 bits plus
 // a * thi placed at bit 64, one shifted copy of a per set bit of thi (thi is

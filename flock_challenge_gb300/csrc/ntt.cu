@@ -143,19 +143,20 @@ ntt_pass_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t s
       // need no product. Blocks are uniform over a tile, so the test rarely
       // diverges.
       // The deepest layers' twiddles are narrow (layer d-1 below 2^d, layer
-      // d-2 below 2^(2d-3)): from layer narrow & 255 on they fit 32 bits,
-      // from layer (narrow >> 8) & 255 on 64 bits, from layer narrow >> 16 on
-      // 72 bits (the host reads the bounds off the table), and their
-      // products take four or six 32-bit products instead of nine (72 bits:
-      // six, plus one shifted copy per set bit above bit 63). The class is
-      // uniform over a layer.
+      // d-2 below 2^(2d-3)): byte 0 of `narrow` is the first layer whose
+      // twiddles fit 32 bits, bytes 1, 2, 3 those for 40, 64 and 72 bits (the
+      // host reads the bounds off the table). Their products take four (32
+      // bits) or six (64 bits) 32-bit products instead of nine; 40 and 72 bits
+      // take those of their low 32 or 64 bits plus one shifted copy of the
+      // operand per higher set bit. The class is uniform over a layer.
       const gf128p* twl = reinterpret_cast<const gf128p*>(tw_any) + twb;
       const bool hi0 = hi == 0;
       const int layer = l0 + t;
-      const int wcls = layer >= (narrow & 255)          ? 1
-                       : layer >= ((narrow >> 8) & 255) ? 2
-                       : layer >= (narrow >> 16)        ? 3
-                                                        : 0;
+      const int wcls = layer >= (narrow & 255)           ? 1
+                       : layer >= ((narrow >> 8) & 255)  ? 4
+                       : layer >= ((narrow >> 16) & 255) ? 2
+                       : layer >= ((narrow >> 24) & 255) ? 3
+                                                         : 0;
       if (wcls == 1) {
 #pragma unroll
         for (int j = 0; j < H; j++) {
@@ -168,6 +169,16 @@ ntt_pass_kernel(gf128* __restrict__ dst, const gf128* __restrict__ src, size_t s
           if (!(hi0 && ti[j] == 0)) {
             const gf128p* q = &twl[ti[j]];
             y[j] = gf_add(y[j], gf_mul_p64(y[j + H], q->m[0], q->m[1], q->m[2]));
+          }
+          y[j + H] = gf_add(y[j + H], y[j]);
+        }
+      } else if (wcls == 4) {
+#pragma unroll
+        for (int j = 0; j < H; j++) {
+          if (!(hi0 && ti[j] == 0)) {
+            const gf128p* q = &twl[ti[j]];
+            const uint4 m1 = q->m[1];  // word 1 of the twiddle in its four masked parts
+            y[j] = gf_add(y[j], gf_mul_p40(y[j + H], q->m[0], m1.x | m1.y | m1.z | m1.w));
           }
           y[j + H] = gf_add(y[j + H], y[j]);
         }
@@ -253,9 +264,9 @@ std::vector<hf::F> host_twiddles(int d) {
 std::mutex g_tw_mu;
 std::map<std::pair<int, int>, void*> g_tw;  // (device, log_d) -> device table
 
-// (w72 << 16) | (w64 << 8) | w32: the first layers from which every twiddle
-// of a transform of 2^log_d positions is below 2^32, 2^64 and 2^72, read off
-// the table (the normalized subspace polynomials of the deepest layers have
+// w32 | (w40 << 8) | (w64 << 16) | (w72 << 24): the first layers from which
+// every twiddle of a transform of 2^log_d positions is below 2^32, 2^40,
+// 2^64 and 2^72, read off the table (the normalized subspace polynomials of the deepest layers have
 // low degree: layer d-1 below 2^d, layer d-2 below 2^(2d-3), layer d-3 below
 // 2^69 at d = 20). Cached per log_d.
 int flock_ntt_narrow_layers(int log_d) {
@@ -267,7 +278,7 @@ int flock_ntt_narrow_layers(int log_d) {
   // a bit is set in some subset sum of a layer's generators iff it is set in
   // one of the generators, so the OR of the generators bounds the layer
   const std::vector<std::vector<hf::F>> ev = twiddle_rows(log_d);
-  int w32 = log_d, w64 = log_d, w72 = log_d;
+  int w32 = log_d, w40 = log_d, w64 = log_d, w72 = log_d;
   for (int layer = log_d - 1; layer >= 0; layer--) {
     uint64_t or_lo = 0, or_hi = 0;
     const auto& row = ev[log_d - layer - 1];
@@ -278,15 +289,16 @@ int flock_ntt_narrow_layers(int log_d) {
     if ((or_hi >> 8) != 0) break;
     w72 = layer;
     if (or_hi == 0 && w64 == layer + 1) w64 = layer;
+    if (or_hi == 0 && (or_lo >> 40) == 0 && w40 == layer + 1) w40 = layer;
     if (or_hi == 0 && (or_lo >> 32) == 0 && w32 == layer + 1) w32 = layer;
   }
-  return cache[log_d] = (w72 << 16) | (w64 << 8) | w32;
+  return cache[log_d] = w32 | (w40 << 8) | (w64 << 16) | (w72 << 24);
 }
 
 template <int F, bool PREP, int V>
 int launch_pass(gf128* dst, const gf128* src, size_t mask, const void* tw, int log_d, int log_lanes, int l0,
                 cudaStream_t st) {
-  const int narrow = PREP ? flock_ntt_narrow_layers(log_d) : (log_d << 16) | (log_d << 8) | log_d;
+  const int narrow = PREP ? flock_ntt_narrow_layers(log_d) : log_d * 0x01010101;
   if constexpr (F > variant_max_layers(V)) {
     return FLOCK_ERR_SHAPE;
   } else {

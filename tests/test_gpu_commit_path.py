@@ -45,11 +45,12 @@ def test_witness_z_only(cuda_device):
 # first layer holds >= 2^9 quad-lanes): (7, 6, 1), (12, 6, 1), (13, 4, 3),
 # (10, 6, 0), (9, 7, 2), (16, 6, 1), (14, 3, 2); (8, 3, 0) and (11, 4, 4) sit
 # exactly at the cutoff (one table pass, then multiply passes). (12, 3, 1)
-# puts layer 8, whose twiddles are below 2^65, in a multiply pass at every
-# table depth the tuner may pick: the product of a twiddle of 64 + k bits.
+# puts layer 8, whose twiddles are below 2^65, and (18, 3, 0) layer 16,
+# below 2^33, in a multiply pass at every table depth the tuner may pick: the
+# products of twiddles of 64 + k and 32 + k bits.
 @pytest.mark.parametrize("log_d,log_lanes,start", [(1, 4, 0), (5, 4, 0), (7, 6, 1), (12, 6, 1), (13, 4, 3),
                                                    (10, 6, 0), (9, 7, 2), (16, 6, 1), (14, 3, 2), (8, 3, 0),
-                                                   (11, 4, 4), (12, 3, 1)])
+                                                   (11, 4, 4), (12, 3, 1), (18, 3, 0)])
 def test_ntt_matches_oracle(ctx, log_d, log_lanes, start):
     rng = np.random.default_rng(log_d * 7 + start)
     data = rng.integers(0, 2**63, (1 << (log_d + log_lanes)) * 2, dtype=np.uint64)
