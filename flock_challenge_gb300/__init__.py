@@ -148,6 +148,7 @@ def _proto_lib():
         L.flock_last_host_waits.argtypes = [P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_double),
                                             ctypes.c_int]
         L.flock_kernel_timing.argtypes = [P, ctypes.c_int]
+        L.flock_set_wait_limit.argtypes = [P, ctypes.c_double]
         L.flock_last_kernel_times.argtypes = [P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
         L.flock_prove_seed.argtypes = [P, ctypes.c_uint32, ctypes.c_uint64, P, ctypes.c_size_t,
                                        ctypes.POINTER(ctypes.c_size_t)]
@@ -368,6 +369,12 @@ class Blake3Setup:
     def stream_handle(self):
         """cudaStream_t the prover launches on (for event timing)."""
         return _proto_lib().flock_stream(self.ctx.handle)
+
+    def set_wait_limit(self, ms):
+        """Bounds each host wait of this prover's later calls by `ms` milliseconds
+        (0: no bound); a call whose wait passes it raises FlockError (timeout)
+        and the next call first waits for its queued work (flock_set_wait_limit)."""
+        check(_proto_lib().flock_set_wait_limit(self.ctx.handle, float(ms)), "flock_set_wait_limit")
 
     def set_kernel_timing(self, on=True):
         """CUDA-event timing of the main kernels of each proof (flock_kernel_timing)."""

@@ -354,6 +354,15 @@ int flock_kernel_timing(flock_ctx* ctx, int enable) {
   return flock_prover_set_timing(ctx->prover, enable != 0);
 }
 
+int flock_set_wait_limit(flock_ctx* ctx, double limit_ms) {
+  if (!ctx) return FLOCK_ERR_ARG;
+  if (!ctx->prover) {
+    ctx->prover = flock_prover_create(ctx->device);
+    if (!ctx->prover) return FLOCK_ERR_CUDA;
+  }
+  return flock_prover_set_wait_limit(ctx->prover, limit_ms);
+}
+
 int flock_last_kernel_times(const flock_ctx* ctx, double* ms, int n) {
   if (!ctx || !ctx->prover || !ms) return FLOCK_ERR_ARG;
   return flock_prover_kernel_times(ctx->prover, ms, n);

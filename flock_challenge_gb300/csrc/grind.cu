@@ -126,7 +126,8 @@ int flock_grind(const uint8_t digest[32], uint32_t bits, void* d_scratch, int* p
     flock_count_launch();
     if (cudaGetLastError() != cudaSuccess) return FLOCK_ERR_CUDA;
     if (cudaMemcpyAsync(h_best, d_best, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess) return FLOCK_ERR_CUDA;
-    if (flock_stream_wait(st, waits) != cudaSuccess) return FLOCK_ERR_CUDA;
+    const cudaError_t we = flock_stream_wait(st, waits);
+    if (we != cudaSuccess) return we == cudaErrorTimeout ? FLOCK_ERR_TIMEOUT : FLOCK_ERR_CUDA;
     if (*h_best != none) {
       *nonce = *h_best;
       return FLOCK_OK;

@@ -62,10 +62,13 @@ struct Fail : std::runtime_error {
   int code;
   Fail(int c, const std::string& w) : std::runtime_error(w), code(c) {}
 };
-#define CK(x)                                                              \
-  do {                                                                     \
-    cudaError_t e_ = (x);                                                  \
-    if (e_ != cudaSuccess) throw Fail(FLOCK_ERR_CUDA, cudaGetErrorString(e_)); \
+// A CUDA status as a failure: a bounded wait that gave up (cudaErrorTimeout,
+// from flock_stream_wait under a wait limit) is FLOCK_ERR_TIMEOUT.
+#define CK(x)                                                                                            \
+  do {                                                                                                   \
+    cudaError_t e_ = (x);                                                                                \
+    if (e_ != cudaSuccess)                                                                               \
+      throw Fail(e_ == cudaErrorTimeout ? FLOCK_ERR_TIMEOUT : FLOCK_ERR_CUDA, cudaGetErrorString(e_)); \
   } while (0)
 #define FK(x)                                      \
   do {                                             \
@@ -567,6 +570,12 @@ void flock_prover_trim(ProverState* S) {
 
 const FlockPhaseTimes& flock_prover_times(const ProverState* S) { return S->times; }
 
+int flock_prover_set_wait_limit(ProverState* S, double limit_ms) {
+  if (!(limit_ms >= 0)) return FLOCK_ERR_ARG;  // NaN included
+  S->waits.limit_ms = limit_ms;
+  return FLOCK_OK;
+}
+
 int flock_prover_set_timing(ProverState* S, bool on) {
   if (on) {
     if (cudaSetDevice(S->device) != cudaSuccess) return FLOCK_ERR_CUDA;
@@ -610,7 +619,9 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
                        bool input_on_device, const ChainReq* chain, fs::Transcript* ext_tr, flock_r1cs_claim* claim) {
   try {
     CK(cudaSetDevice(S->device));
-    CK(cudaStreamSynchronize(S->st));  // the staging area of the previous proof is free again
+    // the staging area of the previous call is free again (under a wait
+    // limit, this also drains the work of a call that gave up waiting)
+    CK(flock_stream_wait(S->st, &S->waits, false));
     S->pin_off = 0;
     S->pin_open_off = 0;
     const int m = 14 + n_log;
@@ -622,7 +633,8 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
     cudaStream_t st = S->st;
     FlockPhaseTimes& T = S->times;
     T = FlockPhaseTimes();
-    S->waits = WaitStats();
+    S->waits.waits = 0;  // counted per proof; the wait limit stays
+    S->waits.blocked_ms = 0;
     uint64_t waits_seen = 0;
     double blocked_seen = 0;
     auto snap_waits = [&](int phase) {
@@ -648,7 +660,7 @@ int flock_prover_prove(ProverState* S, const flock_compression* h_in, size_t n, 
       h2d(*S, S->csc_ai.get(c.a_idx.size() * 4), c.a_idx.data(), c.a_idx.size() * 4);
       h2d(*S, S->csc_bp.get(c.b_ptr.size() * 4), c.b_ptr.data(), c.b_ptr.size() * 4);
       h2d(*S, S->csc_bi.get(c.b_idx.size() * 4), c.b_idx.data(), c.b_idx.size() * 4);
-      CK(cudaStreamSynchronize(st));
+      CK(flock_stream_wait(st, &S->waits, false));
       S->csc_ready = true;
     }
     const Lagrange& LG = lagrange();
@@ -1681,7 +1693,7 @@ static int verify_impl(ProverState* S, const uint8_t* data, size_t len, const ch
   };
   try {
     CK(cudaSetDevice(S->device));
-    CK(cudaStreamSynchronize(S->st));
+    CK(flock_stream_wait(S->st, &S->waits, false));
     S->pin_off = 0;
     cudaStream_t st = S->st;
     Reader rd{data, len};
@@ -1814,7 +1826,7 @@ static int verify_impl(ProverState* S, const uint8_t* data, size_t len, const ch
         h2d(*S, S->csc_ai.get(c.a_idx.size() * 4), c.a_idx.data(), c.a_idx.size() * 4);
         h2d(*S, S->csc_bp.get(c.b_ptr.size() * 4), c.b_ptr.data(), c.b_ptr.size() * 4);
         h2d(*S, S->csc_bi.get(c.b_idx.size() * 4), c.b_idx.data(), c.b_idx.size() * 4);
-        CK(cudaStreamSynchronize(st));
+        CK(flock_stream_wait(st, &S->waits, false));
         S->csc_ready = true;
       }
       auto lag_z = LG.at(z, 0);

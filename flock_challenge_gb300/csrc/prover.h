@@ -52,6 +52,9 @@ const FlockPhaseTimes& flock_prover_times(const ProverState* s);
 // zerocheck round 1.
 int flock_prover_set_timing(ProverState* s, bool on);
 int flock_prover_kernel_times(const ProverState* s, double* ms, int n);
+// Bounds every host wait of the state's later calls by limit_ms (0: no
+// bound): a wait that passes it makes the call return FLOCK_ERR_TIMEOUT.
+int flock_prover_set_wait_limit(ProverState* s, double limit_ms);
 // Device bytes the state holds (its buffers grow to the largest proof seen).
 size_t flock_prover_reserved_bytes(const ProverState* s);
 // Frees the state's device buffers (after its stream is idle); the next proof

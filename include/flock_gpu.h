@@ -27,7 +27,8 @@ enum {
   FLOCK_ERR_OOM = -3,     /* device allocation failed / over budget */
   FLOCK_ERR_ARG = -4,     /* null or inconsistent argument */
   FLOCK_ERR_CAPACITY = -5,/* output buffer too small */
-  FLOCK_ERR_TIMEOUT = -6, /* a bounded search gave up: the grind's nonce range ran out */
+  FLOCK_ERR_TIMEOUT = -6, /* a bounded wait or search gave up: a host wait passed the context's
+                           wait limit (flock_set_wait_limit), or the grind's nonce range ran out */
   FLOCK_ERR_VERIFY = -7,  /* an internal consistency check failed */
   FLOCK_ERR_LIMIT = -8    /* size above the fixed limit of an entry point that allocates nothing */
 };
@@ -202,6 +203,21 @@ int flock_last_host_waits(const flock_ctx* ctx, uint64_t* waits, double* blocked
  * No reference counterpart (measurement only). */
 int flock_kernel_timing(flock_ctx* ctx, int enable);
 int flock_last_kernel_times(const flock_ctx* ctx, double* ms, int n);
+
+/* Bounded waits. With limit_ms > 0, every host wait of this context's later
+ * prove, prove_seed, prove_device, prove_challenger, chain and verify calls
+ * (a round's partial sums, a grind result, a Merkle root, the start-of-call
+ * drain of the previous call's work) polls the context's stream and gives
+ * up after limit_ms: the call then returns FLOCK_ERR_TIMEOUT and writes no
+ * output. The work the call had already queued keeps running on the GPU;
+ * the context's next call waits for it first (under the same limit), so
+ * the context stays usable. The limit bounds each wait, not a whole call.
+ * 0 (the default): unbounded stream synchronisation. FLOCK_ERR_ARG for a
+ * negative or NaN limit. The reference has no counterpart: its GPU waits
+ * spin for a bounded budget and then block in waitUntilCompleted without a
+ * deadline (crates/flock-core/src/gpu_commit.rs:1250-1257), and on a GPU
+ * error it falls back to the CPU (:1462-1465). */
+int flock_set_wait_limit(flock_ctx* ctx, double limit_ms);
 
 /* ---- Verification -------------------------------------------------------- */
 

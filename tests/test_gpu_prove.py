@@ -112,3 +112,25 @@ def test_phase_times_and_host_waits_describe_the_last_proof(cuda_device):
         assert n >= 1 and 0.0 <= blocked <= phases[k] + 1e-3, (k, n, blocked, phases[k])
     # the openings' copies ride on the stream: the proof is still the oracle's
     assert proof == O.prove(O.compressions(10, 3), 10)
+
+
+def test_wait_limit_gives_up_and_the_context_recovers(cuda_device):
+    """A host wait that passes the context's wait limit ends the call with
+    FLOCK_ERR_TIMEOUT; the GPU work the call queued finishes on its own (no
+    fault, no hang), and the context's next call drains it and proves the
+    same bytes."""
+    blocks = O.compressions(12, 5)
+    setup = F.Blake3Setup(1 << 12)
+    ref = setup.prove_fast(blocks)
+    assert ref == O.prove(blocks, 12)
+    setup.set_wait_limit(1e-4)  # 0.1 us: the commit's first wait cannot be met
+    with pytest.raises(F.FlockError, match="timeout"):
+        setup.prove_fast(blocks)
+    setup.set_wait_limit(0)
+    assert setup.prove_fast(blocks) == ref
+    setup.set_wait_limit(60_000)  # a limit no wait reaches changes nothing
+    assert setup.prove_fast(blocks) == ref
+    n, _ = setup.host_waits()["ligerito"]
+    assert n >= 1
+    with pytest.raises(F.FlockError, match="argument"):
+        setup.set_wait_limit(-1.0)
