@@ -161,10 +161,13 @@ def dist_env():
 
 def workload_config(log2, ws):
     """The workload description both arms print (the same dict on each)."""
+    # the prover's device working set scales with the compressions: ~7.5 GiB at 2^18
+    ws_gb = 7.5 * 1.073741824 * 2.0 ** (log2 - 18)
+    l2 = f"working set ~{ws_gb:.3g} GB, {'larger' if ws_gb > 0.129 else 'smaller'} than the 129 MB L2"
     return {"workload": f"one proof of 2^{log2} BLAKE3 compressions per step (m={14 + log2}, rate 1/2, "
                         "64 lanes, Fast profile, BLAKE3 Merkle + transcript, inputs from the reference "
                         "generator)",
-            "parallelism": f"replicas x{ws}", "l2": "working set > 5 GB, larger than L2"}
+            "parallelism": f"replicas x{ws}", "l2": l2}
 
 
 def oracle_baseline(log2=18, proofs=2, gpu_proof=None, gpu_m=None):
