@@ -269,6 +269,7 @@ std::map<std::pair<int, int>, void*> g_tw;  // (device, log_d) -> device table
 // 2^64 and 2^72, read off the table (the normalized subspace polynomials of the deepest layers have
 // low degree: layer d-1 below 2^d, layer d-2 below 2^(2d-3), layer d-3 below
 // 2^69 at d = 20). Cached per log_d.
+constexpr int kMaxTwiddleClassLogD = 40;
 int flock_ntt_narrow_layers(int log_d) {
   static std::mutex mu;
   static std::map<int, int> cache;
@@ -698,6 +699,11 @@ extern "C" int flock_ntt_tuned_table_end(int device, int log_d, int log_lanes, i
   std::lock_guard<std::mutex> lk(g_tune_mu);
   auto it = g_tuned.find(TuneKey{device, log_d, log_lanes, start_layer});
   return it == g_tuned.end() ? -1 : it->second.tab_end;
+}
+
+extern "C" int flock_ntt_twiddle_classes(int log_d) {
+  if (log_d < 1 || log_d > kMaxTwiddleClassLogD) return FLOCK_ERR_ARG;
+  return flock_ntt_narrow_layers(log_d);
 }
 
 // Applies layers [start_layer, log_d) in passes whose shape the autotuner

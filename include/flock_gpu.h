@@ -101,6 +101,15 @@ int flock_ntt(flock_ctx* ctx, void* d_data, int log_d, int log_num_ntts, int sta
 int flock_ntt_tuned_variant(int device, int log_d, int log_lanes, int start_layer);
 int flock_ntt_tuned_table_end(int device, int log_d, int log_lanes, int start_layer);
 
+/* The narrow twiddle classes of a transform of 2^log_d positions: bytes 0..3
+ * are the first layers from which every twiddle is below 2^32, 2^40, 2^64
+ * and 2^72 (log_d where no layer qualifies). The multiply passes take 4
+ * (below 2^32), 4 plus a shifted copy per higher bit (below 2^40), 6 (below
+ * 2^64), 6 plus shifted copies (below 2^72) or 9 (otherwise) 32x32
+ * carry-less pieces per product. Host arithmetic only (no device call);
+ * FLOCK_ERR_ARG outside 1 <= log_d <= 40. No reference counterpart. */
+int flock_ntt_twiddle_classes(int log_d);
+
 /* The Merkle autotuner's choice for a tree shape (n_leaves leaves of
  * leaf_bytes) on `device`, or -1 if that shape has not run yet (or has fewer
  * than 2^12 leaves, which are never tuned): how many parent levels (0..2) the
