@@ -59,14 +59,19 @@ PUBLISHED = 483866.0  # README.md:110-116, unmodified reference, Apple M4 Pro ru
 # L0 commit NTT: DRAM bytes (read + write) per pass at 2^18 positions x 64
 # lanes, mean of the eight L0 passes; times 4 for the bench's 2^20 positions.
 NTT_TRAFFIC_PER_PASS = {20: 4 * 478.8e6}
-NTT_MAX_LAYERS = {0: 4, 1: 6, 2: 8}  # layers per pass of the autotuner's pass shapes
+# layers per pass of the autotuner's pass shapes (3: the deep-table pass of
+# the last three layers)
+NTT_MAX_LAYERS = {0: 4, 1: 6, 2: 8, 3: 3}
+NTT_DEEP_SHAPE = 3
 # Thread instructions per GF(2^128) product in the table passes (mean of the
-# passes over layers 1..8; deeper passes spend more on their table builds) and
-# per butterfly in the multiply pass (its layers are the three deepest, whose
-# narrow twiddles take 4 or 6 32-bit carry-less pieces), 2^18-position L0
-# transform.
+# passes over layers 1..8; deeper passes spend more on their table builds), per
+# butterfly in the multiply pass (its layers are the three deepest, whose
+# narrow twiddles take 4 or 6 32-bit carry-less pieces) and per butterfly in
+# the deep-table pass that replaces it (tables of the narrow twiddles'
+# products for two of those layers), 2^18-position L0 transform.
 NTT_INSTR_PER_TABLE_PRODUCT = 160
 NTT_INSTR_PER_MULTIPLY_BUTTERFLY = 259
+NTT_INSTR_PER_DEEP_BUTTERFLY = 148
 # Zerocheck round 1 at m = 30 (2^17 outer blocks of 128 rows): warp
 # instructions and DRAM bytes (read + write) of one launch, per outer block.
 ZC1_WARP_INSTR_PER_OUTER = 603870960 / 2**17
@@ -330,12 +335,16 @@ def rooflines(F, log2, span_ms, peaks, sms, clock_mhz, dev_index):
 
     def products(l):  # butterflies of layer l with a product (block 0 skips it)
         return ((1 << (log_d - 1)) - (1 << (log_d - l - 1))) * 64
+    deep = variant == NTT_DEEP_SHAPE
     ins = (sum(products(l) for l in range(1, tab_end)) * NTT_INSTR_PER_TABLE_PRODUCT
-           + sum(products(l) for l in range(tab_end, log_d)) * NTT_INSTR_PER_MULTIPLY_BUTTERFLY)
+           + sum(products(l) for l in range(tab_end, log_d))
+           * (NTT_INSTR_PER_DEEP_BUTTERFLY if deep else NTT_INSTR_PER_MULTIPLY_BUTTERFLY))
+    last = ("the deep-table pass of the last 3 layers" if deep
+            else f"{passes - tab_passes} multiply pass(es) of <= {max_f} layers")
     muls = sum(products(l) for l in range(1, log_d))
     out["l0_ntt"] = {
         "kernel": f"L0 commit NTT, layers 1..{log_d - 1} of 2^{log_d} positions x 64 lanes ({tab_passes} two-layer "
-                  f"table passes, then {passes - tab_passes} multiply pass(es) of <= {max_f} layers)",
+                  f"table passes, then {last})",
         "bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
         "frac": alg / (ms * 1e-3) / 1e9 / hbm, "traffic": traffic,
         "algorithmic_bytes": alg, "traffic_over_algorithmic": (traffic / alg) if traffic else None,

@@ -522,6 +522,196 @@ int launch_tab2(gf128* dst, const gf128* src, size_t mask, const gf128* tw, int 
   return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
 }
 
+// ---- deep-table pass ------------------------------------------------------
+//
+// The twiddles of the last three layers are narrow (layer d-1 below 2^d,
+// d-2 below 2^(2d-3), d-3 below 2^69 at d = 20), so a twiddle's carry-less
+// products with all 256 byte values fit a small table of unreduced words,
+// T[v] = t v: one word for layer d-1, three for d-3. A product y t is then the
+// XOR of T[byte k of y] x^(8k) over the 16 bytes of y, reduced once: 16
+// lookups instead of four to six 32x32 carry-less pieces. A block owns one
+// group of 8 positions in all 64 lanes (a thread per lane): it builds the
+// 1 + 4 tables of the group's twiddles for layers d-3 and d-1 (8.25 KiB) and
+// applies the three layers to each lane's 8 positions in registers; layer d-2
+// keeps the carry-less product of its prepared twiddle (gf_mul_p40), which
+// spreads the pass over the ALU and the shared-memory pipes (tables for all
+// three layers measured 6.29 ms for the 2^20-position L0 set, this split
+// 6.07, the multiply passes 6.65: the random lookups conflict on ~60% of
+// shared wavefronts, so the load/store data path binds the all-table form).
+// Used for the last three layers of a 64-lane code whose twiddles there fit
+// 88, 56 and 24 bits, when the autotuner measures it faster than the
+// multiply passes.
+constexpr int kDeepVariant = 3;
+constexpr int D3_LANES = 64;
+constexpr int D3_C_STRIDE = 256 + 16;  // words per layer d-1 table: the skew keeps the build's stores conflict-free
+
+struct Deep3Tabs {
+  uint4 a[256];                // layer d-3: t v below 2^96 (three words used)
+  uint32_t c[4][D3_C_STRIDE];  // layer d-1, twiddles of the four pairs: below 2^32
+};
+
+// Bit width of every twiddle of layer `layer` of a 2^log_d transform (the OR of
+// the layer's generators bounds all its subset sums), cached per log_d.
+int twiddle_layer_width(int log_d, int layer) {
+  static std::mutex mu;
+  static std::map<int, std::vector<int>> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(log_d);
+  if (it == cache.end()) {
+    const std::vector<std::vector<hf::F>> ev = twiddle_rows(log_d);
+    std::vector<int> w(log_d, 0);
+    for (int l = 0; l < log_d; l++) {
+      uint64_t lo = 0, hi = 0;
+      const auto& row = ev[log_d - l - 1];
+      for (int bit = 0; bit < l; bit++) {
+        lo |= row[bit + 1].lo;
+        hi |= row[bit + 1].hi;
+      }
+      w[l] = hi ? 128 - __builtin_clzll(hi) : lo ? 64 - __builtin_clzll(lo) : 0;
+    }
+    it = cache.emplace(log_d, std::move(w)).first;
+  }
+  return it->second[layer];
+}
+
+// The deep-table pass applies to the layers [from, log_d) of a code of
+// 2^log_lanes lanes.
+bool deep3_applies(int log_d, int log_lanes, int from) {
+  return log_d >= 4 && log_d <= 30 && from == log_d - 3 && (1 << log_lanes) == D3_LANES &&
+         twiddle_layer_width(log_d, log_d - 1) <= 24 && twiddle_layer_width(log_d, log_d - 2) <= 56 &&
+         twiddle_layer_width(log_d, log_d - 3) <= 88;
+}
+
+__host__ __device__ constexpr int d3_ctz(int j) { return (j & 1) ? 0 : (j & 2) ? 1 : (j & 4) ? 2 : 3; }
+
+// Words 0..W-1 of a table entry.
+__device__ __forceinline__ void d3_words(uint32_t e, uint32_t (&w)[1]) { w[0] = e; }
+__device__ __forceinline__ void d3_words(uint4 e, uint32_t (&w)[3]) { w[0] = e.x; w[1] = e.y; w[2] = e.z; }
+
+// y t from the table T[v] = t v of W-word entries. Byte k of y adds T[byte]
+// at bit 8k: the lookups go into four accumulators by k mod 4 at word k / 4,
+// which are joined once with 8-, 16- and 24-bit funnel shifts (at most
+// 128 + 32 W bits), then reduced.
+template <int W, class E>
+__device__ __forceinline__ gf128 d3_mul(const E* __restrict__ T, const gf128& y) {
+  uint32_t acc[4][3 + W];
+#pragma unroll
+  for (int s = 0; s < 4; s++)
+#pragma unroll
+    for (int i = 0; i < 3 + W; i++) acc[s][i] = 0;
+#pragma unroll
+  for (int k = 0; k < 16; k++) {
+    const uint32_t v = __byte_perm(y.w[k >> 2], 0, 0x4440u | (uint32_t)(k & 3));
+    uint32_t e[W];
+    d3_words(T[v], e);
+#pragma unroll
+    for (int i = 0; i < W; i++) acc[k & 3][(k >> 2) + i] ^= e[i];
+  }
+  uint32_t r[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    uint32_t x = i < 3 + W ? acc[0][i] : 0u;
+#pragma unroll
+    for (int s = 1; s < 4; s++) {
+      const uint32_t hi = i < 3 + W ? acc[s][i] : 0u, lo = i >= 1 && i - 1 < 3 + W ? acc[s][i - 1] : 0u;
+      x ^= __funnelshift_l(lo, hi, 8 * s);
+    }
+    r[i] = x;
+  }
+  return gf_reduce(r[0] | ((uint64_t)r[1] << 32), r[2] | ((uint64_t)r[3] << 32), r[4] | ((uint64_t)r[5] << 32),
+                   r[6] | ((uint64_t)r[7] << 32));
+}
+
+// Layers log_d-3 .. log_d-1 in place for position group blockIdx.x
+// (positions 8 q .. 8 q + 7), thread = lane. tw: the plain twiddle table;
+// twq: the prepared one (layer d-2's products).
+__global__ void __launch_bounds__(D3_LANES, 8) ntt_deep3_kernel(gf128* __restrict__ data, const gf128* __restrict__ tw,
+                                                             const gf128p* __restrict__ twq, int log_d) {
+  __shared__ Deep3Tabs T;
+  const size_t q = blockIdx.x;
+  const int lane = threadIdx.x;
+  const size_t i17 = ((size_t)1 << (log_d - 3)) - 1 + q;
+  const size_t i18 = ((size_t)1 << (log_d - 2)) - 1 + 2 * q;
+  const size_t i19 = ((size_t)1 << (log_d - 1)) - 1 + 4 * q;
+  // Tables. Thread `lane` owns the entries whose low bits are its index and
+  // walks the high bits in Gray order, one XOR per entry; consecutive lanes
+  // store consecutive entries.
+  {
+    // layer d-1: table lane >> 4, entries (j << 4) | (lane & 15)
+    const int tb = lane >> 4, lo = lane & 15;
+    const uint32_t t = tw[i19 + tb].w[0];
+    uint32_t v = 0;
+#pragma unroll
+    for (int b = 0; b < 4; b++) v ^= (t << b) & (0u - (uint32_t)((lo >> b) & 1));
+#pragma unroll
+    for (int jj = 0; jj < 16; jj++) {
+      if (jj) v ^= t << (4 + d3_ctz(jj));
+      T.c[tb][((jj ^ (jj >> 1)) << 4) | lo] = v;
+    }
+  }
+  {
+    // layer d-3: entries (j << 6) | lane, three words
+    const gf128 t = tw[i17];
+    uint32_t v0 = 0, v1 = 0, v2 = 0;
+#pragma unroll
+    for (int b = 0; b < 6; b++) {
+      const uint32_t m = 0u - (uint32_t)((lane >> b) & 1);
+      v0 ^= (t.w[0] << b) & m;
+      v1 ^= __funnelshift_l(t.w[0], t.w[1], b) & m;
+      v2 ^= __funnelshift_l(t.w[1], t.w[2], b) & m;
+    }
+#pragma unroll
+    for (int jj = 0; jj < 4; jj++) {
+      if (jj) {
+        const int s = 6 + d3_ctz(jj);
+        v0 ^= t.w[0] << s;
+        v1 ^= __funnelshift_l(t.w[0], t.w[1], s);
+        v2 ^= __funnelshift_l(t.w[1], t.w[2], s);
+      }
+      T.a[((jj ^ (jj >> 1)) << 6) | lane] = make_uint4(v0, v1, v2, 0u);
+    }
+  }
+  __syncthreads();
+  gf128 y[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) y[j] = gf_load(&data[((q << 3) | (size_t)j) * D3_LANES + lane]);
+  // layer d-3: pairs (j, j + 4), one twiddle
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    y[j] = gf_add(y[j], d3_mul<3>(T.a, y[j + 4]));
+    y[j + 4] = gf_add(y[j + 4], y[j]);
+  }
+  // layer d-2: pairs (j, j + 2) in each half h, the prepared twiddle of half h
+  // (below 2^56: its low word's four masked parts, then one shifted copy of
+  // y per set bit of its high word)
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const gf128p* qq = &twq[i18 + h];
+    const uint4 m0 = qq->m[0], m1 = qq->m[1];
+    const uint32_t thi = m1.x | m1.y | m1.z | m1.w;
+#pragma unroll
+    for (int j = 4 * h; j < 4 * h + 2; j++) {
+      y[j] = gf_add(y[j], gf_mul_p40(y[j + 2], m0, thi));
+      y[j + 2] = gf_add(y[j + 2], y[j]);
+    }
+  }
+  // layer d-1: pairs (2 i, 2 i + 1), twiddle c[i]
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    y[2 * i] = gf_add(y[2 * i], d3_mul<1>(T.c[i], y[2 * i + 1]));
+    y[2 * i + 1] = gf_add(y[2 * i + 1], y[2 * i]);
+  }
+#pragma unroll
+  for (int j = 0; j < 8; j++) gf_store(&data[((q << 3) | (size_t)j) * D3_LANES + lane], y[j]);
+}
+
+// The deep-table pass in place on data (the caller checked deep3_applies).
+int run_deep3(gf128* data, const gf128* twp, const void* twq, int log_d, cudaStream_t st) {
+  ntt_deep3_kernel<<<(unsigned)((size_t)1 << (log_d - 3)), D3_LANES, 0, st>>>(data, twp, (const gf128p*)twq, log_d);
+  flock_count_launch();
+  return cudaGetLastError() == cudaSuccess ? FLOCK_OK : FLOCK_ERR_CUDA;
+}
+
 __global__ void prepare_twiddles_kernel(const gf128* __restrict__ tw, size_t n, gf128p* __restrict__ out) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     out[i] = gf_prepare(tw[i]);
@@ -579,11 +769,13 @@ const void* flock_ntt_twiddles_prepared(int log_d) {
 // buffer of the same shape (CUDA events on the caller's stream, one warm-up
 // and two timed runs per candidate): the table passes for each table depth of
 // kTabMinLogs, and the multiply passes of every pass shape from each depth's
-// end layer; it keeps the pair with the smallest sum for later calls. All
-// candidates compute identical results; only speed differs.
+// end layer, plus the deep-table pass where a depth leaves exactly the last
+// three layers of a 64-lane code; it keeps the pair with the smallest sum for
+// later calls. All candidates compute identical results; only speed differs.
 // FLOCK_NTT_TUNE=0 in the environment turns tuning off (the default depth and
-// shape everywhere); FLOCK_NTT_VARIANT=0|1|2 fixes the multiply-pass shape
-// (with the default depth).
+// shape everywhere); FLOCK_NTT_VARIANT=0|1|2|3 fixes the multiply-pass shape
+// (with the default depth; 3 falls back to shape 1 where the deep-table pass
+// does not apply).
 namespace {
 
 struct TuneKey {
@@ -658,6 +850,16 @@ TunedShape tune_shape(const TuneKey& k, const void* tw, const gf128* twp, cudaSt
         best = TunedShape{te, v};
       }
     }
+    // the deep-table pass, where the multiply part is exactly the last three layers
+    if (twp && deep3_applies(k.log_d, k.log_lanes, te)) {
+      const auto key = std::make_pair(te, kDeepVariant);
+      if (!mult_ms.count(key)) mult_ms[key] = time_of([&] { return run_deep3(d, twp, tw, k.log_d, st); });
+      const float t = tab_ms[te] + mult_ms[key];
+      if (t < best_ms) {
+        best_ms = t;
+        best = TunedShape{te, kDeepVariant};
+      }
+    }
   }
   cudaStreamSynchronize(st);
   cudaGetLastError();
@@ -671,7 +873,7 @@ TunedShape pick_shape(int log_d, int log_lanes, int start, const void* tw, const
   const TunedShape dflt{tab_layers_end(log_d, log_lanes, start), kDefaultVariant};
   if (const char* f = std::getenv("FLOCK_NTT_VARIANT")) {  // a fixed shape, for measurements
     const int v = f[0] - '0';
-    if (v >= 0 && v < kVariants) return TunedShape{dflt.tab_end, v};
+    if ((v >= 0 && v < kVariants) || v == kDeepVariant) return TunedShape{dflt.tab_end, v};
   }
   if (!tuning_enabled()) return dflt;
   TuneKey k{0, log_d, log_lanes, start};
@@ -746,6 +948,10 @@ int flock_launch_ntt(void* d_data, const void* d_src, int log_d, int log_lanes, 
     }
   }
   if (l == log_d) return FLOCK_OK;
+  if (sh.variant == kDeepVariant) {
+    if (src == data && deep3_applies(log_d, log_lanes, l)) return run_deep3(data, twp, tw, log_d, stream);
+    return run_passes<true>(kDefaultVariant, data, src, mask, tw, log_d, log_lanes, l, stream);
+  }
   return run_passes<true>(sh.variant, data, src, mask, tw, log_d, log_lanes, l, stream);
 }
 

@@ -91,8 +91,10 @@ int flock_ntt(flock_ctx* ctx, void* d_data, int log_d, int log_num_ntts, int sta
 
 /* The NTT autotuner's choice for a transform shape (2^log_d positions x
  * 2^log_lanes lanes from start_layer) on `device`, or -1 if that shape has not
- * run yet: the multiply-pass shape (0, 1, 2: 4, 8 or 16 positions per thread)
- * and the end layer of the byte-table passes (the upper layers run as
+ * run yet: the multiply-pass shape (0, 1, 2: 4, 8 or 16 positions per thread;
+ * 3: the deep-table pass, the last three layers of a 64-lane code through
+ * tables of its narrow twiddles' products) and the end layer of the
+ * byte-table passes (the upper layers run as
  * two-layer table passes while a block holds at least 2^k position-quads x
  * lanes, k tuned among 8, 9, 10; the layers from the end layer on run as
  * multiply passes). The first flock_ntt / commit / proof of a shape times the

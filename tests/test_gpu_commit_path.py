@@ -163,6 +163,22 @@ def test_ntt_every_pass_shape_matches_oracle(ctx, monkeypatch, variant, log_d, l
     assert np.array_equal(host(d).view(np.uint64), O.ntt_interleaved(data, 1 << log_lanes, start))
 
 
+# 64-lane codes whose table passes (default depth) end at layer log_d - 3, so
+# the deep-table pass takes the last three layers: from no table pass (4, 1)
+# to layer 13 of a 2^16-position transform.
+@pytest.mark.parametrize("log_d,start", [(4, 1), (7, 0), (9, 0), (12, 1), (13, 2), (16, 1)])
+def test_ntt_deep_table_pass_matches_oracle(ctx, monkeypatch, log_d, start):
+    """The last three layers through per-block tables of the narrow twiddles'
+    unreduced products (the pass shape FLOCK_NTT_VARIANT=3 fixes)."""
+    monkeypatch.setenv("FLOCK_NTT_VARIANT", "3")
+    rng = np.random.default_rng(log_d * 17 + start)
+    data = rng.integers(0, 2**63, (1 << (log_d + 6)) * 2, dtype=np.uint64)
+    data |= rng.integers(0, 2, data.shape, dtype=np.uint64) << np.uint64(63)
+    d = to_dev(data)
+    F.ntt(ctx, d, log_d, 6, start)
+    assert np.array_equal(host(d).view(np.uint64), O.ntt_interleaved(data, 64, start))
+
+
 def test_rate_quarter_256_columns_2e16_rows(ctx):
     """The kernel-microbench shape at its smallest stated size, 2^16 rows x 256
     columns (rate 1/4: 2^18 codeword positions, 1 GiB): columns are independent
