@@ -264,11 +264,35 @@ std::vector<hf::F> host_twiddles(int d) {
 std::mutex g_tw_mu;
 std::map<std::pair<int, int>, void*> g_tw;  // (device, log_d) -> device table
 
+// Bit width of every twiddle of layer `layer` of a 2^log_d transform (the OR of
+// the layer's generators bounds all its subset sums), cached per log_d.
+int twiddle_layer_width(int log_d, int layer) {
+  static std::mutex mu;
+  static std::map<int, std::vector<int>> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(log_d);
+  if (it == cache.end()) {
+    const std::vector<std::vector<hf::F>> ev = twiddle_rows(log_d);
+    std::vector<int> w(log_d, 0);
+    for (int l = 0; l < log_d; l++) {
+      uint64_t lo = 0, hi = 0;
+      const auto& row = ev[log_d - l - 1];
+      for (int bit = 0; bit < l; bit++) {
+        lo |= row[bit + 1].lo;
+        hi |= row[bit + 1].hi;
+      }
+      w[l] = hi ? 128 - __builtin_clzll(hi) : lo ? 64 - __builtin_clzll(lo) : 0;
+    }
+    it = cache.emplace(log_d, std::move(w)).first;
+  }
+  return it->second[layer];
+}
+
 // w32 | (w40 << 8) | (w64 << 16) | (w72 << 24): the first layers from which
 // every twiddle of a transform of 2^log_d positions is below 2^32, 2^40,
-// 2^64 and 2^72, read off the table (the normalized subspace polynomials of the deepest layers have
-// low degree: layer d-1 below 2^d, layer d-2 below 2^(2d-3), layer d-3 below
-// 2^69 at d = 20). Cached per log_d.
+// 2^64 and 2^72, read off the table (the normalized subspace polynomials of
+// the deepest layers have low degree: layer d-1 below 2^d, layer d-2 below
+// 2^(2d-3), layer d-3 below 2^69 at d = 20). Cached per log_d.
 constexpr int kMaxTwiddleClassLogD = 40;
 int flock_ntt_narrow_layers(int log_d) {
   static std::mutex mu;
@@ -276,24 +300,13 @@ int flock_ntt_narrow_layers(int log_d) {
   std::lock_guard<std::mutex> lk(mu);
   auto it = cache.find(log_d);
   if (it != cache.end()) return it->second;
-  // a bit is set in some subset sum of a layer's generators iff it is set in
-  // one of the generators, so the OR of the generators bounds the layer
-  const std::vector<std::vector<hf::F>> ev = twiddle_rows(log_d);
-  int w32 = log_d, w40 = log_d, w64 = log_d, w72 = log_d;
-  for (int layer = log_d - 1; layer >= 0; layer--) {
-    uint64_t or_lo = 0, or_hi = 0;
-    const auto& row = ev[log_d - layer - 1];
-    for (int bit = 0; bit < layer; bit++) {
-      or_lo |= row[bit + 1].lo;
-      or_hi |= row[bit + 1].hi;
-    }
-    if ((or_hi >> 8) != 0) break;
-    w72 = layer;
-    if (or_hi == 0 && w64 == layer + 1) w64 = layer;
-    if (or_hi == 0 && (or_lo >> 40) == 0 && w40 == layer + 1) w40 = layer;
-    if (or_hi == 0 && (or_lo >> 32) == 0 && w32 == layer + 1) w32 = layer;
-  }
-  return cache[log_d] = w32 | (w40 << 8) | (w64 << 16) | (w72 << 24);
+  // the first layer from which every deeper layer's twiddles fit `bits`
+  auto first_fit = [log_d](int bits) {
+    int w = log_d;
+    while (w > 0 && twiddle_layer_width(log_d, w - 1) <= bits) w--;
+    return w;
+  };
+  return cache[log_d] = first_fit(32) | (first_fit(40) << 8) | (first_fit(64) << 16) | (first_fit(72) << 24);
 }
 
 template <int F, bool PREP, int V>
@@ -549,30 +562,6 @@ struct Deep3Tabs {
   uint4 a[256];                // layer d-3: t v below 2^96 (three words used)
   uint32_t c[4][D3_C_STRIDE];  // layer d-1, twiddles of the four pairs: below 2^32
 };
-
-// Bit width of every twiddle of layer `layer` of a 2^log_d transform (the OR of
-// the layer's generators bounds all its subset sums), cached per log_d.
-int twiddle_layer_width(int log_d, int layer) {
-  static std::mutex mu;
-  static std::map<int, std::vector<int>> cache;
-  std::lock_guard<std::mutex> lk(mu);
-  auto it = cache.find(log_d);
-  if (it == cache.end()) {
-    const std::vector<std::vector<hf::F>> ev = twiddle_rows(log_d);
-    std::vector<int> w(log_d, 0);
-    for (int l = 0; l < log_d; l++) {
-      uint64_t lo = 0, hi = 0;
-      const auto& row = ev[log_d - l - 1];
-      for (int bit = 0; bit < l; bit++) {
-        lo |= row[bit + 1].lo;
-        hi |= row[bit + 1].hi;
-      }
-      w[l] = hi ? 128 - __builtin_clzll(hi) : lo ? 64 - __builtin_clzll(lo) : 0;
-    }
-    it = cache.emplace(log_d, std::move(w)).first;
-  }
-  return it->second[layer];
-}
 
 // The deep-table pass applies to the layers [from, log_d) of a code of
 // 2^log_lanes lanes.
